@@ -1,0 +1,172 @@
+/*
+ * rift_gb300.h -- C ABI of the GB300-native RIFT shallow-water step.
+ *
+ * The reference drives its device step through the C++ launcher set in
+ * grid.h:6-63 (SetDeviceConstants, AllocateGrid, InitGrid, ComputeFluxes,
+ * Integrate_1, Integrate_2, Grow, ApplyBoundaries, InterpGrid, FillGrid,
+ * SumReduce, FreeGrid) plus the dt reduction in simulator.cu:540-566
+ * (Simulator::ComputeTimestep) and the source hooks simulator.cu:891-907.
+ * Those launchers take raw FP64 pitched device pointers and keep their state
+ * in __constant__ symbols and host globals.  This header replaces that seam
+ * with an opaque handle: the handle owns every device buffer, one CUDA
+ * stream per handle, every call returns an int status (never exit()).
+ *
+ * Host arrays exchanged through this ABI use the reference's host layout:
+ * row-major FP64, h_ny rows of h_nx cells (the 2-cell ghost ring included),
+ * cell (j,i) at [j*ld + i].  BX is h_ny x (h_nx+1) (west face of cell i at
+ * column i), BY is (h_ny+1) x h_nx (south face of cell j at row j), as built
+ * by Simulator::InitSimulation (simulator.cu:384-431).
+ *
+ * Tiles are the reference's 16 x 14 cell blocks (grid.cu:18-19):
+ * nBX = ceil(h_nx/16), nBY = ceil(h_ny/14), tile id = bY*nBX + bX.
+ */
+#ifndef RIFT_GB300_H
+#define RIFT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define RIFT_OK            0
+#define RIFT_ERR_ARG       1  /* bad argument (null pointer, bad size, bad enum) */
+#define RIFT_ERR_CUDA      2  /* a CUDA runtime call failed; see rift_last_error */
+#define RIFT_ERR_STATE     3  /* call out of order (e.g. step before init) */
+#define RIFT_ERR_NUMERIC   4  /* device detected a non-finite or negative depth */
+#define RIFT_ERR_NOMEM     5  /* device allocation failed */
+#define RIFT_ERR_UNSUPPORTED 6
+
+/* ---- feature flags: the reference's __constant__ bools (grid.cu:21-25) -- */
+#define RIFT_F_RAIN_UNIFORM  (1u << 0)  /* rainfall_averaged: hyetograph CSV */
+#define RIFT_F_RAIN_GRID     (1u << 1)  /* rainfall_gridded: rain map series */
+#define RIFT_F_DRAIN_UNIFORM (1u << 2)  /* drain_averaged */
+#define RIFT_F_DRAIN_GRID    (1u << 3)  /* drain_gridded */
+#define RIFT_F_INFILTRATION  (1u << 4)  /* Green-Ampt (K, psi, dtheta) */
+#define RIFT_F_SURGE_GRID    (1u << 5)  /* surge_gridded */
+#define RIFT_F_EULER         (1u << 6)  /* euler_integration: stage 1 only */
+#define RIFT_F_SAVE_MAX      (1u << 7)  /* h_max, q_max (+ t_peak, t_dry in Euler mode) */
+#define RIFT_F_SAVE_ARRIVAL  (1u << 8)  /* t_wet */
+#define RIFT_F_TILE_ACCEL    (1u << 9)  /* tile_acceleration: skip dry tiles */
+#define RIFT_F_POINT_SOURCE  (1u << 10) /* dambreak: hydrograph point/rect source */
+#define RIFT_F_H_INIT        (1u << 11) /* h_init: initial depth map */
+
+/* ---- map slots for rift_set_map ---------------------------------------- */
+#define RIFT_MAP_RAIN  0  /* m/s, hyetograph_gridded_rate */
+#define RIFT_MAP_DRAIN 1  /* m/s, drain_gridded_rate */
+#define RIFT_MAP_SURGE 2  /* m,   surge_gridded_depth (nodata aware) */
+
+/* ---- field ids for rift_get_field -------------------------------------- */
+#define RIFT_FIELD_W     0   /* water-surface elevation (FP64, ghost ring included) */
+#define RIFT_FIELD_HU    1
+#define RIFT_FIELD_HV    2
+#define RIFT_FIELD_F     3   /* Green-Ampt cumulative infiltration */
+#define RIFT_FIELD_H     4   /* clamped depth map (dev_h, Integrate_2_k:1108-1111) */
+#define RIFT_FIELD_Q     5   /* unit discharge map (dev_q, Integrate_2_k:1113-1119) */
+#define RIFT_FIELD_HMAX  6
+#define RIFT_FIELD_QMAX  7
+#define RIFT_FIELD_TPEAK 8
+#define RIFT_FIELD_TDRY  9
+#define RIFT_FIELD_TWET  10
+#define RIFT_FIELD_BC    11  /* cell-centre bed elevation (InitGrid_k:532) */
+
+typedef struct rift_grid_desc {
+    int32_t  h_nx, h_ny;   /* cells incl. ghost ring; b_nx+3 (grid_config.cpp:84-85) */
+    double   dx, dy;       /* h_dx, h_dy in metres */
+    double   kappa;        /* desingularisation constant (simulator.cu:281) */
+    double   nodata;       /* GridConfig::nodata (-9999) */
+    double   courant;      /* courant_max (simulator.cu:61-72) */
+    double   psi, dtheta;  /* Green-Ampt suction head and moisture deficit */
+    uint32_t flags;        /* RIFT_F_* */
+    int32_t  device;       /* CUDA device ordinal */
+} rift_grid_desc;
+
+typedef struct rift_handle rift_handle;
+
+/* Replaces SetDeviceConstants (grid.cu:321) + AllocateGrid (grid.cu:347). */
+int rift_create(const rift_grid_desc* g, rift_handle** out);
+
+/* Replaces the H2D uploads of simulator.cu:433-450.  n and K are per-cell
+ * (h_ny x h_nx); K is already in m/s (simulator.cu:426).  h0 may be NULL. */
+int rift_upload_static(rift_handle* h, const double* BX, const double* BY,
+                       const double* n, const double* K_mps, const double* h0);
+
+/* Replaces InitGrid (grid.cu:556) followed by ApplyBoundaries (simulator.cu:731).
+ * Sets t = t0, dt_prev = 1e-7f (simulator.cu:35). */
+int rift_init(rift_handle* h, double t0);
+
+/* Uniform rain and drain rates for the next rift_step, m/s (the caller's
+ * Source::interpolated_rate after unit conversion, simulator.cu:500-538). */
+int rift_set_uniform_rates(rift_handle* h, double rain_mps, double drain_mps);
+
+/* Point / rectangular hydrograph source cells: flat indices j*h_nx+i and
+ * rates in m/s (Simulator::InitializeSources/setSourceValue,
+ * simulator.cu:858-907). */
+int rift_set_point_sources(rift_handle* h, const int32_t* idx,
+                           const double* rate_mps, int32_t n);
+
+/* Gridded map for the next step (GridSeries::update, GridSeries.cu:144-403).
+ * t1map == NULL: hold t0map.  Otherwise the map is
+ * InterpGrid(factor, t0map, t1map) (grid.cu:292-311), evaluated on device. */
+int rift_set_map(rift_handle* h, int32_t which, const double* t0map,
+                 const double* t1map, double factor);
+
+/* Only the interpolation factor changes (same t0/t1 maps). */
+int rift_set_map_factor(rift_handle* h, int32_t which, double factor);
+
+/* One full RK2 (or Euler) step, Grow included: the body of
+ * Simulator::RunSimulation (simulator.cu:773-853) from Grow to the last
+ * ApplyBoundaries.  Returns the new t and dt. */
+int rift_step(rift_handle* h, double* t, double* dt);
+
+/* Run nsteps steps on device without a host round trip (CUDA graph replay).
+ * Uniform rates / maps stay as last set.  Stops early once t >= t_stop. */
+int rift_run(rift_handle* h, int32_t nsteps, double t_stop, double* t,
+             double* dt, int32_t* steps_done);
+
+/* Device-resident uniform CSV series (Source::InterpolateRate,
+ * source.cc:65-73, with the in-place unit division of simulator.cu:500-538).
+ * which: 0 = hyetograph (mm/hr), 1 = drain (mm/hr), 2 = hydrograph (cfs,
+ * spread over the point-source cells).  times in seconds. */
+int rift_set_series(rift_handle* h, int32_t which, const float* times_s,
+                    const float* rates, int32_t n);
+
+/* Copy a field to host memory, h_ny rows with leading dimension ld. */
+int rift_get_field(rift_handle* h, int32_t which, double* host, size_t ld);
+
+/* Tile state in the reference encoding: wet flag per tile (GridSize bytes),
+ * the active tile ids sorted ascending, and their count. */
+int rift_get_tiles(rift_handle* h, uint8_t* wet, int32_t* active,
+                   int32_t* n_active);
+
+/* Per-tile local speed maxima mx/my (GridSize doubles each). */
+int rift_get_tile_speeds(rift_handle* h, double* mx, double* my);
+
+/* Hotstart-style state upload (Simulator::ReadHotstart, simulator.cu:975).
+ * active_ids (sorted ids of the active tiles, n_active of them), F, wet, mx
+ * and my may be NULL (n_active < 0 keeps the current active set). */
+int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w,
+                   const double* hu, const double* hv, const double* F,
+                   const uint8_t* wet, const int32_t* active_ids,
+                   int32_t n_active, const double* mx, const double* my);
+
+/* Current t and dt. */
+int rift_get_time(rift_handle* h, double* t, double* dt);
+
+/* FP64 compensated volume sum over interior cells of (h [+F]), m of depth
+ * summed (multiply by dx*dy for m^3) -- the device counterpart of the host
+ * volume check in simulator.cu:609-637. */
+int rift_volume(rift_handle* h, double* volume);
+
+/* Sizes: GridSize (tiles) and the tile grid. */
+int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
+
+const char* rift_last_error(rift_handle* h);
+void rift_destroy(rift_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RIFT_GB300_H */

@@ -1,0 +1,269 @@
+"""ctypes binding of the C ABI declared in include/rift_gb300.h.
+
+`Sim` drives any library that exports that ABI under a symbol prefix (the
+CUDA engine exports it as "rift_*").  A library whose create call takes an
+extra int32 mode argument is bound with `create_has_mode=True`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "librift_gb300.so")
+
+RIFT_OK = 0
+ERRORS = {1: "bad argument", 2: "CUDA error", 3: "call out of order", 4: "numeric fault",
+          5: "out of device memory", 6: "unsupported"}
+
+FIELD = dict(W=0, HU=1, HV=2, F=3, H=4, Q=5, HMAX=6, QMAX=7, TPEAK=8, TDRY=9, TWET=10, BC=11)
+MAP = dict(RAIN=0, DRAIN=1, SURGE=2)
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("h_nx", C.c_int32), ("h_ny", C.c_int32), ("dx", C.c_double), ("dy", C.c_double),
+                ("kappa", C.c_double), ("nodata", C.c_double), ("courant", C.c_double),
+                ("psi", C.c_double), ("dtheta", C.c_double), ("flags", C.c_uint32),
+                ("device", C.c_int32)]
+
+
+class RiftError(RuntimeError):
+    pass
+
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_F = C.POINTER(C.c_float)
+_I = C.POINTER(C.c_int32)
+_U8 = C.POINTER(C.c_uint8)
+
+
+def _sig(lib, name, res, args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = args
+    return f
+
+
+def exported_symbols():
+    """Entry points of include/rift_gb300.h (without the prefix)."""
+    return ["create", "upload_static", "init", "set_uniform_rates", "set_point_sources",
+            "set_map", "set_map_factor", "step", "run", "set_series", "get_field", "get_tiles",
+            "get_tile_speeds", "set_state", "get_time", "volume", "get_tile_grid", "last_error",
+            "destroy"]
+
+
+def bind(lib, prefix: str, create_has_mode: bool = False):
+    """Attach argtypes/restype for every ABI entry point; returns a namespace."""
+    p = prefix
+    ns = {}
+    if create_has_mode:
+        ns["create"] = _sig(lib, p + "create", C.c_int, [C.POINTER(GridDesc), C.c_int32, C.POINTER(_P)])
+    else:
+        ns["create"] = _sig(lib, p + "create", C.c_int, [C.POINTER(GridDesc), C.POINTER(_P)])
+    ns["upload_static"] = _sig(lib, p + "upload_static", C.c_int, [_P, _D, _D, _D, _D, _D])
+    ns["init"] = _sig(lib, p + "init", C.c_int, [_P, C.c_double])
+    ns["set_uniform_rates"] = _sig(lib, p + "set_uniform_rates", C.c_int, [_P, C.c_double, C.c_double])
+    ns["set_point_sources"] = _sig(lib, p + "set_point_sources", C.c_int, [_P, _I, _D, C.c_int32])
+    ns["set_map"] = _sig(lib, p + "set_map", C.c_int, [_P, C.c_int32, _D, _D, C.c_double])
+    ns["set_map_factor"] = _sig(lib, p + "set_map_factor", C.c_int, [_P, C.c_int32, C.c_double])
+    ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
+    ns["step"] = _sig(lib, p + "step", C.c_int, [_P, _D, _D])
+    ns["run"] = _sig(lib, p + "run", C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _I])
+    ns["get_field"] = _sig(lib, p + "get_field", C.c_int, [_P, C.c_int32, _D, C.c_size_t])
+    ns["get_tiles"] = _sig(lib, p + "get_tiles", C.c_int, [_P, _U8, _I, _I])
+    ns["get_tile_speeds"] = _sig(lib, p + "get_tile_speeds", C.c_int, [_P, _D, _D])
+    ns["set_state"] = _sig(lib, p + "set_state", C.c_int,
+                           [_P, C.c_double, C.c_double, _D, _D, _D, _D, _U8, _I, C.c_int32, _D, _D])
+    ns["get_time"] = _sig(lib, p + "get_time", C.c_int, [_P, _D, _D])
+    ns["volume"] = _sig(lib, p + "volume", C.c_int, [_P, _D])
+    ns["get_tile_grid"] = _sig(lib, p + "get_tile_grid", C.c_int, [_P, _I, _I])
+    ns["last_error"] = _sig(lib, p + "last_error", C.c_char_p, [_P])
+    ns["destroy"] = _sig(lib, p + "destroy", None, [_P])
+    return ns
+
+
+def _dp(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_D)
+
+
+_product = None
+
+
+def load_product():
+    """Load the in-tree CUDA library.  Fails loudly when it is missing: there
+    is no CPU fallback on the product path."""
+    global _product
+    if _product is None:
+        if not os.path.exists(LIB_PATH):
+            raise RiftError(f"CUDA extension not built: {LIB_PATH} missing (run build())")
+        lib = C.CDLL(LIB_PATH)
+        _product = (lib, bind(lib, "rift_"))
+    return _product
+
+
+class Sim:
+    """One simulation handle behind the C ABI."""
+
+    def __init__(self, case, api=None, create_mode=None, device=0):
+        if api is None:
+            api = load_product()
+        self.lib, self.f = api
+        self.case = case
+        self.nx, self.ny = case.h_nx, case.h_ny
+        d = GridDesc(case.h_nx, case.h_ny, case.cell, case.cell, case.kappa, -9999.0,
+                     case.courant, case.psi, case.dtheta, case.flags, device)
+        self._desc = d
+        h = _P()
+        if create_mode is None:
+            rc = self.f["create"](C.byref(d), C.byref(h))
+        else:
+            rc = self.f["create"](C.byref(d), create_mode, C.byref(h))
+        self._check(rc, "create", h)
+        self.h = h
+        nbx, nby = C.c_int32(), C.c_int32()
+        self._check(self.f["get_tile_grid"](h, C.byref(nbx), C.byref(nby)), "get_tile_grid")
+        self.nBX, self.nBY = nbx.value, nby.value
+        self.grid_size = self.nBX * self.nBY
+
+    def _check(self, rc, what, h=None):
+        if rc != RIFT_OK:
+            msg = ""
+            hh = h if h is not None else getattr(self, "h", None)
+            if hh:
+                m = self.f["last_error"](hh)
+                msg = m.decode() if m else ""
+            raise RiftError(f"{what} failed: {ERRORS.get(rc, rc)} {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.f["destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- setup ------------------------------------------------------------
+    def upload(self):
+        c = self.case
+        BX, BY = c.faces()
+        BX = np.ascontiguousarray(BX, dtype=np.float64)
+        BY = np.ascontiguousarray(BY, dtype=np.float64)
+        n = np.ascontiguousarray(c.n, dtype=np.float64)
+        K = None if c.K is None else np.ascontiguousarray(c.K, dtype=np.float64)
+        h0 = None if c.h0 is None else np.ascontiguousarray(c.h0, dtype=np.float64)
+        self._keep = (BX, BY, n, K, h0)
+        self._check(self.f["upload_static"](self.h, _dp(BX), _dp(BY), _dp(n), _dp(K), _dp(h0)),
+                    "upload_static")
+        for which, (t, r) in c.series.items():
+            self.set_series(which, t, r)
+        if c.src_idx is not None:
+            idx = np.ascontiguousarray(c.src_idx, dtype=np.int32)
+            rate = np.zeros(len(idx))
+            self.set_point_sources(idx, rate)
+        return self
+
+    def init(self, t0=None):
+        self._check(self.f["init"](self.h, self.case.t0 if t0 is None else t0), "init")
+        return self
+
+    def setup(self):
+        return self.upload().init()
+
+    def set_series(self, which, times, rates):
+        t = np.ascontiguousarray(times, dtype=np.float32)
+        r = np.ascontiguousarray(rates, dtype=np.float32)
+        self._check(self.f["set_series"](self.h, which, t.ctypes.data_as(_F), r.ctypes.data_as(_F),
+                                         len(t)), "set_series")
+
+    def set_uniform_rates(self, rain, drain):
+        self._check(self.f["set_uniform_rates"](self.h, rain, drain), "set_uniform_rates")
+
+    def set_point_sources(self, idx, rate):
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        rate = np.ascontiguousarray(rate, dtype=np.float64)
+        self._check(self.f["set_point_sources"](self.h, idx.ctypes.data_as(_I), _dp(rate), len(idx)),
+                    "set_point_sources")
+
+    def set_map(self, which, t0, t1=None, factor=0.0):
+        a0 = np.ascontiguousarray(t0, dtype=np.float64)
+        a1 = None if t1 is None else np.ascontiguousarray(t1, dtype=np.float64)
+        self._check(self.f["set_map"](self.h, which, _dp(a0), _dp(a1), factor), "set_map")
+
+    def set_map_factor(self, which, factor):
+        self._check(self.f["set_map_factor"](self.h, which, factor), "set_map_factor")
+
+    # -- stepping ---------------------------------------------------------
+    def step(self):
+        t, dt = C.c_double(), C.c_double()
+        self._check(self.f["step"](self.h, C.byref(t), C.byref(dt)), "step")
+        return t.value, dt.value
+
+    def run(self, nsteps, t_stop=float("inf")):
+        t, dt, k = C.c_double(), C.c_double(), C.c_int32()
+        self._check(self.f["run"](self.h, nsteps, t_stop, C.byref(t), C.byref(dt), C.byref(k)), "run")
+        return t.value, dt.value, k.value
+
+    # -- readback ---------------------------------------------------------
+    def field(self, name):
+        out = np.zeros((self.ny, self.nx))
+        self._check(self.f["get_field"](self.h, FIELD[name], _dp(out), self.nx), f"get_field {name}")
+        return out
+
+    def tiles(self):
+        wet = np.zeros(self.grid_size, dtype=np.uint8)
+        act = np.zeros(self.grid_size, dtype=np.int32)
+        n = C.c_int32()
+        self._check(self.f["get_tiles"](self.h, wet.ctypes.data_as(_U8), act.ctypes.data_as(_I),
+                                        C.byref(n)), "get_tiles")
+        return wet, act[: n.value].copy()
+
+    def tile_speeds(self):
+        mx = np.zeros(self.grid_size)
+        my = np.zeros(self.grid_size)
+        self._check(self.f["get_tile_speeds"](self.h, _dp(mx), _dp(my)), "get_tile_speeds")
+        return mx, my
+
+    def time(self):
+        t, dt = C.c_double(), C.c_double()
+        self._check(self.f["get_time"](self.h, C.byref(t), C.byref(dt)), "get_time")
+        return t.value, dt.value
+
+    def volume(self):
+        v = C.c_double()
+        self._check(self.f["volume"](self.h, C.byref(v)), "volume")
+        return v.value
+
+    def set_state(self, t, dt_prev, w, hu, hv, F=None, wet=None, active=None, mx=None, my=None):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None
+                for a in (w, hu, hv, F, mx, my)]
+        w_, hu_, hv_, F_, mx_, my_ = arrs
+        wet_ = None if wet is None else np.ascontiguousarray(wet, dtype=np.uint8)
+        act_ = None if active is None else np.ascontiguousarray(active, dtype=np.int32)
+        self._check(self.f["set_state"](
+            self.h, t, dt_prev, _dp(w_), _dp(hu_), _dp(hv_), _dp(F_),
+            None if wet_ is None else wet_.ctypes.data_as(_U8),
+            None if act_ is None else act_.ctypes.data_as(_I),
+            -1 if act_ is None else len(act_), _dp(mx_), _dp(my_)), "set_state")
+
+    def snapshot(self):
+        """Everything needed to restart the step bit-for-bit."""
+        t, dt = self.time()
+        wet, act = self.tiles()
+        mx, my = self.tile_speeds()
+        snap = dict(t=t, dt=dt, w=self.field("W"), hu=self.field("HU"), hv=self.field("HV"),
+                    wet=wet, active=act, mx=mx, my=my)
+        if self.case.flags & 16:
+            snap["F"] = self.field("F")
+        return snap
+
+    def load_snapshot(self, s):
+        self.set_state(s["t"], s["dt"], s["w"], s["hu"], s["hv"], s.get("F"), s["wet"],
+                       s["active"], s["mx"], s["my"])

@@ -1,0 +1,859 @@
+// rift_engine.cu -- host engine and C ABI (include/rift_gb300.h) of the GB300
+// RIFT step.  The handle owns every device buffer and one CUDA stream; the
+// per-step launch sequence is captured once into a CUDA graph and replayed.
+//
+// Device layout (FP32, pitched, ghost ring included, cell (j,i) at column i
+// of row j):
+//   A, B   [3][rows][pitch]  depth h, hu, hv  (U^n / U*; double-buffered so
+//                            no CTA reads a cell another CTA is writing)
+//   E      [4][rows][pitch]  eW, eE, eS, eN: face elevation minus the cell's
+//                            reference elevation, differenced in FP64
+//   nman, K, FA, FB, hmax, qmax, twet, tpeak, tdry, maps  [rows][pitch]
+// Host keeps the FP64 reference elevation of every cell to rebuild
+// w = Bref + h at output.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/rift_gb300.h"
+#include "rift_kernels.cuh"
+
+using namespace rift;
+
+namespace {
+
+typedef CUresult (*PFN_encodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                    const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+PFN_encodeTiled getEncodeTiled() {
+    static PFN_encodeTiled fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_encodeTiled)p;
+    }
+    return fn;
+}
+
+}  // namespace
+
+struct rift_handle {
+    rift_grid_desc g{};
+    int nx = 0, ny = 0, nBX = 0, nBY = 0, gridSize = 0, pitch = 0, rows = 0;
+    int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0;
+    cudaStream_t stream = nullptr;
+    float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
+    float *FA = nullptr, *FB = nullptr, *hmax = nullptr, *qmax = nullptr, *twet = nullptr;
+    float *tpeak = nullptr, *tdry = nullptr;
+    float* maps[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    int mapMode[3] = {0, 0, 0};
+    uint8_t *wet = nullptr, *prevAct = nullptr;
+    int *act = nullptr, *deact = nullptr, *inact = nullptr;
+    float *mx = nullptr, *my = nullptr;
+    int* srcIdx = nullptr;
+    float* srcRate = nullptr;
+    int *srcTileStart = nullptr, *srcTileList = nullptr;
+    int nsrc = 0;
+    float *serT = nullptr, *serR = nullptr;
+    int serN[3] = {0, 0, 0};
+    DevState* st = nullptr;
+    DevState* hst = nullptr;  // pinned mirror
+    double* volPartial = nullptr;
+    CUtensorMap tmA{}, tmB{}, tmE{};
+    std::vector<double> Bref, BC, h0_;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    bool haveStatic = false, inited = false;
+    std::string err;
+
+    bool has(uint32_t f) const { return (g.flags & f) != 0; }
+    size_t plane() const { return (size_t)rows * pitch; }
+};
+
+namespace {
+
+int fail(rift_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+#define CUDA_TRY(h, call)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? RIFT_ERR_NOMEM : RIFT_ERR_CUDA, \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+Params makeParams(rift_handle* h) {
+    Params P{};
+    P.nx = h->nx;
+    P.ny = h->ny;
+    P.nBX = h->nBX;
+    P.nBY = h->nBY;
+    P.gridSize = h->gridSize;
+    P.pitch = h->pitch;
+    P.rows = h->rows;
+    P.dx = (float)h->g.dx;
+    P.dy = (float)h->g.dy;
+    P.inv_dx = (float)(1.0 / h->g.dx);
+    P.inv_dy = (float)(1.0 / h->g.dy);
+    P.kappa = (float)h->g.kappa;
+    P.psiDtheta = (float)(h->g.psi * h->g.dtheta);
+    P.nodata = (float)h->g.nodata;
+    P.dxd = h->g.dx;
+    P.dyd = h->g.dy;
+    P.kappad = h->g.kappa;
+    P.courant = h->g.courant;
+    P.flags = h->g.flags;
+    P.A = h->A;
+    P.B = h->B;
+    P.E = h->E;
+    P.nman = h->nman;
+    P.K = h->K;
+    P.FA = h->FA;
+    P.FB = h->FB;
+    P.hmax = h->hmax;
+    P.qmax = h->qmax;
+    P.twet = h->twet;
+    P.tpeak = h->tpeak;
+    P.tdry = h->tdry;
+    for (int k = 0; k < 3; k++) {
+        P.map0[k] = h->maps[k][0];
+        P.map1[k] = h->maps[k][1];
+        P.mapMode[k] = h->mapMode[k];
+    }
+    P.wet = h->wet;
+    P.prevAct = h->prevAct;
+    P.act = h->act;
+    P.deact = h->deact;
+    P.inact = h->inact;
+    P.mx = h->mx;
+    P.my = h->my;
+    P.srcIdx = h->srcIdx;
+    P.srcRate = h->srcRate;
+    P.srcTileStart = h->srcTileStart;
+    P.srcTileList = h->srcTileList;
+    P.nsrc = h->nsrc;
+    P.serT = h->serT;
+    P.serR = h->serR;
+    for (int k = 0; k < 3; k++) P.serN[k] = h->serN[k];
+    P.st = h->st;
+    return P;
+}
+
+int encodeMap(rift_handle* h, CUtensorMap* tm, float* base, int nfields) {
+    PFN_encodeTiled enc = getEncodeTiled();
+    if (!enc) return fail(h, RIFT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->rows, (cuuint64_t)nfields};
+    cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)h->plane() * 4};
+    cuuint32_t box[3] = {(cuuint32_t)SW, (cuuint32_t)SH, (cuuint32_t)nfields};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                     CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(h, RIFT_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    return RIFT_OK;
+}
+
+void destroyGraph(rift_handle* h) {
+    if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->graphExec = nullptr;
+    h->graph = nullptr;
+}
+
+// The launch sequence of one step (captured into the graph).
+void enqueueStep(rift_handle* h) {
+    Params P = makeParams(h);
+    cudaStream_t s = h->stream;
+    k_begin<<<1, 32, 0, s>>>(P);
+    if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
+        k_track<<<h->gridTrack, NT, 0, s>>>(P);
+    k_grow<<<1, GROW_T, 0, s>>>(P);
+    k_speed<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
+    k_dt<<<h->gridDt, 256, 0, s>>>(P);
+    k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
+    if (!h->has(RIFT_F_EULER)) k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
+}
+
+int buildGraph(rift_handle* h) {
+    if (h->graphExec) return RIFT_OK;
+    CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueueStep(h);
+    cudaError_t e = cudaStreamEndCapture(h->stream, &h->graph);
+    if (e != cudaSuccess) return fail(h, RIFT_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+    CUDA_TRY(h, cudaGraphInstantiate(&h->graphExec, h->graph, 0));
+    return RIFT_OK;
+}
+
+int pullState(rift_handle* h) {
+    CUDA_TRY(h, cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (h->hst->error) return fail(h, RIFT_ERR_CUDA, "device wait timed out (TMA barrier)");
+    return RIFT_OK;
+}
+
+int pushState(rift_handle* h) {
+    CUDA_TRY(h, cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
+inline size_t hidx(const rift_handle* h, int j, int i) { return (size_t)j * h->nx + i; }
+
+// Reference elevation per cell: the cell's own BC in the interior, the BC of
+// the interior cell a ghost copies from (ApplyBoundaries writes
+// w_ghost = BC_interior + H), and for the four corner blocks the value the
+// reference leaves there (InitGrid_k sets w = BC for i,j >= 2, else 0).
+void buildReference(rift_handle* h, const double* BX, const double* BY) {
+    const int nx = h->nx, ny = h->ny;
+    h->BC.assign((size_t)nx * ny, 0.0);
+    h->Bref.assign((size_t)nx * ny, 0.0);
+    auto bx = [&](int j, int i) { return BX[(size_t)j * (nx + 1) + i]; };
+    auto by = [&](int j, int i) { return BY[(size_t)j * nx + i]; };
+    for (int j = 2; j < ny; j++)
+        for (int i = 2; i < nx; i++)  // InitGrid_k:532
+            h->BC[hidx(h, j, i)] = 0.25 * (bx(j, i + 1) + bx(j, i) + by(j + 1, i) + by(j, i));
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            bool xin = i >= 2 && i <= nx - 3, yin = j >= 2 && j <= ny - 3;
+            double r;
+            if (xin && yin)
+                r = h->BC[hidx(h, j, i)];
+            else if (yin)
+                r = h->BC[hidx(h, j, i < 2 ? 2 : nx - 3)];
+            else if (xin)
+                r = h->BC[hidx(h, j < 2 ? 2 : ny - 3, i)];
+            else
+                r = h->BC[hidx(h, j, i)];
+            h->Bref[hidx(h, j, i)] = r;
+        }
+}
+
+float depthFromW(const rift_handle* h, double w, int j, int i) {
+    return (float)(w - h->Bref[hidx(h, j, i)]);
+}
+
+// Critical-depth ghosts on the host (init / state upload), same rule as the
+// device writeGhosts.
+void hostGhosts(rift_handle* h, std::vector<float>& H, std::vector<float>& U,
+                std::vector<float>& V) {
+    const int nx = h->nx, ny = h->ny;
+    auto crit = [](float q, float d) { return std::fmin(std::cbrt(q * q / kG), d); };
+    for (int j = 2; j <= ny - 3; j++) {
+        for (int side = 0; side < 2; side++) {
+            int ii = side ? nx - 3 : 2;
+            size_t c = hidx(h, j, ii);
+            float HL = crit(U[c], H[c]);
+            HL = (HL > kEps) ? HL : 0.f;
+            int g0 = side ? nx - 2 : 0, g1 = side ? nx - 1 : 1;
+            for (int gi : {g0, g1}) {
+                size_t q = hidx(h, j, gi);
+                H[q] = HL;
+                U[q] = U[c];
+                V[q] = V[c];
+            }
+        }
+    }
+    for (int i = 2; i <= nx - 3; i++) {
+        for (int side = 0; side < 2; side++) {
+            int jj = side ? ny - 3 : 2;
+            size_t c = hidx(h, jj, i);
+            float HB = crit(V[c], H[c]);
+            int g0 = side ? ny - 2 : 0, g1 = side ? ny - 1 : 1;
+            for (int gj : {g0, g1}) {
+                size_t q = hidx(h, gj, i);
+                H[q] = HB;
+                U[q] = U[c];
+                V[q] = V[c];
+            }
+        }
+    }
+}
+
+int upField(rift_handle* h, float* dev, const std::vector<float>& host) {
+    CUDA_TRY(h, cudaMemcpy2DAsync(dev, (size_t)h->pitch * 4, host.data(), (size_t)h->nx * 4,
+                                  (size_t)h->nx * 4, h->ny, cudaMemcpyHostToDevice, h->stream));
+    return RIFT_OK;
+}
+
+int downField(rift_handle* h, const float* dev, std::vector<float>& host) {
+    host.resize((size_t)h->nx * h->ny);
+    CUDA_TRY(h, cudaMemcpy2DAsync(host.data(), (size_t)h->nx * 4, dev, (size_t)h->pitch * 4,
+                                  (size_t)h->nx * 4, h->ny, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
+bool tileInGrid(const rift_handle* h, int b) {
+    int i0 = (b % h->nBX) * TW + 2, j0 = (b / h->nBX) * TH + 2;
+    return i0 < h->nx && j0 < h->ny;
+}
+
+// Upload U (A and B), tile flags and lists.
+int uploadState(rift_handle* h, const std::vector<float>& H, const std::vector<float>& U,
+                const std::vector<float>& V, const std::vector<uint8_t>& wet,
+                const std::vector<uint8_t>& activeFlags, const std::vector<int>& inactList) {
+    const size_t pl = h->plane();
+    int r;
+    if ((r = upField(h, h->A, H)) || (r = upField(h, h->A + pl, U)) ||
+        (r = upField(h, h->A + 2 * pl, V)))
+        return r;
+    CUDA_TRY(h, cudaMemcpyAsync(h->B, h->A, 3 * pl * 4, cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->wet, wet.data(), h->gridSize, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->prevAct, activeFlags.data(), h->gridSize,
+                                cudaMemcpyHostToDevice, h->stream));
+    if (!inactList.empty())
+        CUDA_TRY(h, cudaMemcpyAsync(h->inact, inactList.data(), inactList.size() * 4,
+                                    cudaMemcpyHostToDevice, h->stream));
+    h->hst->nInact = (int)inactList.size();
+    return RIFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rift_create(const rift_grid_desc* g, rift_handle** out) {
+    if (!g || !out) return RIFT_ERR_ARG;
+    *out = nullptr;
+    if (g->h_nx < 5 || g->h_ny < 5 || !(g->dx > 0) || !(g->dy > 0) || !(g->kappa > 0) ||
+        !(g->courant > 0))
+        return RIFT_ERR_ARG;
+    rift_handle* h = new rift_handle();
+    h->g = *g;
+    h->nx = g->h_nx;
+    h->ny = g->h_ny;
+    h->nBX = (h->nx + TW - 1) / TW;
+    h->nBY = (h->ny + TH - 1) / TH;
+    h->gridSize = h->nBX * h->nBY;
+    // every staged block (columns 16bX .. 16bX+19, rows 14bY .. 14bY+17) lies
+    // inside the allocation
+    h->pitch = ((h->nBX * TW + 8) + 31) / 32 * 32;
+    h->rows = h->nBY * TH + 4;
+    *out = h;
+    cudaError_t e = cudaSetDevice(g->device);
+    if (e != cudaSuccess) return fail(h, RIFT_ERR_CUDA, cudaGetErrorString(e));
+    int dev = g->device;
+    cudaDeviceGetAttribute(&h->numSMs, cudaDevAttrMultiProcessorCount, dev);
+    CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    const size_t pl = h->plane() * 4;
+    CUDA_TRY(h, cudaMalloc(&h->A, 3 * pl));
+    CUDA_TRY(h, cudaMalloc(&h->B, 3 * pl));
+    CUDA_TRY(h, cudaMalloc(&h->E, 4 * pl));
+    CUDA_TRY(h, cudaMalloc(&h->nman, pl));
+    CUDA_TRY(h, cudaMemset(h->A, 0, 3 * pl));
+    CUDA_TRY(h, cudaMemset(h->B, 0, 3 * pl));
+    CUDA_TRY(h, cudaMemset(h->E, 0, 4 * pl));
+    CUDA_TRY(h, cudaMemset(h->nman, 0, pl));
+    auto opt = [&](float*& p, bool on) -> int {
+        if (!on) return RIFT_OK;
+        CUDA_TRY(h, cudaMalloc(&p, pl));
+        CUDA_TRY(h, cudaMemset(p, 0, pl));
+        return RIFT_OK;
+    };
+    int r;
+    if ((r = opt(h->K, h->has(RIFT_F_INFILTRATION))) || (r = opt(h->FA, h->has(RIFT_F_INFILTRATION))) ||
+        (r = opt(h->FB, h->has(RIFT_F_INFILTRATION))) || (r = opt(h->hmax, h->has(RIFT_F_SAVE_MAX))) ||
+        (r = opt(h->qmax, h->has(RIFT_F_SAVE_MAX))) ||
+        (r = opt(h->tpeak, h->has(RIFT_F_SAVE_MAX))) || (r = opt(h->tdry, h->has(RIFT_F_SAVE_MAX))) ||
+        (r = opt(h->twet, h->has(RIFT_F_SAVE_ARRIVAL))))
+        return r;
+    const int G = h->gridSize;
+    CUDA_TRY(h, cudaMalloc(&h->wet, G));
+    CUDA_TRY(h, cudaMalloc(&h->prevAct, G));
+    CUDA_TRY(h, cudaMalloc(&h->act, (size_t)G * 4));
+    CUDA_TRY(h, cudaMalloc(&h->deact, (size_t)G * 4));
+    CUDA_TRY(h, cudaMalloc(&h->inact, (size_t)G * 4));
+    CUDA_TRY(h, cudaMalloc(&h->mx, (size_t)G * 4));
+    CUDA_TRY(h, cudaMalloc(&h->my, (size_t)G * 4));
+    CUDA_TRY(h, cudaMemset(h->wet, 0, G));
+    CUDA_TRY(h, cudaMemset(h->prevAct, 0, G));
+    CUDA_TRY(h, cudaMemset(h->mx, 0, (size_t)G * 4));
+    CUDA_TRY(h, cudaMemset(h->my, 0, (size_t)G * 4));
+    CUDA_TRY(h, cudaMalloc(&h->srcTileStart, ((size_t)G + 1) * 4));
+    CUDA_TRY(h, cudaMemset(h->srcTileStart, 0, ((size_t)G + 1) * 4));
+    CUDA_TRY(h, cudaMalloc(&h->serT, 3 * MAX_SERIES * 4));
+    CUDA_TRY(h, cudaMalloc(&h->serR, 3 * MAX_SERIES * 4));
+    CUDA_TRY(h, cudaMalloc(&h->st, sizeof(DevState)));
+    CUDA_TRY(h, cudaMallocHost(&h->hst, sizeof(DevState)));
+    std::memset(h->hst, 0, sizeof(DevState));
+    CUDA_TRY(h, cudaMalloc(&h->volPartial, 2 * 1024 * sizeof(double)));
+    if ((r = encodeMap(h, &h->tmA, h->A, 3)) || (r = encodeMap(h, &h->tmB, h->B, 3)) ||
+        (r = encodeMap(h, &h->tmE, h->E, 4)))
+        return r;
+    int occ = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_stage<1>, NT, 0);
+    if (occ < 1) occ = 1;
+    h->gridStage = std::max(1, std::min(G, h->numSMs * occ));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_speed, NT, 0);
+    if (occ < 1) occ = 1;
+    h->gridSpeed = std::max(1, std::min(G, h->numSMs * occ));
+    h->gridTrack = std::max(1, std::min(G, h->numSMs * 4));
+    h->gridDt = std::max(1, std::min((G + 255) / 256, h->numSMs * 2));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
+int rift_upload_static(rift_handle* h, const double* BX, const double* BY, const double* n,
+                       const double* K_mps, const double* h0) {
+    if (!h || !BX || !BY || !n) return RIFT_ERR_ARG;
+    if (h->has(RIFT_F_INFILTRATION) && !K_mps) return fail(h, RIFT_ERR_ARG, "K required");
+    const int nx = h->nx, ny = h->ny;
+    buildReference(h, BX, BY);
+    auto bx = [&](int j, int i) { return BX[(size_t)j * (nx + 1) + i]; };
+    auto by = [&](int j, int i) { return BY[(size_t)j * nx + i]; };
+    std::vector<float> e[4];
+    for (auto& v : e) v.assign((size_t)nx * ny, 0.f);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            size_t c = hidx(h, j, i);
+            double r = h->Bref[c];
+            e[0][c] = (float)(bx(j, i) - r);
+            e[1][c] = (float)(bx(j, i + 1) - r);
+            e[2][c] = (float)(by(j, i) - r);
+            e[3][c] = (float)(by(j + 1, i) - r);
+        }
+    int rc;
+    for (int f = 0; f < 4; f++)
+        if ((rc = upField(h, h->E + f * h->plane(), e[f]))) return rc;
+    std::vector<float> tmp((size_t)nx * ny);
+    for (size_t c = 0; c < tmp.size(); c++) tmp[c] = (float)n[c];
+    if ((rc = upField(h, h->nman, tmp))) return rc;
+    if (h->K) {
+        for (size_t c = 0; c < tmp.size(); c++) tmp[c] = (float)K_mps[c];
+        if ((rc = upField(h, h->K, tmp))) return rc;
+    }
+    h->h0_.assign(h0 ? h0 : nullptr, h0 ? h0 + (size_t)nx * ny : nullptr);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->haveStatic = true;
+    return RIFT_OK;
+}
+
+
+// InitGrid (grid.cu:506-553) then ApplyBoundaries (simulator.cu:731):
+// h = h0 (or 0), hu = hv = 0, every in-grid tile wet and active.
+int rift_init(rift_handle* h, double t0) {
+    if (!h) return RIFT_ERR_ARG;
+    if (!h->haveStatic) return fail(h, RIFT_ERR_STATE, "upload_static first");
+    const int nx = h->nx, ny = h->ny;
+    const size_t N = (size_t)nx * ny;
+    std::vector<float> H(N, 0.f), U(N, 0.f), V(N, 0.f);
+    if (h->has(RIFT_F_H_INIT) && !h->h0_.empty())
+        for (int j = 2; j < ny; j++)
+            for (int i = 2; i < nx; i++) H[hidx(h, j, i)] = (float)h->h0_[hidx(h, j, i)];
+    hostGhosts(h, H, U, V);
+    std::vector<uint8_t> wet(h->gridSize), actf(h->gridSize);
+    bool anyOut = false;
+    for (int b = 0; b < h->gridSize; b++) {
+        bool in = tileInGrid(h, b);
+        wet[b] = actf[b] = in ? 1 : 0;
+        if (!in) anyOut = true;
+    }
+    // before the first Grow the only negative active_blocks entries are the
+    // -1 fills of tiles InitGrid_k never reached; TrackRainfall_k maps them
+    // all to tile abs(-1) = 1
+    std::vector<int> inact;
+    if (anyOut && h->gridSize > 1) inact.push_back(1);
+    // rates and map factors set before init survive it
+    float keepF[3] = {h->hst->factor[0], h->hst->factor[1], h->hst->factor[2]};
+    float keepRain = h->hst->rain_rate, keepDrain = h->hst->drain_rate;
+    std::memset(h->hst, 0, sizeof(DevState));
+    for (int k = 0; k < 3; k++) h->hst->factor[k] = keepF[k];
+    h->hst->rain_rate = keepRain;
+    h->hst->drain_rate = keepDrain;
+    int rc = uploadState(h, H, U, V, wet, actf, inact);
+    if (rc) return rc;
+    const size_t pl = h->plane() * 4;
+    if (h->FA) {
+        CUDA_TRY(h, cudaMemsetAsync(h->FA, 0, pl, h->stream));
+        CUDA_TRY(h, cudaMemsetAsync(h->FB, 0, pl, h->stream));
+    }
+    if (h->hmax) {
+        CUDA_TRY(h, cudaMemsetAsync(h->hmax, 0, pl, h->stream));
+        CUDA_TRY(h, cudaMemsetAsync(h->qmax, 0, pl, h->stream));
+        CUDA_TRY(h, cudaMemsetAsync(h->tpeak, 0, pl, h->stream));
+        CUDA_TRY(h, cudaMemsetAsync(h->tdry, 0, pl, h->stream));
+    }
+    if (h->twet) {
+        std::vector<float> tw(N, 0.f);
+        for (int j = 2; j < ny; j++)
+            for (int i = 2; i < nx; i++) tw[hidx(h, j, i)] = -9999.f;
+        if ((rc = upField(h, h->twet, tw))) return rc;
+    }
+    CUDA_TRY(h, cudaMemsetAsync(h->mx, 0, (size_t)h->gridSize * 4, h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(h->my, 0, (size_t)h->gridSize * 4, h->stream));
+    DevState& s = *h->hst;
+    s.t = t0;
+    s.dt = (double)0.0000001f;  // simulator.cu:35
+    s.dt_old = s.dt;
+    s.t_stop = INFINITY;
+    s.nInact = (int)inact.size();
+    h->inited = true;
+    return pushState(h);
+}
+
+int rift_set_uniform_rates(rift_handle* h, double rain_mps, double drain_mps) {
+    if (!h) return RIFT_ERR_ARG;
+    if (!h->inited) {
+        h->hst->rain_rate = (float)rain_mps;
+        h->hst->drain_rate = (float)drain_mps;
+        return RIFT_OK;
+    }
+    int rc = pullState(h);
+    if (rc) return rc;
+    h->hst->rain_rate = (float)rain_mps;
+    h->hst->drain_rate = (float)drain_mps;
+    return pushState(h);
+}
+
+int rift_set_point_sources(rift_handle* h, const int32_t* idx, const double* rate, int32_t n) {
+    if (!h || n < 0 || (n > 0 && (!idx || !rate))) return RIFT_ERR_ARG;
+    cudaFree(h->srcIdx);
+    cudaFree(h->srcRate);
+    cudaFree(h->srcTileList);
+    h->srcIdx = nullptr;
+    h->srcRate = nullptr;
+    h->srcTileList = nullptr;
+    h->nsrc = n;
+    std::vector<int> start(h->gridSize + 1, 0), list;
+    if (n > 0) {
+        std::vector<int> tileOf(n, -1);
+        for (int k = 0; k < n; k++) {
+            int i = idx[k] % h->nx, j = idx[k] / h->nx;
+            if (idx[k] >= 0 && i >= 2 && j >= 2 && j < h->ny)
+                tileOf[k] = ((j - 2) / TH) * h->nBX + (i - 2) / TW;
+            if (tileOf[k] >= h->gridSize) tileOf[k] = -1;
+            if (tileOf[k] >= 0) start[tileOf[k] + 1]++;
+        }
+        for (int b = 0; b < h->gridSize; b++) start[b + 1] += start[b];
+        list.assign(std::max(1, start[h->gridSize]), 0);
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int k = 0; k < n; k++)
+            if (tileOf[k] >= 0) list[fill[tileOf[k]]++] = k;
+        std::vector<float> fr(n);
+        for (int k = 0; k < n; k++) fr[k] = (float)rate[k];
+        CUDA_TRY(h, cudaMalloc(&h->srcIdx, (size_t)n * 4));
+        CUDA_TRY(h, cudaMalloc(&h->srcRate, (size_t)n * 4));
+        CUDA_TRY(h, cudaMalloc(&h->srcTileList, list.size() * 4));
+        CUDA_TRY(h, cudaMemcpyAsync(h->srcIdx, idx, (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(h->srcRate, fr.data(), (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(h->srcTileList, list.data(), list.size() * 4,
+                                    cudaMemcpyHostToDevice, h->stream));
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->srcTileStart, start.data(), start.size() * 4,
+                                cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    destroyGraph(h);
+    return RIFT_OK;
+}
+
+int rift_set_map(rift_handle* h, int32_t which, const double* t0map, const double* t1map,
+                 double factor) {
+    if (!h || which < 0 || which > 2 || !t0map) return RIFT_ERR_ARG;
+    const size_t N = (size_t)h->nx * h->ny, pl = h->plane() * 4;
+    int newMode = t1map ? 2 : 1;
+    for (int k = 0; k < newMode; k++)
+        if (!h->maps[which][k]) {
+            CUDA_TRY(h, cudaMalloc(&h->maps[which][k], pl));
+            CUDA_TRY(h, cudaMemset(h->maps[which][k], 0, pl));
+        }
+    std::vector<float> tmp(N);
+    int rc;
+    for (size_t c = 0; c < N; c++) tmp[c] = (float)t0map[c];
+    if ((rc = upField(h, h->maps[which][0], tmp))) return rc;
+    if (t1map) {
+        for (size_t c = 0; c < N; c++) tmp[c] = (float)t1map[c];
+        if ((rc = upField(h, h->maps[which][1], tmp))) return rc;
+    }
+    if (h->mapMode[which] != newMode) destroyGraph(h);
+    h->mapMode[which] = newMode;
+    if (h->inited) {
+        if ((rc = pullState(h))) return rc;
+        h->hst->factor[which] = (float)factor;
+        return pushState(h);
+    }
+    h->hst->factor[which] = (float)factor;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
+int rift_set_map_factor(rift_handle* h, int32_t which, double factor) {
+    if (!h || which < 0 || which > 2 || !h->mapMode[which]) return RIFT_ERR_ARG;
+    int rc = pullState(h);
+    if (rc) return rc;
+    h->hst->factor[which] = (float)factor;
+    return pushState(h);
+}
+
+int rift_set_series(rift_handle* h, int32_t which, const float* times, const float* rates,
+                    int32_t n) {
+    if (!h || which < 0 || which > 2 || n < 0 || n > MAX_SERIES || (n > 0 && (!times || !rates)))
+        return RIFT_ERR_ARG;
+    if (n > 0) {
+        CUDA_TRY(h, cudaMemcpyAsync(h->serT + which * MAX_SERIES, times, (size_t)n * 4,
+                                    cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(h->serR + which * MAX_SERIES, rates, (size_t)n * 4,
+                                    cudaMemcpyHostToDevice, h->stream));
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (h->serN[which] != n) destroyGraph(h);
+    h->serN[which] = n;
+    return RIFT_OK;
+}
+
+int rift_run(rift_handle* h, int32_t nsteps, double t_stop, double* t, double* dt,
+             int32_t* steps_done) {
+    if (!h || nsteps < 0) return RIFT_ERR_ARG;
+    if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
+    int rc = pullState(h);
+    if (rc) return rc;
+    h->hst->t_stop = t_stop;
+    h->hst->steps_done = 0;
+    if ((rc = pushState(h))) return rc;
+    if ((rc = buildGraph(h))) return rc;
+    for (int k = 0; k < nsteps; k++) CUDA_TRY(h, cudaGraphLaunch(h->graphExec, h->stream));
+    CUDA_TRY(h, cudaGetLastError());
+    if ((rc = pullState(h))) return rc;
+    if (t) *t = h->hst->t;
+    if (dt) *dt = h->hst->dt;
+    if (steps_done) *steps_done = h->hst->steps_done;
+    return RIFT_OK;
+}
+
+int rift_step(rift_handle* h, double* t, double* dt) {
+    int32_t done = 0;
+    int rc = rift_run(h, 1, INFINITY, t, dt, &done);
+    return rc;
+}
+
+int rift_get_time(rift_handle* h, double* t, double* dt) {
+    if (!h) return RIFT_ERR_ARG;
+    int rc = pullState(h);
+    if (rc) return rc;
+    if (t) *t = h->hst->t;
+    if (dt) *dt = h->hst->dt;
+    return RIFT_OK;
+}
+
+int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY) {
+    if (!h) return RIFT_ERR_ARG;
+    if (nBX) *nBX = h->nBX;
+    if (nBY) *nBY = h->nBY;
+    return RIFT_OK;
+}
+
+int rift_get_field(rift_handle* h, int32_t which, double* host, size_t ld) {
+    if (!h || !host || ld < (size_t)h->nx) return RIFT_ERR_ARG;
+    const int nx = h->nx, ny = h->ny;
+    const size_t pl = h->plane();
+    std::vector<float> a, b, c;
+    int rc = 0;
+    auto put = [&](auto fn) {
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) host[(size_t)j * ld + i] = fn(j, i);
+    };
+    auto zero = [&](int, int) { return 0.0; };
+    switch (which) {
+        case RIFT_FIELD_W:
+            if ((rc = downField(h, h->A, a))) return rc;
+            put([&](int j, int i) { return h->Bref[hidx(h, j, i)] + (double)a[hidx(h, j, i)]; });
+            break;
+        case RIFT_FIELD_HU:
+        case RIFT_FIELD_HV:
+            if ((rc = downField(h, h->A + (which == RIFT_FIELD_HU ? 1 : 2) * pl, a))) return rc;
+            put([&](int j, int i) { return (double)a[hidx(h, j, i)]; });
+            break;
+        case RIFT_FIELD_H:
+            if ((rc = downField(h, h->A, a))) return rc;
+            put([&](int j, int i) {
+                bool in = i >= 2 && j >= 2 && i <= nx - 3 && j <= ny - 3;
+                float v = a[hidx(h, j, i)];
+                return in ? (double)((v > kEps) ? v : 0.f) : 0.0;
+            });
+            break;
+        case RIFT_FIELD_Q:
+            if ((rc = downField(h, h->A, a)) || (rc = downField(h, h->A + pl, b)) ||
+                (rc = downField(h, h->A + 2 * pl, c)))
+                return rc;
+            put([&](int j, int i) {
+                bool in = i >= 2 && j >= 2 && i <= nx - 3 && j <= ny - 3;
+                if (!in) return 0.0;
+                size_t q = hidx(h, j, i);
+                float hc = (a[q] > kEps) ? a[q] : 0.f;
+                float h2 = hc * hc;
+                float fac = 2.f * hc / (h2 + std::fmax(h2, (float)h->g.kappa));
+                float u = b[q] * fac, v = c[q] * fac;
+                return (double)(hc * std::sqrt(v * v + u * u));
+            });
+            break;
+        case RIFT_FIELD_BC:
+            put([&](int j, int i) { return h->BC[hidx(h, j, i)]; });
+            break;
+        case RIFT_FIELD_F:
+        case RIFT_FIELD_HMAX:
+        case RIFT_FIELD_QMAX:
+        case RIFT_FIELD_TPEAK:
+        case RIFT_FIELD_TDRY:
+        case RIFT_FIELD_TWET: {
+            const float* src = which == RIFT_FIELD_F      ? h->FA
+                               : which == RIFT_FIELD_HMAX ? h->hmax
+                               : which == RIFT_FIELD_QMAX ? h->qmax
+                               : which == RIFT_FIELD_TPEAK ? h->tpeak
+                               : which == RIFT_FIELD_TDRY ? h->tdry
+                                                          : h->twet;
+            if (!src) {
+                put(zero);
+                break;
+            }
+            if ((rc = downField(h, src, a))) return rc;
+            put([&](int j, int i) { return (double)a[hidx(h, j, i)]; });
+            break;
+        }
+        default:
+            return RIFT_ERR_ARG;
+    }
+    return RIFT_OK;
+}
+
+int rift_get_tiles(rift_handle* h, uint8_t* wet, int32_t* active, int32_t* n_active) {
+    if (!h) return RIFT_ERR_ARG;
+    int rc = pullState(h);
+    if (rc) return rc;
+    std::vector<uint8_t> flags(h->gridSize);
+    // the active set of the last step is prevAct (k_grow keeps it per tile)
+    CUDA_TRY(h, cudaMemcpyAsync(flags.data(), h->prevAct, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
+    if (wet) CUDA_TRY(h, cudaMemcpyAsync(wet, h->wet, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    int k = 0;
+    for (int b = 0; b < h->gridSize; b++)
+        if (flags[b]) {
+            if (active) active[k] = b;
+            k++;
+        }
+    if (n_active) *n_active = k;
+    return RIFT_OK;
+}
+
+int rift_get_tile_speeds(rift_handle* h, double* mx, double* my) {
+    if (!h) return RIFT_ERR_ARG;
+    std::vector<float> a(h->gridSize), b(h->gridSize);
+    CUDA_TRY(h, cudaMemcpyAsync(a.data(), h->mx, (size_t)h->gridSize * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(b.data(), h->my, (size_t)h->gridSize * 4, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < h->gridSize; k++) {
+        if (mx) mx[k] = a[k];
+        if (my) my[k] = b[k];
+    }
+    return RIFT_OK;
+}
+
+// Simulator::ReadHotstart (simulator.cu:975-1090) followed by ApplyBoundaries
+// (simulator.cu:731): state in the reference representation.
+int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, const double* hu,
+                   const double* hv, const double* F, const uint8_t* wet,
+                   const int32_t* active_ids, int32_t n_active, const double* mx, const double* my) {
+    if (!h || !w || !hu || !hv) return RIFT_ERR_ARG;
+    if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
+    const int nx = h->nx, ny = h->ny;
+    const size_t N = (size_t)nx * ny;
+    std::vector<float> H(N), U(N), V(N);
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            size_t c = hidx(h, j, i);
+            H[c] = depthFromW(h, w[c], j, i);
+            U[c] = (float)hu[c];
+            V[c] = (float)hv[c];
+        }
+    hostGhosts(h, H, U, V);
+    int rc = pullState(h);
+    if (rc) return rc;
+    std::vector<uint8_t> wetv(h->gridSize), actf(h->gridSize);
+    CUDA_TRY(h, cudaMemcpyAsync(wetv.data(), h->wet, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(actf.data(), h->prevAct, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (wet) std::copy(wet, wet + h->gridSize, wetv.begin());
+    if (active_ids && n_active >= 0) {
+        std::fill(actf.begin(), actf.end(), 0);
+        for (int k = 0; k < n_active; k++)
+            if (active_ids[k] >= 0 && active_ids[k] < h->gridSize) actf[active_ids[k]] = 1;
+    }
+    std::vector<int> inact;
+    for (int b = 1; b < h->gridSize; b++)
+        if (!actf[b]) inact.push_back(b);
+    if ((rc = uploadState(h, H, U, V, wetv, actf, inact))) return rc;
+    if (F && h->FA) {
+        std::vector<float> f(N);
+        for (size_t c = 0; c < N; c++) f[c] = (float)F[c];
+        if ((rc = upField(h, h->FA, f)) || (rc = upField(h, h->FB, f))) return rc;
+    }
+    if (mx || my) {
+        std::vector<float> a(h->gridSize), b(h->gridSize);
+        for (int k = 0; k < h->gridSize; k++) {
+            a[k] = mx ? (float)mx[k] : 0.f;
+            b[k] = my ? (float)my[k] : 0.f;
+        }
+        CUDA_TRY(h, cudaMemcpyAsync(h->mx, a.data(), a.size() * 4, cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(h->my, b.data(), b.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+    h->hst->t = t;
+    h->hst->dt = dt_prev;
+    h->hst->dt_old = dt_prev;
+    return pushState(h);
+}
+
+int rift_volume(rift_handle* h, double* volume) {
+    if (!h || !volume) return RIFT_ERR_ARG;
+    Params P = makeParams(h);
+    const int blocks = 1024;
+    k_volume<<<blocks, 256, 0, h->stream>>>(P, h->volPartial);
+    std::vector<double> part(2 * blocks);
+    CUDA_TRY(h, cudaMemcpyAsync(part.data(), h->volPartial, part.size() * 8, cudaMemcpyDeviceToHost,
+                                h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    double S = 0.0, C = 0.0;
+    for (int b = 0; b < blocks; b++) {
+        double v = part[2 * b];
+        double t = S + v;
+        C += (std::fabs(S) >= std::fabs(v)) ? (S - t) + v : (v - t) + S;
+        S = t;
+        C += part[2 * b + 1];
+    }
+    *volume = S + C;
+    return RIFT_OK;
+}
+
+const char* rift_last_error(rift_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+void rift_destroy(rift_handle* h) {
+    if (!h) return;
+    destroyGraph(h);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (float* p : {h->A, h->B, h->E, h->nman, h->K, h->FA, h->FB, h->hmax, h->qmax, h->twet,
+                     h->tpeak, h->tdry, h->mx, h->my, h->srcRate, h->serT, h->serR})
+        if (p) cudaFree(p);
+    for (int k = 0; k < 3; k++)
+        for (int q = 0; q < 2; q++)
+            if (h->maps[k][q]) cudaFree(h->maps[k][q]);
+    for (void* p : {(void*)h->wet, (void*)h->prevAct, (void*)h->act, (void*)h->deact,
+                    (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,
+                    (void*)h->srcTileList, (void*)h->st, (void*)h->volPartial})
+        if (p) cudaFree(p);
+    if (h->hst) cudaFreeHost(h->hst);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+}  // extern "C"

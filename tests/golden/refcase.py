@@ -1,0 +1,65 @@
+"""Write a workload in the format oracle/refkit/refrun.cu reads, and read back
+its dumps.  Test infrastructure: used by make_golden.py (run on the GPU machine)
+and by the parity tests."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+
+def write_case(case, d, nsteps, dump=(), timing=False, maps=None, rates=None, src_rate=None):
+    """case: rift_gb300.synth.Case.  maps: {name: (mode, t0, t1, factor)} with
+    name in rain/drain/surge and mode 1 = hold, 2 = interpolate.
+    rates: (rain_mps, drain_mps) fixed uniform rates when no series is set."""
+    os.makedirs(d, exist_ok=True)
+    BX, BY = case.faces()
+    BX.astype(np.float64).tofile(os.path.join(d, "BX.bin"))
+    BY.astype(np.float64).tofile(os.path.join(d, "BY.bin"))
+    case.n.astype(np.float64).tofile(os.path.join(d, "n.bin"))
+    if case.K is not None:
+        case.K.astype(np.float64).tofile(os.path.join(d, "K.bin"))
+    if case.h0 is not None:
+        case.h0.astype(np.float64).tofile(os.path.join(d, "h0.bin"))
+    p = dict(nx=case.h_nx, ny=case.h_ny, flags=case.flags, dx=repr(case.cell), dy=repr(case.cell),
+             kappa=repr(case.kappa), nodata="-9999", courant=repr(case.courant), psi=repr(case.psi),
+             dtheta=repr(case.dtheta), t0=repr(case.t0), nsteps=nsteps, timing=int(timing))
+    if dump:
+        p["dump"] = ",".join(str(s) for s in dump)
+    for which, (t, r) in case.series.items():
+        p[f"series{which}"] = len(t)
+        np.asarray(t, np.float32).tofile(os.path.join(d, f"series{which}_t.bin"))
+        np.asarray(r, np.float32).tofile(os.path.join(d, f"series{which}_r.bin"))
+    if case.src_idx is not None:
+        p["nsrc"] = len(case.src_idx)
+        np.asarray(case.src_idx, np.int32).tofile(os.path.join(d, "src_idx.bin"))
+        if src_rate is not None:
+            np.asarray(src_rate, np.float64).tofile(os.path.join(d, "src_rate.bin"))
+    if rates is not None:
+        p["rain_rate"] = repr(float(rates[0]))
+        p["drain_rate"] = repr(float(rates[1]))
+    for name, (mode, t0, t1, factor) in (maps or {}).items():
+        p[f"map_{name}"] = mode
+        p[f"factor_{name}"] = repr(float(factor))
+        np.asarray(t0, np.float64).tofile(os.path.join(d, f"{name}_t0.bin"))
+        if t1 is not None:
+            np.asarray(t1, np.float64).tofile(os.path.join(d, f"{name}_t1.bin"))
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        for k, v in p.items():
+            f.write(f"{k} {v}\n")
+
+
+def read_dump(out, step, nx, ny, grid_size, names=("w", "hu", "hv")):
+    pre = os.path.join(out, f"s{step:05d}_")
+    r = {}
+    for nm in names:
+        fn = pre + nm + ".bin"
+        if os.path.exists(fn):
+            r[nm] = np.fromfile(fn, dtype=np.float64).reshape(ny, nx)
+    r["wet"] = np.fromfile(pre + "wet.bin", dtype=np.uint8)
+    r["active"] = np.fromfile(pre + "active.bin", dtype=np.int32)
+    r["mx"] = np.fromfile(pre + "mx.bin", dtype=np.float64)
+    r["my"] = np.fromfile(pre + "my.bin", dtype=np.float64)
+    t = np.fromfile(pre + "t.bin", dtype=np.float64)
+    r["t"], r["dt"] = float(t[0]), float(t[1])
+    return r

@@ -1,0 +1,32 @@
+"""The C-ABI library loads and exports every entry point include/rift_gb300.h
+declares (no device calls)."""
+import ctypes
+import os
+import re
+
+from rift_gb300 import build as eb
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "rift_gb300.h")).read()
+    return sorted(set(re.findall(r"\b(rift_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(eb.build())
+    names = declared_symbols()
+    assert len(names) >= 19
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_product_has_no_cpu_fallback():
+    """The package never loads the oracle: no reference to it in product code."""
+    pkg = os.path.join(ROOT, "rift_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                txt = open(os.path.join(dirpath, f)).read()
+                assert "rift_oracle" not in txt, f

@@ -1,0 +1,69 @@
+"""Parity of the CUDA engine with the reference's own kernels (golden
+fixtures run on the GB300) and with the FP64 oracle, through the C ABI.
+
+Bars: tile wet flags and active-tile lists bit-exact; depth within 1e-5 m of
+the reference at every dumped step of these short runs (the benchmark spec bound for
+one simulated hour: 1e-4 m); simulated time within 1e-6 relative.
+"""
+import numpy as np
+import pytest
+
+import fixture as FX
+from rift_gb300 import capi
+
+pytestmark = pytest.mark.gpu
+
+DEPTH_TOL = 1e-5
+
+
+def _run_against_golden(engine_api, name):
+    fx, case = FX.load(name)
+    eng = FX.start(capi.Sim(case, api=engine_api), fx)
+    step = 0
+    log = fx["steps_log"]
+    for s in FX.dumps(fx):
+        while step < s:
+            t, dt = eng.step()
+            step += 1
+            wet, act = eng.tiles()
+            assert len(act) == int(log[step - 1][3]), f"{name}: active count at step {step}"
+        ref = FX.ref_state(fx, s)
+        wet, act = eng.tiles()
+        assert np.array_equal(wet, ref["wet"]), f"{name}: wet tiles differ at step {s}"
+        assert np.array_equal(act, ref["active"]), f"{name}: active tiles differ at step {s}"
+        assert abs(t - ref["t"]) <= 1e-6 * max(1.0, abs(ref["t"])), f"{name}: t {t} vs {ref['t']}"
+        dw = np.abs(FX.interior(eng.field("W") - ref["w"])).max()
+        assert dw <= DEPTH_TOL, f"{name}: max |dw| {dw} at step {s}"
+        if "F" in ref:
+            dF = np.abs(FX.interior(eng.field("F") - ref["F"])).max()
+            assert dF <= DEPTH_TOL, f"{name}: max |dF| {dF} at step {s}"
+        if "hmax" in ref:
+            d = np.abs(FX.interior(eng.field("HMAX") - ref["hmax"])).max()
+            assert d <= DEPTH_TOL, f"{name}: max |dhmax| {d}"
+
+
+@pytest.mark.parametrize("name", FX.CASES)
+def test_engine_matches_reference_kernels(engine_api, name):
+    _run_against_golden(engine_api, name)
+
+
+@pytest.mark.parametrize("name", ["rain", "front", "gridrain_surge", "h0_infil_src"])
+def test_one_step_from_identical_snapshot(engine_api, oracle_api, name):
+    """From the reference's own state at a dumped step, one engine step and one
+    oracle step give identical tile sets and depths within tolerance."""
+    fx, case = FX.load(name)
+    s = FX.dumps(fx)[-2] if len(FX.dumps(fx)) > 1 else FX.dumps(fx)[0]
+    ref = FX.ref_state(fx, s)
+    runs = []
+    for api, mode in ((engine_api, None), (oracle_api, 0)):
+        sim = FX.start(capi.Sim(case, api=api, create_mode=mode), fx)
+        sim.set_state(ref["t"], ref["dt"], ref["w"], ref["hu"], ref["hv"], ref.get("F"),
+                      ref["wet"], ref["active"], ref["mx"], ref["my"])
+        sim.step()
+        runs.append((sim.tiles(), sim.field("W"), sim.time()))
+    (we, ae), w_e, t_e = runs[0]
+    (wo, ao), w_o, t_o = runs[1]
+    assert np.array_equal(we, wo)
+    assert np.array_equal(ae, ao)
+    assert abs(t_e[0] - t_o[0]) <= 1e-6 * max(1.0, t_o[0])
+    assert np.abs(FX.interior(w_e - w_o)).max() <= DEPTH_TOL
