@@ -1,0 +1,326 @@
+"""Benchmark of the GB300 RIFT step (one JSON line on stdout).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3]
+                    [--impl ours|reference]
+
+A step is one full RK2 time step (both stages, Grow, dt) of the whole domain
+with only active tiles computed, as the reference does.  Workloads are the
+seeded synthetic configs of rift_gb300.synth (no datasets are involved):
+  1: 512^2 bumpy plane, uniform rain           (the reference's small case)
+  2: 2048^2 fractal + channel, point-source hydrograph, Green-Ampt (default)
+  3: 8192^2 urban fractal with buildings, uniform drain, interpolated rain maps
+The state is spun up (untimed) to --spinup seconds of simulated time so the
+timed steps see a developed flood, then W warm-up and K timed steps run.
+
+value  = domain cell-updates/s = interior cells x K / device time (CUDA
+         events on the engine's stream around the K graph launches);
+e2e    = the same metric through the C ABI with host buffers: static fields
+         uploaded from host arrays, K rift_step calls (each returns t and dt
+         to the host), the depth map read back, all inside the timed region;
+roofline: HBM bytes per active cell-update (algorithmic, FP32 words of the
+         reference data model) x active cell-updates / device time, against
+         the measured copy bandwidth.
+--impl reference times the FP64 CPU restatement of the reference step on all
+host cores over a bounded sample of the same state (the reference has no CPU
+path of its own; its CUDA build, run through oracle/refkit, is reported
+beside it when the prebuilt fatbin is present).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from rift_gb300 import capi, synth  # noqa: E402
+
+# algorithmic FP32 words per active cell-update (both stages):
+# plain core 23 words; Green-Ampt +7; interpolated map +4; gridded hold +2
+WORDS = {1: 23, 2: 23 + 7, 3: 23 + 4}
+
+
+def make_case(cfg, N=None):
+    if cfg == 1:
+        return synth.config1(N=N or 512)
+    if cfg == 2:
+        return synth.config2(N=N or 2048)
+    if cfg == 3:
+        return synth.config3(N=N or 8192)
+    raise ValueError(cfg)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", "0", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 6:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=2)
+            except Exception:
+                pass
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[2 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons}
+
+
+def spin_up(sim, t_target, chunk=2000):
+    t = sim.time()[0]
+    while t < t_target:
+        t, _, done = sim.run(chunk, t_target)
+        if done == 0:
+            break
+    return t
+
+
+def device_timed_run(sim, steps):
+    """K graph launches bracketed by CUDA events on the engine stream."""
+    lib = sim.lib
+    D = ctypes.POINTER(ctypes.c_double)
+    lib.rift_bench_run.restype = ctypes.c_int
+    lib.rift_bench_run.argtypes = [ctypes.c_void_p, ctypes.c_int32, D, D, D, D, D]
+    out = [ctypes.c_double() for _ in range(5)]
+    rc = lib.rift_bench_run(sim.h, steps, *[ctypes.byref(o) for o in out])
+    if rc != 0:
+        raise RuntimeError(f"rift_bench_run rc={rc}")
+    ms, act_total, done, stage_ms, stage_act = (o.value for o in out)
+    return ms, act_total, done, stage_ms, stage_act
+
+
+def run_ours(args):
+    cfg = args.config
+    case = make_case(cfg, args.N)
+    interior = (case.h_nx - 4) * (case.h_ny - 4)
+    spin = args.spinup if args.spinup is not None else {1: 600.0, 2: 3600.0, 3: 120.0}[cfg]
+
+    # ---- e2e through the C ABI with host buffers ----------------------------
+    t0 = time.perf_counter()
+    sim = capi.Sim(case)
+    sim.setup()
+    t_setup = time.perf_counter() - t0
+    spin_up(sim, spin)
+    snap = sim.snapshot()
+    for _ in range(args.warmup):
+        sim.step()
+    e2e_steps = min(args.steps, 200)
+    h2d = 0
+    t0 = time.perf_counter()
+    sim.load_snapshot(snap)  # host arrays -> device (state upload)
+    h2d += sum(snap[k].nbytes for k in ("w", "hu", "hv", "wet", "active", "mx", "my"))
+    if "F" in snap:
+        h2d += snap["F"].nbytes
+    for _ in range(e2e_steps):
+        sim.step()
+    depth = sim.field("H")
+    t_e2e = time.perf_counter() - t0
+    e2e_value = interior * e2e_steps / t_e2e
+    d2h = depth.nbytes + 16 * e2e_steps
+
+    # ---- device-timed run (inputs resident) --------------------------------
+    sim.load_snapshot(snap)
+    for _ in range(args.warmup):
+        sim.step()
+    clocks = ClockSampler().start()
+    ms, active_cells, done, stage_ms, stage_cells = device_timed_run(sim, args.steps)
+    clk = clocks.stop()
+    steps = int(done)
+    value = interior * steps / (ms * 1e-3)
+    active_rate = active_cells / (ms * 1e-3)
+    peak, peak_kind = peaks()
+    bytes_per = 4 * WORDS[cfg]
+    achieved = stage_cells * bytes_per / (stage_ms * 1e-3) / 1e9 if stage_ms > 0 else None
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", f"traffic_config{cfg}.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_step")
+        except Exception:
+            traffic = None
+    line = {
+        "metric": "cell-updates/s",
+        "value": value,
+        "unit": "cell-updates/s",
+        "n_gpus": args.gpus,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / max(steps, 1),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": case.name, "cells": interior, "spinup_s": spin,
+                   "active_cell_updates_per_s": active_rate,
+                   "active_fraction": active_cells / max(steps, 1) / interior,
+                   "l2": "inputs larger than L2 (state + statics > 129 MB)" if interior > 2e6
+                   else "inputs smaller than L2; steps are back to back",
+                   "parallelism": "replicas only"},
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / e2e_steps,
+                "d2h_bytes_per_step": d2h / e2e_steps, "setup_s": t_setup},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "peak_kind": peak_kind, "bytes_per_active_cell_update": bytes_per,
+                     "kernel": "k_stage (both RK stages, fused)"},
+        "clocks": clk,
+        "gpu_launches": steps * (7 if case.flags & synth.RAIN_GRID else 6),
+    }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(case, snap, args)
+    sim.close()
+    return line
+
+
+def cpu_baseline(case, snap, args, seconds=15.0):
+    from oracle import build as ob
+    lib = ctypes.CDLL(ob.build_oracle())
+    threads = lib.rift_oracle_set_threads(os.cpu_count() or 1)
+    api = (lib, capi.bind(lib, "rift_oracle_", create_has_mode=True))
+    sim = capi.Sim(case, api=api, create_mode=0).setup()
+    sim.load_snapshot(snap)
+    interior = (case.h_nx - 4) * (case.h_ny - 4)
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        sim.step()
+        steps += 1
+    el = time.perf_counter() - t0
+    return {"value": interior * steps / el, "unit": "cell-updates/s", "cores": int(threads),
+            "kind": "port",
+            "sample": f"{steps} steps of {case.name} from the spun-up state ({el:.1f} s)"}
+
+
+def reference_gpu(case, snap, steps):
+    """The reference's own CUDA kernels (oracle/refkit) on the same workload,
+    when the prebuilt fatbin and runner are present."""
+    from oracle import build as ob
+    fat = ob.fatbin_path()
+    if not os.path.exists(fat):
+        return None
+    try:
+        run = ob.build_refrun()
+    except Exception:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import refcase
+    d = f"/tmp/rift_refbench_{os.getpid()}"
+    refcase.write_case(case, d, steps, timing=True)
+    refcase.write_state(d, snap)
+    r = subprocess.run([run, fat, d, d], capture_output=True, text=True)
+    if r.returncode != 0:
+        return {"error": r.stderr.strip()[-300:]}
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def run_reference(args):
+    case = make_case(args.config, args.N)
+    spin = args.spinup if args.spinup is not None else {1: 600.0, 2: 3600.0, 3: 120.0}[args.config]
+    sim = capi.Sim(case)
+    sim.setup()
+    spin_up(sim, spin)
+    snap = sim.snapshot()
+    sim.close()
+    interior = (case.h_nx - 4) * (case.h_ny - 4)
+    cb = cpu_baseline(case, snap, args, seconds=args.ref_seconds)
+    line = {"metric": "cell-updates/s", "value": cb["value"], "unit": "cell-updates/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": case.name, "cells": interior, "spinup_s": spin},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    ref = reference_gpu(case, snap, max(args.steps, 20))
+    if ref is not None:
+        line["reference_cuda_gb300"] = ref
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3))
+    ap.add_argument("--N", type=int, default=None, help="override the grid size (cells per side)")
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--spinup", type=float, default=None)
+    ap.add_argument("--ref-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        # replicas only: every rank runs the same workload on its own GPU
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        args.cpu_baseline = args.cpu_baseline and rank == 0
+        dist.barrier()
+        line = run_ours(args)
+        t = torch.tensor([line["ms_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        if rank == 0:
+            line["ms_per_step"] = float(t.item())
+            line["value"] = line["value"] * world
+            print(json.dumps(line))
+        dist.destroy_process_group()
+        return
+    print(json.dumps(run_ours(args)))
+
+
+if __name__ == "__main__":
+    main()

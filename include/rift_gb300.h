@@ -116,6 +116,12 @@ int rift_set_map(rift_handle* h, int32_t which, const double* t0map,
 /* Only the interpolation factor changes (same t0/t1 maps). */
 int rift_set_map_factor(rift_handle* h, int32_t which, double factor);
 
+/* The interpolation factor of map `which` follows the simulated time:
+ * factor = (t - t0) / (t1 - t0) at the start of every step, the value
+ * InterpolatedGridSeries::p_update computes after the previous step
+ * (GridSeries.cu:398).  t1 <= t0 turns it off (fixed factor). */
+int rift_set_map_times(rift_handle* h, int32_t which, double t0, double t1);
+
 /* One full RK2 (or Euler) step, Grow included: the body of
  * Simulator::RunSimulation (simulator.cu:773-853) from Grow to the last
  * ApplyBoundaries.  Returns the new t and dt. */
@@ -159,6 +165,17 @@ int rift_get_time(rift_handle* h, double* t, double* dt);
  * summed (multiply by dx*dy for m^3) -- the device counterpart of the host
  * volume check in simulator.cu:609-637. */
 int rift_volume(rift_handle* h, double* volume);
+
+/* Measurement entry point (no reference counterpart; the reference only
+ * prints a wall-clock Mcells/s line, simulator.cu:836-841): nsteps step-graph
+ * replays timed with CUDA events on the handle's stream (ms_total; summed
+ * active interior cells in active_total; steps_done), then up to 20 more
+ * steps launched one by one with events around the two fused stage kernels
+ * (stage_ms = their mean duration per step, active_cells = mean active
+ * interior cells per step of that pass). */
+int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total,
+                   double* active_total, double* steps_done, double* stage_ms,
+                   double* active_cells);
 
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);

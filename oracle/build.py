@@ -83,7 +83,10 @@ def build_refrun(force=False):
     src = os.path.join(HERE, "refkit", "refrun.cu")
     out = refrun_path()
     if force or not _newer(out, [src]):
-        _run(["nvcc", "-O2", "-std=c++17", *ARCH, "-o", out, src, "-lcuda"])
+        # host float arithmetic without FMA contraction (the series
+        # interpolation must round like the x86 host build of the reference)
+        _run(["nvcc", "-O2", "-std=c++17", *ARCH, "-Xcompiler", "-ffp-contract=off", "-o", out,
+              src, "-lcuda"])
     return out
 
 

@@ -389,6 +389,29 @@ int main(int argc, char** argv) {
 
     double t = getd("t0", 0.0), dt = (double)0.0000001f;
     if (P.count("dt0")) dt = getd("dt0", dt);
+    if (geti("state", 0)) {
+        // hotstart-like state: Simulator::ReadHotstart (simulator.cu:975-1090)
+        // then ApplyBoundaries (simulator.cu:731)
+        up(w, readBin<double>(dir + "/state_w.bin", N), nx, ny, pitch);
+        up(hu, readBin<double>(dir + "/state_hu.bin", N), nx, ny, pitch);
+        up(hv, readBin<double>(dir + "/state_hv.bin", N), nx, ny, pitch);
+        if (infil) up(F, readBin<double>(dir + "/state_F.bin", N), nx, ny, pitch);
+        auto wb = readBin<unsigned char>(dir + "/state_wet.bin", GridSize);
+        CR(cudaMemcpy(wet_blocks, wb.data(), GridSize, cudaMemcpyHostToDevice));
+        int na = (int)geti("state_nactive", 0);
+        auto ids = readBin<int>(dir + "/state_active.bin", na);
+        std::vector<int> enc(GridSize);
+        std::vector<char> on(GridSize, 0);
+        for (int k = 0; k < na; k++) on[ids[k]] = 1;
+        for (int b = 0; b < GridSize; b++) enc[b] = on[b] ? b : -b;
+        CR(cudaMemcpy(active_blocks, enc.data(), GridSize * 4, cudaMemcpyHostToDevice));
+        nBlocks = na;
+        auto m1 = readBin<double>(dir + "/state_mx.bin", GridSize);
+        auto m2 = readBin<double>(dir + "/state_my.bin", GridSize);
+        CR(cudaMemcpy(mx, m1.data(), GridSize * 8, cudaMemcpyHostToDevice));
+        CR(cudaMemcpy(my, m2.data(), GridSize * 8, cudaMemcpyHostToDevice));
+        applyBC();
+    }
     double rainRate = rainRateFixed, drainRate = drainRateFixed;
     long numSources = nsrc;
     if (nsrc > 0) CR(cudaMemcpy(srcIdx, srcIdxH.data(), nsrc * 4, cudaMemcpyHostToDevice));

@@ -189,6 +189,8 @@ struct Map {
     double factor = 0.0;
     bool interp = false;
     bool set = false;
+    bool timed = false;  // factor = (t - tA) / (tB - tA) at each step start
+    double tA = 0.0, tB = 0.0;
 };
 
 }  // namespace
@@ -647,6 +649,13 @@ void updateSeries(rift_oracle* o) {
 
 void oneStep(rift_oracle* o) {
     updateSeries(o);
+    // InterpolatedGridSeries::p_update (GridSeries.cu:398): the factor of the
+    // map used during this step comes from the time at its start
+    for (int w = 0; w < 3; w++)
+        if (o->maps[w].set && o->maps[w].timed) {
+            o->maps[w].factor = (o->t - o->maps[w].tA) / (o->maps[w].tB - o->maps[w].tA);
+            refreshMap(o, w);
+        }
     grow(o);
     computeFluxes(o, o->dt);
     computeTimestep(o);
@@ -787,6 +796,14 @@ int rift_oracle_set_map_factor(rift_oracle* o, int32_t which, double factor) {
     if (!o || which < 0 || which > 2 || !o->maps[which].set) return RIFT_ERR_ARG;
     o->maps[which].factor = factor;
     refreshMap(o, which);
+    return RIFT_OK;
+}
+
+int rift_oracle_set_map_times(rift_oracle* o, int32_t which, double t0, double t1) {
+    if (!o || which < 0 || which > 2 || !o->maps[which].set) return RIFT_ERR_ARG;
+    o->maps[which].timed = t1 > t0;
+    o->maps[which].tA = t0;
+    o->maps[which].tB = t1;
     return RIFT_OK;
 }
 

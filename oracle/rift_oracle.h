@@ -46,6 +46,7 @@ int rift_oracle_set_point_sources(rift_oracle* o, const int32_t* idx,
 int rift_oracle_set_map(rift_oracle* o, int32_t which, const double* t0map,
                         const double* t1map, double factor);
 int rift_oracle_set_map_factor(rift_oracle* o, int32_t which, double factor);
+int rift_oracle_set_map_times(rift_oracle* o, int32_t which, double t0, double t1);
 int rift_oracle_set_series(rift_oracle* o, int32_t which, const float* times_s,
                            const float* rates, int32_t n);
 int rift_oracle_step(rift_oracle* o, double* t, double* dt);

@@ -50,7 +50,7 @@ def _sig(lib, name, res, args):
 def exported_symbols():
     """Entry points of include/rift_gb300.h (without the prefix)."""
     return ["create", "upload_static", "init", "set_uniform_rates", "set_point_sources",
-            "set_map", "set_map_factor", "step", "run", "set_series", "get_field", "get_tiles",
+            "set_map", "set_map_factor", "set_map_times", "step", "run", "set_series", "get_field", "get_tiles",
             "get_tile_speeds", "set_state", "get_time", "volume", "get_tile_grid", "last_error",
             "destroy"]
 
@@ -69,6 +69,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
     ns["set_point_sources"] = _sig(lib, p + "set_point_sources", C.c_int, [_P, _I, _D, C.c_int32])
     ns["set_map"] = _sig(lib, p + "set_map", C.c_int, [_P, C.c_int32, _D, _D, C.c_double])
     ns["set_map_factor"] = _sig(lib, p + "set_map_factor", C.c_int, [_P, C.c_int32, C.c_double])
+    ns["set_map_times"] = _sig(lib, p + "set_map_times", C.c_int,
+                               [_P, C.c_int32, C.c_double, C.c_double])
     ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
     ns["step"] = _sig(lib, p + "step", C.c_int, [_P, _D, _D])
     ns["run"] = _sig(lib, p + "run", C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _I])
@@ -168,6 +170,11 @@ class Sim:
             idx = np.ascontiguousarray(c.src_idx, dtype=np.int32)
             rate = np.zeros(len(idx))
             self.set_point_sources(idx, rate)
+        if c.rain_maps is not None:
+            m0, m1 = c.rain_maps
+            self.set_map(0, m0, m1, 0.0)
+            if c.map_times is not None:
+                self.set_map_times(0, *c.map_times)
         return self
 
     def init(self, t0=None):
@@ -199,6 +206,9 @@ class Sim:
 
     def set_map_factor(self, which, factor):
         self._check(self.f["set_map_factor"](self.h, which, factor), "set_map_factor")
+
+    def set_map_times(self, which, t0, t1):
+        self._check(self.f["set_map_times"](self.h, which, t0, t1), "set_map_times")
 
     # -- stepping ---------------------------------------------------------
     def step(self):

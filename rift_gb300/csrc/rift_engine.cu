@@ -178,14 +178,15 @@ void destroyGraph(rift_handle* h) {
 void enqueueStep(rift_handle* h) {
     Params P = makeParams(h);
     cudaStream_t s = h->stream;
-    k_begin<<<1, 32, 0, s>>>(P);
     if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
         k_track<<<h->gridTrack, NT, 0, s>>>(P);
     k_grow<<<1, GROW_T, 0, s>>>(P);
-    k_speed<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
-    k_dt<<<h->gridDt, 256, 0, s>>>(P);
+    k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
     k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
-    if (!h->has(RIFT_F_EULER)) k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
+    if (!h->has(RIFT_F_EULER))
+        k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
+    else
+        k_commit<<<h->gridStage, NT, 0, s>>>(P);
 }
 
 int buildGraph(rift_handle* h) {
@@ -398,7 +399,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_stage<1>, NT, 0);
     if (occ < 1) occ = 1;
     h->gridStage = std::max(1, std::min(G, h->numSMs * occ));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_speed, NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_speed_dt, NT, 0);
     if (occ < 1) occ = 1;
     h->gridSpeed = std::max(1, std::min(G, h->numSMs * occ));
     h->gridTrack = std::max(1, std::min(G, h->numSMs * 4));
@@ -470,8 +471,14 @@ int rift_init(rift_handle* h, double t0) {
     // rates and map factors set before init survive it
     float keepF[3] = {h->hst->factor[0], h->hst->factor[1], h->hst->factor[2]};
     float keepRain = h->hst->rain_rate, keepDrain = h->hst->drain_rate;
+    DevState keep = *h->hst;
     std::memset(h->hst, 0, sizeof(DevState));
-    for (int k = 0; k < 3; k++) h->hst->factor[k] = keepF[k];
+    for (int k = 0; k < 3; k++) {
+        h->hst->factor[k] = keepF[k];
+        h->hst->map_timed[k] = keep.map_timed[k];
+        h->hst->map_t0[k] = keep.map_t0[k];
+        h->hst->map_t1[k] = keep.map_t1[k];
+    }
     h->hst->rain_rate = keepRain;
     h->hst->drain_rate = keepDrain;
     int rc = uploadState(h, H, U, V, wet, actf, inact);
@@ -596,6 +603,18 @@ int rift_set_map_factor(rift_handle* h, int32_t which, double factor) {
     if (rc) return rc;
     h->hst->factor[which] = (float)factor;
     return pushState(h);
+}
+
+int rift_set_map_times(rift_handle* h, int32_t which, double t0, double t1) {
+    if (!h || which < 0 || which > 2 || !h->mapMode[which]) return RIFT_ERR_ARG;
+    if (h->inited) {
+        int rc = pullState(h);
+        if (rc) return rc;
+    }
+    h->hst->map_timed[which] = (t1 > t0) ? 1 : 0;
+    h->hst->map_t0[which] = t0;
+    h->hst->map_t1[which] = t1;
+    return h->inited ? pushState(h) : RIFT_OK;
 }
 
 int rift_set_series(rift_handle* h, int32_t which, const float* times, const float* rates,
@@ -832,6 +851,69 @@ int rift_volume(rift_handle* h, double* volume) {
         C += part[2 * b + 1];
     }
     *volume = S + C;
+    return RIFT_OK;
+}
+
+// Timed run for measurement: nsteps graph replays bracketed by CUDA events on
+// the handle's stream (ms_total), then up to 20 more steps launched one by
+// one with events around the two fused stage kernels (stage_ms: their mean
+// duration per step, active_cells: mean active interior cells per step of
+// that pass).  Active cells of the graph pass go to *active_total.
+int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* active_total,
+                   double* steps_done, double* stage_ms, double* active_cells) {
+    if (!h || nsteps < 1) return RIFT_ERR_ARG;
+    if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
+    int rc = pullState(h);
+    if (rc) return rc;
+    h->hst->t_stop = INFINITY;
+    h->hst->steps_done = 0;
+    h->hst->activeCells = 0;
+    if ((rc = pushState(h)) || (rc = buildGraph(h))) return rc;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(h, cudaEventCreate(&e0));
+    CUDA_TRY(h, cudaEventCreate(&e1));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaEventRecord(e0, h->stream));
+    for (int k = 0; k < nsteps; k++) CUDA_TRY(h, cudaGraphLaunch(h->graphExec, h->stream));
+    CUDA_TRY(h, cudaEventRecord(e1, h->stream));
+    CUDA_TRY(h, cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CUDA_TRY(h, cudaEventElapsedTime(&ms, e0, e1));
+    if ((rc = pullState(h))) return rc;
+    if (ms_total) *ms_total = ms;
+    if (steps_done) *steps_done = h->hst->steps_done;
+    double graphCells = (double)h->hst->activeCells;
+    // per-kernel pass
+    const int M = std::min(nsteps, 20);
+    h->hst->activeCells = 0;
+    if ((rc = pushState(h))) return rc;
+    Params P = makeParams(h);
+    cudaStream_t s = h->stream;
+    double stageSum = 0.0;
+    for (int k = 0; k < M; k++) {
+        if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
+            k_track<<<h->gridTrack, NT, 0, s>>>(P);
+        k_grow<<<1, GROW_T, 0, s>>>(P);
+        k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
+        CUDA_TRY(h, cudaEventRecord(e0, s));
+        k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
+        if (!h->has(RIFT_F_EULER))
+            k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
+        else
+            k_commit<<<h->gridStage, NT, 0, s>>>(P);
+        CUDA_TRY(h, cudaEventRecord(e1, s));
+        CUDA_TRY(h, cudaEventSynchronize(e1));
+        float sm = 0.f;
+        CUDA_TRY(h, cudaEventElapsedTime(&sm, e0, e1));
+        stageSum += sm;
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    if ((rc = pullState(h))) return rc;
+    if (stage_ms) *stage_ms = stageSum / M;
+    if (active_cells) *active_cells = (double)h->hst->activeCells / M;
+    if (active_total) *active_total = graphCells;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     return RIFT_OK;
 }
 

@@ -1,26 +1,31 @@
 // rift_kernels.cuh -- device kernels of the GB300 step.
 //
 // One step (the body of Simulator::RunSimulation, simulator.cu:773-853):
-//   k_begin   : stop test, uniform-source interpolation (simulator.cu:500-538)
 //   k_track   : re-wet inactive tiles under gridded rain / surge
-//               (TrackRainfall_k / TrackSurge_k, grid.cu:1224-1276)
-//   k_grow    : 4-neighbour dilation of the wet tiles and on-device
-//               compaction of the active / inactive / deactivated tile lists
-//               (Grow, grid.cu:1188-1322) with warp ballots and a block scan
-//   k_speed   : per-tile local-speed maxima on U^n (the speed output of the
-//               first ComputeFluxes, grid.cu:813-838); re-syncs the stage
-//               buffer of tiles that just went inactive
-//   k_dt      : max over every tile's speed (stale entries included, as
-//               simulator.cu:544-545 does) -> dt, t (FP64)
+//               (TrackRainfall_k / TrackSurge_k, grid.cu:1224-1276); only
+//               when a gridded rain or surge series is on
+//   k_grow    : start of step (stop test, uniform-source interpolation of
+//               simulator.cu:500-538), then the 4-neighbour dilation of the
+//               wet tiles and the on-device compaction of the active /
+//               inactive / deactivated tile lists (Grow, grid.cu:1188-1322)
+//               with warp ballots and one block scan per 1024 tiles
+//   k_speed_dt: per-tile local-speed maxima on U^n (the speed output of the
+//               first ComputeFluxes, grid.cu:813-838), the max over every
+//               tile (stale speeds of inactive tiles included, A5) and, in
+//               the last CTA, dt and t (Simulator::ComputeTimestep,
+//               simulator.cu:540-566); also re-syncs the stage buffer of
+//               tiles that just went inactive
 //   k_stage<1>: fused flux + sources + friction + RK stage 1 + ghost cells
 //               (ComputeFluxes_k + Integrate_1_k + ApplyBoundaries)
 //   k_stage<2>: fused flux + sources + RK stage 2 + ghost cells + outputs +
 //               tile wet flags + tile speeds
 //               (ComputeFluxes_k + Integrate_2_k + ApplyBoundaries)
-// Every stage kernel is persistent over the compacted active-tile list and
-// stages each tile's halo'd block of (h, hu, hv) and the four face-elevation
-// offsets in shared memory with TMA (cp.async.bulk.tensor, 3-D maps over the
-// stacked fields) completing on an mbarrier.
+//   k_commit  : Euler mode only, copies the single stage's result back
+// The tile kernels are persistent over the compacted list of active tiles.
+// Each CTA stages a tile's halo'd block of (h, hu, hv) and of the four
+// face-elevation offsets in shared memory with TMA (cp.async.bulk.tensor on
+// 3-D maps over the stacked fields), double-buffered: the next tile's block
+// is in flight while the current one is computed.
 #pragma once
 #include <cuda.h>
 #include <cstdint>
@@ -33,7 +38,7 @@ constexpr int TW = 16;          // tile width  (BLOCK_COLS, grid.cu:19)
 constexpr int TH = 14;          // tile height (BLOCK_ROWS, grid.cu:18)
 constexpr int SW = TW + 4;      // staged block width  (2-cell halo)
 constexpr int SH = TH + 4;      // staged block height
-constexpr int NT = 256;         // threads per stage CTA
+constexpr int NT = 256;         // threads per tile CTA
 constexpr int GROW_T = 1024;    // threads of the single-CTA grow kernel
 constexpr int MAX_SERIES = 4096;
 
@@ -48,9 +53,12 @@ constexpr int ERR_TMA_TIMEOUT = 1;
 // Device-resident scalars of the run (one per handle).
 struct DevState {
     double t;          // simulated time, FP64 accumulator
-    double dt;         // dt of the current step (after k_dt)
+    double dt;         // dt of the current step (after k_speed_dt)
     double dt_old;     // dt of the previous step (stage-1 source clamps)
     double t_stop;     // kernels idle once t >= t_stop at step start
+    double map_t0[3];  // map interval [t0, t1) when the factor follows t
+    double map_t1[3];
+    int map_timed[3];
     float rain_rate;   // uniform rates, m/s, as the reference's float rates
     float drain_rate;
     float ser_interp[3];  // Source::interpolated_rate state (A11)
@@ -60,6 +68,7 @@ struct DevState {
     int nActive, nDeact, nInact;
     int stop;
     int steps_done;
+    unsigned long long activeCells;  // interior cells of active tiles, summed over steps
     int error;
     int err_info;
 };
@@ -86,8 +95,8 @@ struct Params {
     const float* map1[3];
     int mapMode[3];    // 0 none, 1 hold, 2 interpolate
     uint8_t* wet;
-    uint8_t* prevAct;
-    int* act;
+    uint8_t* prevAct;  // active set of the current step (after k_grow)
+    int* act;          // active tiles that hold interior cells
     int* deact;
     int* inact;
     float* mx;
@@ -148,8 +157,8 @@ __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* tm) {
     asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)tm) : "memory");
 }
 
-// Bounded wait on an mbarrier phase; returns false after the spin limit (the
-// caller records the error and leaves the tile loop).
+// Bounded wait on an mbarrier phase; false after the spin limit (the caller
+// records the error and leaves the tile loop).
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
     for (int it = 0; it < (1 << 20); ++it)
         if (mbar_try_wait(bar, parity)) return true;
@@ -157,10 +166,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 }
 
 // ------------------------------------------------------------- shared block
-struct __align__(128) StageSmem {
+struct __align__(128) TileBuf {
     float in[3][SH][SW];    // h, hu, hv     (TMA destination, 4320 B)
     float pad0[8];          // keeps `e` 128-byte aligned
     float e[4][SH][SW];     // eW, eE, eS, eN (TMA destination, 5760 B)
+};
+static_assert(offsetof(TileBuf, e) % 128 == 0, "TMA destination alignment");
+static_assert(sizeof(TileBuf) % 128 == 0, "TMA destination alignment");
+
+struct __align__(128) StageSmem {
+    TileBuf buf[2];
     union {
         struct {
             float P[3][TH][TW + 2];
@@ -174,17 +189,17 @@ struct __align__(128) StageSmem {
     float FX[3][TH][TW + 1];
     float FY[3][TH + 1][TW];
     float red[2][NT / 32];
-    uint64_t bar;
+    uint64_t bar[2];
 };
-static_assert(offsetof(StageSmem, e) % 128 == 0, "TMA destination alignment");
 constexpr uint32_t BYTES_IN = 3 * SH * SW * 4;
 constexpr uint32_t BYTES_E = 4 * SH * SW * 4;
 
-__device__ __forceinline__ bool tileHasInterior(const Params& P, int tile, int& i0, int& j0) {
-    int bX = tile % P.nBX, bY = tile / P.nBX;
+__device__ __forceinline__ void tileOrigin(const Params& P, int tile, int& bX, int& bY, int& i0,
+                                           int& j0) {
+    bX = tile % P.nBX;
+    bY = tile / P.nBX;
     i0 = bX * TW + 2;
     j0 = bY * TH + 2;
-    return i0 <= P.nx - 3 && j0 <= P.ny - 3;
 }
 
 // Gridded map value at a cell (hold or InterpGrid_k semantics, grid.cu:292-311).
@@ -202,39 +217,60 @@ __device__ __forceinline__ float mapValue(const Params& P, int which, size_t c, 
     return factor * (x1 - x0) + x0;
 }
 
-__device__ __forceinline__ float blockMax(float v, float* red, int slot) {
+// Block-wide max (non-negative values); result valid in thread 0.
+__device__ __forceinline__ float blockMax(float v, float* red) {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     if (l == 0) red[w] = v;
     __syncthreads();
     float r = 0.f;
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0)
         for (int k = 0; k < NT / 32; k++) r = fmaxf(r, red[k]);
-    }
-    (void)slot;
-    return r;  // valid in thread 0
+    return r;
 }
 
-// Issue the TMA loads of one tile's staged block and wait for them.
-__device__ __forceinline__ bool stageTile(StageSmem& S, const CUtensorMap* tmIn,
-                                          const CUtensorMap* tmE, int bX, int bY,
-                                          uint32_t& phase) {
+// Thread 0 issues the TMA loads of one tile's staged block into `b`.
+__device__ __forceinline__ void issueTile(TileBuf& b, uint64_t* bar, const CUtensorMap* tmIn,
+                                          const CUtensorMap* tmE, const Params& P, int tile) {
+    int bX = tile % P.nBX, bY = tile / P.nBX;
+    fence_proxy_async();
+    mbar_expect_tx(bar, BYTES_IN + BYTES_E);
+    tma_load_3d(&b.in[0][0][0], tmIn, bar, bX * TW, bY * TH, 0);
+    tma_load_3d(&b.e[0][0][0], tmE, bar, bX * TW, bY * TH, 0);
+}
+
+// Prologue shared by the tile kernels: barriers and the first tile's load.
+__device__ __forceinline__ void tilePrologue(StageSmem& S, const CUtensorMap* tmIn,
+                                             const CUtensorMap* tmE, const Params& P, int nAct) {
     if (threadIdx.x == 0) {
-        fence_proxy_async();
-        mbar_expect_tx(&S.bar, BYTES_IN + BYTES_E);
-        tma_load_3d(&S.in[0][0][0], tmIn, &S.bar, bX * TW, bY * TH, 0);
-        tma_load_3d(&S.e[0][0][0], tmE, &S.bar, bX * TW, bY * TH, 0);
+        prefetch_tmap(tmIn);
+        prefetch_tmap(tmE);
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        fence_mbar_init();
+        if ((int)blockIdx.x < nAct) issueTile(S.buf[0], &S.bar[0], tmIn, tmE, P, P.act[blockIdx.x]);
     }
-    bool ok = mbar_wait_bounded(&S.bar, phase);
-    phase ^= 1u;
+    __syncthreads();
+}
+
+// Wait for the current tile (buffer b), then prefetch the CTA's next tile
+// into the other buffer, whose readers all passed the barrier.
+__device__ __forceinline__ bool tileAcquire(StageSmem& S, const CUtensorMap* tmIn,
+                                            const CUtensorMap* tmE, const Params& P, int b,
+                                            uint32_t* ph, int kNext, int nAct) {
+    bool ok = mbar_wait_bounded(&S.bar[b], ph[b]);
+    ph[b] ^= 1u;
+    ok = __syncthreads_and(ok);
+    if (ok && threadIdx.x == 0 && kNext < nAct)
+        issueTile(S.buf[b ^ 1], &S.bar[b ^ 1], tmIn, tmE, P, P.act[kNext]);
     return ok;
 }
 
-// ---------------------------------------------------------------- k_begin
-// Start of a step: stop test and the uniform sources of
-// Simulator::UpdateSource (simulator.cu:500-538): each CSV series is
-// interpolated at float(t) (source.cc:65-73) and its float state divided in
-// place (A11).  IEEE float ops (_rn intrinsics) keep the host arithmetic.
+// ---------------------------------------------------------------- sources
+// Uniform sources of Simulator::UpdateSource (simulator.cu:500-538): each CSV
+// series is interpolated at float(t) (source.cc:65-73) and its float state
+// divided in place (A11).  IEEE float ops (_rn intrinsics) keep the host's
+// arithmetic (no contraction, exact division).
 __device__ __forceinline__ float seriesInterp(const float* T, const float* R, int n, float t,
                                               float cur) {
     for (int i = 0; i + 1 < n; i++) {
@@ -247,13 +283,7 @@ __device__ __forceinline__ float seriesInterp(const float* T, const float* R, in
     return cur;
 }
 
-__global__ void k_begin(Params P) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    DevState* s = P.st;
-    if (s->t >= s->t_stop) {
-        s->stop = 1;
-        return;
-    }
+__device__ void beginStep(const Params& P, DevState* s) {
     s->stop = 0;
     s->steps_done += 1;
     s->max_bits[0] = 0u;
@@ -281,6 +311,11 @@ __global__ void k_begin(Params P) {
         s->ser_interp[1] = v;
         s->drain_rate = v;
     }
+    // map factor following t (GridSeries::update computes it at the end of
+    // the previous step from the same t, GridSeries.cu:398)
+    for (int w = 0; w < 3; w++)
+        if (s->map_timed[w])
+            s->factor[w] = (float)((s->t - s->map_t0[w]) / (s->map_t1[w] - s->map_t0[w]));
 }
 
 // ---------------------------------------------------------------- k_track
@@ -288,8 +323,11 @@ __global__ void k_begin(Params P) {
 // previous Grow.  A9: the rows come from blockY * BLOCK_COLS (16), not 14.
 __global__ void __launch_bounds__(NT) k_track(Params P) {
     const DevState* s = P.st;
-    if (s->stop) return;
+    if (s->t >= s->t_stop) return;
     const int n = s->nInact;
+    float fac0 = s->factor[0], fac2 = s->factor[2];
+    if (s->map_timed[0]) fac0 = (float)((s->t - s->map_t0[0]) / (s->map_t1[0] - s->map_t0[0]));
+    if (s->map_timed[2]) fac2 = (float)((s->t - s->map_t0[2]) / (s->map_t1[2] - s->map_t0[2]));
     for (int k = blockIdx.x; k < n; k += gridDim.x) {
         const int tile = P.inact[k];
         if (P.wet[tile]) continue;  // uniform across the block
@@ -301,11 +339,11 @@ __global__ void __launch_bounds__(NT) k_track(Params P) {
             if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
                 size_t c = cidx(P, 0, j, i);
                 if (P.flags & F_RAIN_G) {
-                    float v = mapValue(P, 0, c, s->factor[0]);
+                    float v = mapValue(P, 0, c, fac0);
                     if (v > kEps) hit = true;
                 }
                 if (P.flags & F_SURGE) {
-                    float v = mapValue(P, 2, c, s->factor[2]);
+                    float v = mapValue(P, 2, c, fac2);
                     if (v != P.nodata && v > 0.f) hit = true;
                 }
             }
@@ -315,117 +353,137 @@ __global__ void __launch_bounds__(NT) k_track(Params P) {
 }
 
 // ---------------------------------------------------------------- k_grow
-// Single CTA: active(t) = wet(t) | wet(4-neighbours), false outside the tile
-// grid; tile 0 is always kept (A8: it encodes as 0, never negative).
-// Compacts (ascending) the active ids, the inactive ids other than tile 0
-// (tracked next step) and the tiles that went from active to inactive.
-__device__ __forceinline__ int blockScanExclusive(int flag, int* warpSums, int& total) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    unsigned b = __ballot_sync(0xffffffffu, flag);
-    int inWarp = __popc(b & ((1u << lane) - 1u));
-    if (lane == 0) warpSums[w] = __popc(b);
-    __syncthreads();
-    if (w == 0) {
-        int v = (lane < GROW_T / 32) ? warpSums[lane] : 0;
-        int x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        if (lane < GROW_T / 32) warpSums[lane] = x - v;  // exclusive
-        if (lane == 31) warpSums[32] = x;
-    }
-    __syncthreads();
-    int r = warpSums[w] + inWarp;
-    total = warpSums[32];
-    __syncthreads();
-    return r;
-}
-
+// Single CTA.  active(t) = wet(t) | wet(4-neighbours), false outside the tile
+// grid; tile 0 is always kept (A8: it encodes as 0, never negative).  One
+// block scan per 1024 tiles compacts (ascending) the active tiles that hold
+// interior cells, the inactive tiles other than tile 0 (tracked next step)
+// and the tiles that went from active to inactive.  Active tiles without
+// interior cells (the reference computes them and writes mx = my = 0) get
+// their zero speeds here and are not scheduled.
 __global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
     DevState* s = P.st;
-    if (s->stop) return;
-    __shared__ int sumsA[33], sumsD[33], sumsI[33];
-    int baseA = 0, baseD = 0, baseI = 0;
-    const int nBX = P.nBX, nBY = P.nBY;
-    for (int b0 = 0; b0 < P.gridSize; b0 += GROW_T) {
-        int b = b0 + threadIdx.x;
-        int a = 0, d = 0, in = 0;
-        if (b < P.gridSize) {
-            int bX = b % nBX, bY = b / nBX;
-            bool v = P.wet[b] || (bX > 0 && P.wet[b - 1]) || (bX < nBX - 1 && P.wet[b + 1]) ||
-                     (bY > 0 && P.wet[b - nBX]) || (bY < nBY - 1 && P.wet[b + nBX]) || b == 0;
-            a = v ? 1 : 0;
-            d = (P.prevAct[b] && !v) ? 1 : 0;
-            in = (!v && b != 0) ? 1 : 0;
-        }
-        int tA, tD, tI;
-        int pa = blockScanExclusive(a, sumsA, tA);
-        int pd = blockScanExclusive(d, sumsD, tD);
-        int pi = blockScanExclusive(in, sumsI, tI);
-        if (b < P.gridSize) {
-            if (a) P.act[baseA + pa] = b;
-            if (d) P.deact[baseD + pd] = b;
-            if (in) P.inact[baseI + pi] = b;
-            P.prevAct[b] = (uint8_t)a;
-        }
-        baseA += tA;
-        baseD += tD;
-        baseI += tI;
-    }
+    __shared__ int stop;
+    __shared__ int wsum[3][33];
+    __shared__ unsigned long long cellSum;
     if (threadIdx.x == 0) {
-        s->nActive = baseA;
-        s->nDeact = baseD;
-        s->nInact = baseI;
+        stop = (s->t >= s->t_stop) ? 1 : 0;
+        if (stop)
+            s->stop = 1;
+        else
+            beginStep(P, s);
+        cellSum = 0ull;
+    }
+    __syncthreads();
+    if (stop) return;
+    const int nBX = P.nBX, nBY = P.nBY;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int base[3] = {0, 0, 0};
+    unsigned long long myCells = 0ull;
+    for (int b0 = 0; b0 < P.gridSize; b0 += GROW_T) {
+        const int b = b0 + threadIdx.x;
+        int flag[3] = {0, 0, 0};  // scheduled active, deactivated, inactive
+        bool v = false;
+        if (b < P.gridSize) {
+            const int bX = b % nBX, bY = b / nBX;
+            v = P.wet[b] || (bX > 0 && P.wet[b - 1]) || (bX < nBX - 1 && P.wet[b + 1]) ||
+                (bY > 0 && P.wet[b - nBX]) || (bY < nBY - 1 && P.wet[b + nBX]) || b == 0;
+            const int i0 = bX * TW + 2, j0 = bY * TH + 2;
+            const bool interior = i0 <= P.nx - 3 && j0 <= P.ny - 3;
+            if (v && interior) {
+                flag[0] = 1;
+                int ci = min(P.nx - 3, i0 + TW - 1) - i0 + 1;
+                int cj = min(P.ny - 3, j0 + TH - 1) - j0 + 1;
+                myCells += (unsigned long long)(ci * cj);
+            } else if (v) {
+                P.mx[b] = 0.f;
+                P.my[b] = 0.f;
+            }
+            flag[1] = (P.prevAct[b] && !v) ? 1 : 0;
+            flag[2] = (!v && b != 0) ? 1 : 0;
+        }
+        unsigned bal[3];
+        int inWarp[3];
+        for (int q = 0; q < 3; q++) {
+            bal[q] = __ballot_sync(0xffffffffu, flag[q]);
+            inWarp[q] = __popc(bal[q] & ((1u << lane) - 1u));
+            if (lane == 0) wsum[q][w] = __popc(bal[q]);
+        }
+        __syncthreads();
+        if (w < 3) {  // warp q scans list q's 32 warp totals
+            int v0 = wsum[w][lane], x = v0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            wsum[w][lane] = x - v0;
+            if (lane == 31) wsum[w][32] = x;
+        }
+        __syncthreads();
+        if (b < P.gridSize) {
+            if (flag[0]) P.act[base[0] + wsum[0][w] + inWarp[0]] = b;
+            if (flag[1]) P.deact[base[1] + wsum[1][w] + inWarp[1]] = b;
+            if (flag[2]) P.inact[base[2] + wsum[2][w] + inWarp[2]] = b;
+            P.prevAct[b] = (uint8_t)(v ? 1 : 0);
+        }
+        for (int q = 0; q < 3; q++) base[q] += wsum[q][32];
+        __syncthreads();
+    }
+    for (int o = 16; o > 0; o >>= 1) myCells += __shfl_xor_sync(0xffffffffu, myCells, o);
+    if (lane == 0) atomicAdd(&cellSum, myCells);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s->nActive = base[0];
+        s->nDeact = base[1];
+        s->nInact = base[2];
+        s->activeCells += cellSum;
     }
 }
 
-// ---------------------------------------------------------------- k_speed
-// Per-tile speed maxima of U^n over the active tiles (what the first
-// ComputeFluxes of a step writes to mx/my, grid.cu:813-838), and the stage
-// buffer re-sync of tiles that just went inactive (U* = U^n there).
-__global__ void __launch_bounds__(NT) k_speed(const __grid_constant__ CUtensorMap tmA,
-                                              const __grid_constant__ CUtensorMap tmE, Params P) {
+// ------------------------------------------------------------- k_speed_dt
+// Per-tile speed maxima of U^n over the scheduled active tiles (what the
+// first ComputeFluxes of a step writes to mx/my, grid.cu:813-838); the max
+// over all tiles, stale entries of inactive tiles included (A5); in the last
+// CTA, dt with the reference's rounding points (fmaxf of the scaled maxima,
+// FP64 division) and t += dt.  Also re-syncs U* with U^n on tiles that went
+// inactive this step (interior cells and the ghost cells they own).
+__global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtensorMap tmA,
+                                                 const __grid_constant__ CUtensorMap tmE, Params P) {
     __shared__ StageSmem S;
-    const DevState* st = P.st;
+    __shared__ bool last;
+    DevState* st = P.st;
     if (st->stop) return;
     const int tid = threadIdx.x;
-    if (tid == 0) {
-        prefetch_tmap(&tmA);
-        prefetch_tmap(&tmE);
-        mbar_init(&S.bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    uint32_t phase = 0;
-    const float kappa = P.kappa;
     const int nAct = st->nActive;
-    for (int k = blockIdx.x; k < nAct; k += gridDim.x) {
-        const int tile = P.act[k];
-        int i0, j0;
-        if (!tileHasInterior(P, tile, i0, j0)) {
-            if (tid == 0) {
-                P.mx[tile] = 0.f;
-                P.my[tile] = 0.f;
-            }
-            continue;
+    tilePrologue(S, &tmA, &tmE, P, nAct);
+    const float kappa = P.kappa;
+    // stale speeds of tiles that are not active this step
+    float amx = 0.f, amy = 0.f;
+    for (int b = blockIdx.x * NT + tid; b < P.gridSize; b += gridDim.x * NT)
+        if (!P.prevAct[b]) {
+            amx = fmaxf(amx, P.mx[b]);
+            amy = fmaxf(amy, P.my[b]);
         }
-        const int bX = tile % P.nBX, bY = tile / P.nBX;
-        __syncthreads();
-        bool ok = stageTile(S, &tmA, &tmE, bX, bY, phase);
-        if (!__syncthreads_and(ok)) {
-            if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
+    uint32_t ph[2] = {0u, 0u};
+    int bsel = 0;
+    float tmx = 0.f, tmy = 0.f;  // thread 0: max of this CTA's new tile speeds
+    for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
+        const int tile = P.act[k];
+        int bX, bY, i0, j0;
+        tileOrigin(P, tile, bX, bY, i0, j0);
+        if (!tileAcquire(S, &tmA, &tmE, P, bsel, ph, k + gridDim.x, nAct)) {
+            if (tid == 0) atomicOr(&st->error, ERR_TMA_TIMEOUT);
             return;
         }
+        const TileBuf& T = S.buf[bsel];
         float spx = 0.f, spy = 0.f;
         // x: depth + hu reconstruction of cells i0-1..i0+16 on the tile rows
         if (tid < TH * (TW + 2)) {
             int r = tid / (TW + 2), c = tid % (TW + 2);
             int sr = r + 2, sc = c + 1;
-            RecN R = constructN(S.in[0][sr][sc], S.in[1][sr][sc], S.in[0][sr][sc + 1],
-                                S.in[1][sr][sc + 1], S.in[0][sr][sc - 1], S.in[1][sr][sc - 1],
-                                S.e[0][sr][sc], S.e[1][sr][sc], S.e[1][sr][sc] - S.e[0][sr][sc + 1],
-                                S.e[1][sr][sc - 1] - S.e[0][sr][sc]);
+            RecN R = constructN(T.in[0][sr][sc], T.in[1][sr][sc], T.in[0][sr][sc + 1],
+                                T.in[1][sr][sc + 1], T.in[0][sr][sc - 1], T.in[1][sr][sc - 1],
+                                T.e[0][sr][sc], T.e[1][sr][sc], T.e[1][sr][sc] - T.e[0][sr][sc + 1],
+                                T.e[1][sr][sc - 1] - T.e[0][sr][sc]);
             S.rec.x.P[0][r][c] = R.hP;
             S.rec.x.P[1][r][c] = R.qP;
             S.rec.x.M[0][r][c] = R.hM;
@@ -434,20 +492,19 @@ __global__ void __launch_bounds__(NT) k_speed(const __grid_constant__ CUtensorMa
         __syncthreads();
         if (tid < TH * TW) {  // east face of tile cell (ty, tx)
             int ty = tid / TW, tx = tid % TW;
-            int i = i0 + tx, j = j0 + ty;
-            if (i <= P.nx - 3 && j <= P.ny - 3)
+            if (i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3)
                 spx = faceSpeed(S.rec.x.P[0][ty][tx + 1], S.rec.x.P[1][ty][tx + 1],
                                 S.rec.x.M[0][ty][tx + 2], S.rec.x.M[1][ty][tx + 2], kappa);
         }
         __syncthreads();
-        // y: depth + hv reconstruction of rows j0-1..j0+14 (only j0..j0+14 needed)
+        // y: depth + hv reconstruction of rows j0..j0+14
         if (tid < (TH + 2) * TW) {
             int r = tid / TW, c = tid % TW;
             int sr = r + 1, sc = c + 2;
-            RecN R = constructN(S.in[0][sr][sc], S.in[2][sr][sc], S.in[0][sr + 1][sc],
-                                S.in[2][sr + 1][sc], S.in[0][sr - 1][sc], S.in[2][sr - 1][sc],
-                                S.e[2][sr][sc], S.e[3][sr][sc], S.e[3][sr][sc] - S.e[2][sr + 1][sc],
-                                S.e[3][sr - 1][sc] - S.e[2][sr][sc]);
+            RecN R = constructN(T.in[0][sr][sc], T.in[2][sr][sc], T.in[0][sr + 1][sc],
+                                T.in[2][sr + 1][sc], T.in[0][sr - 1][sc], T.in[2][sr - 1][sc],
+                                T.e[2][sr][sc], T.e[3][sr][sc], T.e[3][sr][sc] - T.e[2][sr + 1][sc],
+                                T.e[3][sr - 1][sc] - T.e[2][sr][sc]);
             S.rec.y.P[0][r][c] = R.hP;
             S.rec.y.P[1][r][c] = R.qP;
             S.rec.y.M[0][r][c] = R.hM;
@@ -456,28 +513,51 @@ __global__ void __launch_bounds__(NT) k_speed(const __grid_constant__ CUtensorMa
         __syncthreads();
         if (tid < TH * TW) {  // north face of tile cell (ty, tx)
             int ty = tid / TW, tx = tid % TW;
-            int i = i0 + tx, j = j0 + ty;
-            if (i <= P.nx - 3 && j <= P.ny - 3)
+            if (i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3)
                 spy = faceSpeed(S.rec.y.P[0][ty + 1][tx], S.rec.y.P[1][ty + 1][tx],
                                 S.rec.y.M[0][ty + 2][tx], S.rec.y.M[1][ty + 2][tx], kappa);
         }
-        float mxv = blockMax(spx, S.red[0], 0);
-        __syncthreads();
-        float myv = blockMax(spy, S.red[1], 1);
+        float mxv = blockMax(spx, S.red[0]);
+        float myv = blockMax(spy, S.red[1]);
         if (tid == 0) {
             P.mx[tile] = mxv;
             P.my[tile] = myv;
+            tmx = fmaxf(tmx, mxv);
+            tmy = fmaxf(tmy, myv);
         }
+        __syncthreads();
     }
-    // re-sync U* with U^n on tiles that went inactive, including the ghost
-    // cells their edge cells own
+    // dt: block max of stale + new speeds, one atomic per CTA, last CTA finishes
+    __syncthreads();
+    float bmx = blockMax(fmaxf(amx, tid == 0 ? tmx : 0.f), S.red[0]);
+    float bmy = blockMax(fmaxf(amy, tid == 0 ? tmy : 0.f), S.red[1]);
+    if (tid == 0) {
+        // speeds are non-negative: their bit patterns order like the values
+        atomicMax(&st->max_bits[0], __float_as_uint(bmx));
+        atomicMax(&st->max_bits[1], __float_as_uint(bmy));
+        __threadfence();
+        last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && tid == 0) {
+        __threadfence();
+        double maxx = (double)__uint_as_float(atomicOr(&st->max_bits[0], 0u));
+        double maxy = (double)__uint_as_float(atomicOr(&st->max_bits[1], 0u));
+        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
+        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
+        double dt = cx < cy ? cx : cy;
+        if (st->t == 0.0) dt = (double)0.000001f;
+        st->dt_old = st->dt;
+        st->dt = dt;
+        st->t = st->t + dt;
+    }
+    // re-sync U* with U^n on tiles that went inactive
     const int nDe = st->nDeact;
     for (int k = blockIdx.x; k < nDe; k += gridDim.x) {
         const int tile = P.deact[k];
         const int bX = tile % P.nBX, bY = tile / P.nBX;
         if (tid < TW * TH) {
-            int tx = tid % TW, ty = tid / TW;
-            int i = bX * TW + tx + 2, j = bY * TH + ty + 2;
+            const int i = bX * TW + tid % TW + 2, j = bY * TH + tid / TW + 2;
             auto cp = [&](int jj, int ii) {
                 for (int f = 0; f < 3; f++) P.B[cidx(P, f, jj, ii)] = P.A[cidx(P, f, jj, ii)];
             };
@@ -501,58 +581,6 @@ __global__ void __launch_bounds__(NT) k_speed(const __grid_constant__ CUtensorMa
                 }
             }
         }
-    }
-}
-
-// ---------------------------------------------------------------- k_dt
-// Simulator::ComputeTimestep (simulator.cu:540-566) on device.  The max runs
-// over every tile (stale speeds of inactive tiles included, A5).  The last
-// CTA to finish turns the maxima into dt with the reference's rounding
-// points (fmaxf on the scaled maxima, FP64 division), then t += dt.
-__global__ void __launch_bounds__(256) k_dt(Params P) {
-    DevState* s = P.st;
-    if (s->stop) return;
-    float mx = 0.f, my = 0.f;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < P.gridSize; b += gridDim.x * blockDim.x) {
-        mx = fmaxf(mx, P.mx[b]);
-        my = fmaxf(my, P.my[b]);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
-    }
-    __shared__ float rx[8], ry[8];
-    __shared__ bool last;
-    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) {
-        rx[w] = mx;
-        ry[w] = my;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < (int)(blockDim.x >> 5); k++) {
-            mx = fmaxf(mx, rx[k]);
-            my = fmaxf(my, ry[k]);
-        }
-        // speeds are non-negative: their bit patterns order like the values
-        atomicMax(&s->max_bits[0], __float_as_uint(mx));
-        atomicMax(&s->max_bits[1], __float_as_uint(my));
-        __threadfence();
-        unsigned tk = atomicAdd(&s->ticket, 1u);
-        last = (tk == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        double maxx = (double)__uint_as_float(atomicOr(&s->max_bits[0], 0u));
-        double maxy = (double)__uint_as_float(atomicOr(&s->max_bits[1], 0u));
-        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
-        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
-        double dt = cx < cy ? cx : cy;
-        if (s->t == 0.0) dt = (double)0.000001f;
-        s->dt_old = s->dt;
-        s->dt = dt;
-        s->t = s->t + dt;
     }
 }
 
@@ -603,14 +631,8 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
     const DevState* st = P.st;
     if (st->stop) return;
     const int tid = threadIdx.x;
-    if (tid == 0) {
-        prefetch_tmap(&tmIn);
-        prefetch_tmap(&tmE);
-        mbar_init(&S.bar, 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
-    uint32_t phase = 0;
+    const int nAct = st->nActive;
+    tilePrologue(S, &tmIn, &tmE, P, nAct);
     const float kappa = P.kappa;
     const uint32_t fl = P.flags;
     const bool euler = (fl & F_EULER) != 0;
@@ -625,35 +647,28 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
     float* Uout = (STAGE == 1) ? P.B : P.A;
     const float* Fin = (STAGE == 1) ? P.FA : P.FB;
     float* Fout = (STAGE == 1) ? P.FB : P.FA;
-    const int nAct = st->nActive;
 
-    for (int k = blockIdx.x; k < nAct; k += gridDim.x) {
+    uint32_t ph[2] = {0u, 0u};
+    int bsel = 0;
+    for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];
-        int i0, j0;
-        if (!tileHasInterior(P, tile, i0, j0)) {
-            if (STAGE == 2 && tid == 0) {
-                P.mx[tile] = 0.f;
-                P.my[tile] = 0.f;
-            }
-            continue;
-        }
-        const int bX = tile % P.nBX, bY = tile / P.nBX;
-        __syncthreads();
-        bool ok = stageTile(S, &tmIn, &tmE, bX, bY, phase);
-        if (!__syncthreads_and(ok)) {
+        int bX, bY, i0, j0;
+        tileOrigin(P, tile, bX, bY, i0, j0);
+        if (!tileAcquire(S, &tmIn, &tmE, P, bsel, ph, k + gridDim.x, nAct)) {
             if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
             return;
         }
+        const TileBuf& T = S.buf[bsel];
         // ---- x reconstruction: cells i0-1 .. i0+16 on the 14 tile rows
         if (tid < TH * (TW + 2)) {
             int r = tid / (TW + 2), c = tid % (TW + 2);
             int sr = r + 2, sc = c + 1;
-            Rec R = construct(S.in[0][sr][sc], S.in[1][sr][sc], S.in[2][sr][sc],
-                              S.in[0][sr][sc + 1], S.in[1][sr][sc + 1], S.in[2][sr][sc + 1],
-                              S.in[0][sr][sc - 1], S.in[1][sr][sc - 1], S.in[2][sr][sc - 1],
-                              S.e[0][sr][sc], S.e[1][sr][sc],
-                              S.e[1][sr][sc] - S.e[0][sr][sc + 1],
-                              S.e[1][sr][sc - 1] - S.e[0][sr][sc]);
+            Rec R = construct(T.in[0][sr][sc], T.in[1][sr][sc], T.in[2][sr][sc],
+                              T.in[0][sr][sc + 1], T.in[1][sr][sc + 1], T.in[2][sr][sc + 1],
+                              T.in[0][sr][sc - 1], T.in[1][sr][sc - 1], T.in[2][sr][sc - 1],
+                              T.e[0][sr][sc], T.e[1][sr][sc],
+                              T.e[1][sr][sc] - T.e[0][sr][sc + 1],
+                              T.e[1][sr][sc - 1] - T.e[0][sr][sc]);
             S.rec.x.P[0][r][c] = R.hP;
             S.rec.x.P[1][r][c] = R.uP;
             S.rec.x.P[2][r][c] = R.vP;
@@ -689,12 +704,12 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
         if (tid < (TH + 2) * TW) {
             int r = tid / TW, c = tid % TW;
             int sr = r + 1, sc = c + 2;
-            Rec R = construct(S.in[0][sr][sc], S.in[1][sr][sc], S.in[2][sr][sc],
-                              S.in[0][sr + 1][sc], S.in[1][sr + 1][sc], S.in[2][sr + 1][sc],
-                              S.in[0][sr - 1][sc], S.in[1][sr - 1][sc], S.in[2][sr - 1][sc],
-                              S.e[2][sr][sc], S.e[3][sr][sc],
-                              S.e[3][sr][sc] - S.e[2][sr + 1][sc],
-                              S.e[3][sr - 1][sc] - S.e[2][sr][sc]);
+            Rec R = construct(T.in[0][sr][sc], T.in[1][sr][sc], T.in[2][sr][sc],
+                              T.in[0][sr + 1][sc], T.in[1][sr + 1][sc], T.in[2][sr + 1][sc],
+                              T.in[0][sr - 1][sc], T.in[1][sr - 1][sc], T.in[2][sr - 1][sc],
+                              T.e[2][sr][sc], T.e[3][sr][sc],
+                              T.e[3][sr][sc] - T.e[2][sr + 1][sc],
+                              T.e[3][sr - 1][sc] - T.e[2][sr][sc]);
             S.rec.y.P[0][r][c] = R.hP;
             S.rec.y.P[1][r][c] = R.uP;
             S.rec.y.P[2][r][c] = R.vP;
@@ -723,11 +738,11 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
             const int i = i0 + tx, j = j0 + ty;
             if (i <= P.nx - 3 && j <= P.ny - 3) {
                 const size_t c = cidx(P, 0, j, i);
-                const float hC = S.in[0][ty + 2][tx + 2];
-                const float hu0 = S.in[1][ty + 2][tx + 2];
-                const float hv0 = S.in[2][ty + 2][tx + 2];
-                const float eW = S.e[0][ty + 2][tx + 2], eE = S.e[1][ty + 2][tx + 2];
-                const float eS = S.e[2][ty + 2][tx + 2], eN = S.e[3][ty + 2][tx + 2];
+                const float hC = T.in[0][ty + 2][tx + 2];
+                const float hu0 = T.in[1][ty + 2][tx + 2];
+                const float hv0 = T.in[2][ty + 2][tx + 2];
+                const float eW = T.e[0][ty + 2][tx + 2], eE = T.e[1][ty + 2][tx + 2];
+                const float eS = T.e[2][ty + 2][tx + 2], eN = T.e[3][ty + 2][tx + 2];
                 // bed-slope source, grid.cu:701,751-752
                 const float S1 = -kG * hC * ((eE - eW) * P.inv_dx);
                 const float S2 = -kG * hC * ((eN - eS) * P.inv_dy);
@@ -833,13 +848,53 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
             if (tid == 0) P.wet[tile] = (uint8_t)((!(fl & F_TILE_ACC)) || any);
         }
         if (STAGE == 2) {
-            float mxv = blockMax(spx, S.red[0], 0);
-            __syncthreads();
-            float myv = blockMax(spy, S.red[1], 1);
+            float mxv = blockMax(spx, S.red[0]);
+            float myv = blockMax(spy, S.red[1]);
             if (tid == 0) {
                 P.mx[tile] = mxv;
                 P.my[tile] = myv;
             }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------- k_commit
+// Euler mode (euler_integration, simulator.cu:801) has a single stage: its
+// result, written to the stage buffer so that no CTA reads a halo cell
+// another CTA is updating, is copied back over U^n for the active tiles
+// (interior cells and the ghost cells they own), together with F.
+__global__ void __launch_bounds__(NT) k_commit(Params P) {
+    const DevState* st = P.st;
+    if (st->stop) return;
+    const int nAct = st->nActive;
+    const int tid = threadIdx.x;
+    for (int k = blockIdx.x; k < nAct; k += gridDim.x) {
+        const int tile = P.act[k];
+        const int bX = tile % P.nBX, bY = tile / P.nBX;
+        if (tid >= TW * TH) continue;
+        const int i = bX * TW + tid % TW + 2, j = bY * TH + tid / TW + 2;
+        if (!(i <= P.nx - 3 && j <= P.ny - 3)) continue;
+        auto cp = [&](int jj, int ii) {
+            for (int f = 0; f < 3; f++) P.A[cidx(P, f, jj, ii)] = P.B[cidx(P, f, jj, ii)];
+        };
+        cp(j, i);
+        if (P.flags & F_INFIL) P.FA[cidx(P, 0, j, i)] = P.FB[cidx(P, 0, j, i)];
+        if (i == 2) {
+            cp(j, 0);
+            cp(j, 1);
+        }
+        if (i == P.nx - 3) {
+            cp(j, P.nx - 2);
+            cp(j, P.nx - 1);
+        }
+        if (j == 2) {
+            cp(0, i);
+            cp(1, i);
+        }
+        if (j == P.ny - 3) {
+            cp(P.ny - 2, i);
+            cp(P.ny - 1, i);
         }
     }
 }

@@ -90,7 +90,8 @@ class Case:
     flags: int = 0
     series: dict = dataclasses.field(default_factory=dict)  # which -> (times_s f32, rates f32)
     src_idx: np.ndarray | None = None
-    rain_maps: list | None = None  # list of (h_ny, h_nx) m/s maps
+    rain_maps: list | None = None  # two (h_ny, h_nx) maps in m/s bracketing the run
+    map_times: tuple | None = None  # (t0, t1) of those two maps
     map_dt: float = 0.0
 
     @property
@@ -248,8 +249,16 @@ def config3(N=8192, seed=2, cell=2.0, tf=10800.0, nblocks=4000) -> Case:
     nC = np.where(roof, 0.015, 0.05)
     n = cell_mean(nC)
     t, r = csv_series([0, 3], [5, 5])
-    return Case(name=f"config3_{N}", B=z, cell=cell, n=n, tf=tf,
+    case = Case(name=f"config3_{N}", B=z, cell=cell, n=n, tf=tf,
                 flags=RAIN_GRID | DRAIN_UNIFORM | TILE_ACCEL, series={1: (t, r)}, map_dt=300.0)
+    # the first two of the rain maps (every 300 s), interpolated in time
+    maps = []
+    for k in range(2):
+        mm = rain_map_corners(z.shape, cell, np.random.default_rng(1000 + seed * 100 + k))
+        maps.append(cell_mean(mm) / (3600.0 * 1000.0))
+    case.rain_maps = maps
+    case.map_times = (0.0, 300.0)
+    return case
 
 
 def smooth_field(shape, corr_cells, rng):

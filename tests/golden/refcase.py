@@ -49,6 +49,20 @@ def write_case(case, d, nsteps, dump=(), timing=False, maps=None, rates=None, sr
             f.write(f"{k} {v}\n")
 
 
+def write_state(d, snap):
+    """A hotstart-like state (reference representation) for refrun."""
+    for k in ("w", "hu", "hv", "F"):
+        if k in snap and snap[k] is not None:
+            np.asarray(snap[k], np.float64).tofile(os.path.join(d, f"state_{k}.bin"))
+    np.asarray(snap["wet"], np.uint8).tofile(os.path.join(d, "state_wet.bin"))
+    np.asarray(snap["active"], np.int32).tofile(os.path.join(d, "state_active.bin"))
+    np.asarray(snap["mx"], np.float64).tofile(os.path.join(d, "state_mx.bin"))
+    np.asarray(snap["my"], np.float64).tofile(os.path.join(d, "state_my.bin"))
+    with open(os.path.join(d, "params.txt"), "a") as f:
+        f.write(f"state 1\nstate_nactive {len(snap['active'])}\n")
+        f.write(f"t0 {float(snap['t'])!r}\ndt0 {float(snap['dt'])!r}\n")
+
+
 def read_dump(out, step, nx, ny, grid_size, names=("w", "hu", "hv")):
     pre = os.path.join(out, f"s{step:05d}_")
     r = {}
