@@ -180,6 +180,39 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total,
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
 
+/* Volume sum for callers that cannot allocate device memory.  This entry
+ * point has no counterpart in the reference.
+ *
+ * Some callers must not call cudaMalloc: a coupled model (for instance the
+ * 1D drainage side of a 1D-2D coupling) that checks the 2D mass balance from
+ * inside its own time loop, whose device memory comes from its own pool, or
+ * that is recording work on a stream it does not want synchronised --
+ * cudaMalloc and cudaFree synchronise the whole device.  This call takes
+ * only the caller's buffers and allocates nothing: its scratch (one FP64
+ * compensated partial sum per grid row) is a fixed array inside this
+ * library's device image, present on every GPU that loads the library until
+ * the process exits.
+ *
+ * depth: device pointer to an FP32 depth field, h_ny rows with leading
+ *        dimension ld floats, cell (j,i) at depth[j*ld + i]; only interior
+ *        cells (2 <= i,j <= n-3) are summed;
+ * infil: optional device pointer to the Green-Ampt F field, same layout;
+ * volume_dev: device pointer to one double receiving sum(h [+ F]) (metres of
+ *        depth summed; multiply by dx*dy for m^3);
+ * stream: the cudaStream_t to launch on (NULL: the legacy default stream).
+ * The call is asynchronous on `stream`.
+ * Limits: h_ny <= RIFT_NOALLOC_MAX_ROWS, else RIFT_ERR_TOO_LARGE and nothing
+ * is launched.  All calls on a device share the scratch array, which keeps
+ * the last call's partial sums (each call rewrites every partial it reads);
+ * calls that overlap on the GPU race on it and must be serialised by the
+ * caller.  The first call on each device looks up the array's address with
+ * that device current; make it before recording any stream capture there. */
+#define RIFT_NOALLOC_MAX_ROWS 32768
+#define RIFT_ERR_TOO_LARGE 7
+int rift_volume_noalloc(const float* depth, const float* infil, int32_t h_nx,
+                        int32_t h_ny, int64_t ld, double* volume_dev,
+                        void* stream);
+
 const char* rift_last_error(rift_handle* h);
 void rift_destroy(rift_handle* h);
 

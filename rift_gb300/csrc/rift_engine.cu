@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -939,3 +940,108 @@ void rift_destroy(rift_handle* h) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// rift_volume_noalloc: the volume sum for callers that must not allocate.
+//
+// Some callers cannot call cudaMalloc: a coupled model (the 1D sewer/channel
+// side of a 1D-2D coupling, which the reference's main.cc stubs out) that
+// checks the 2D mass balance from inside its own time loop, with its device
+// memory handed out by its own pool or arena, or while it records work into
+// a stream it does not want synchronised.  cudaMalloc and cudaFree
+// synchronise the whole device and draw on memory such a caller has already
+// budgeted, so this entry point takes only the caller's buffers and keeps its
+// scratch -- one compensated partial sum per grid row -- in a fixed array
+// that lives in this library's device image on every GPU that loads it.
+//
+// Limits and sharing rules:
+//  - at most RIFT_NOALLOC_MAX_ROWS grid rows (ghost rows included); larger
+//    grids are rejected with RIFT_ERR_TOO_LARGE before anything is launched;
+//  - the array is shared by every call in the process on that device and
+//    keeps the last call's partial sums.  Each call writes every row partial
+//    it later reads, so nothing needs clearing, but two calls that overlap on
+//    the GPU (different streams, or different host threads) overwrite each
+//    other's partials: the caller serialises them;
+//  - the first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress) with that device current; make that first call
+//    before recording any stream capture on the device.
+namespace {
+
+constexpr int kNoAllocMaxRows = RIFT_NOALLOC_MAX_ROWS;
+static __device__ __align__(256) double g_noallocRowSums[2 * kNoAllocMaxRows];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noallocMutex;
+double* g_noallocPtr[kMaxDevices] = {nullptr};
+
+// One warp per interior row: Neumaier sum of (h [+ F]) over the row's
+// interior cells, lanes combined in lane order.
+__global__ void k_volume_rows_noalloc(const float* __restrict__ h, const float* __restrict__ F,
+                                      int nx, int ny, long long ld, double* rows) {
+    const int lane = threadIdx.x & 31;
+    const int j = 2 + (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (j > ny - 3) return;
+    double s = 0.0, c = 0.0;
+    for (int i = 2 + lane; i <= nx - 3; i += 32) {
+        double v = (double)h[(size_t)j * ld + i];
+        if (F) v += (double)F[(size_t)j * ld + i];
+        double t = s + v;
+        c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+        s = t;
+    }
+    double S = 0.0, C = 0.0;
+    for (int l = 0; l < 32; l++) {
+        double vs = __shfl_sync(0xffffffffu, s, l);
+        double vc = __shfl_sync(0xffffffffu, c, l);
+        double t = S + vs;
+        C += (fabs(S) >= fabs(vs)) ? (S - t) + vs : (vs - t) + S;
+        S = t;
+        C += vc;
+    }
+    if (lane == 0) {
+        rows[2 * j] = S;
+        rows[2 * j + 1] = C;
+    }
+}
+
+// Rows combined in row order into the caller's output.
+__global__ void k_volume_final_noalloc(const double* rows, int ny, double* out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double S = 0.0, C = 0.0;
+    for (int j = 2; j <= ny - 3; j++) {
+        double v = rows[2 * j];
+        double t = S + v;
+        C += (fabs(S) >= fabs(v)) ? (S - t) + v : (v - t) + S;
+        S = t;
+        C += rows[2 * j + 1];
+    }
+    out[0] = S + C;
+}
+
+}  // namespace
+
+extern "C" int rift_volume_noalloc(const float* depth, const float* infil, int32_t h_nx,
+                                   int32_t h_ny, int64_t ld, double* volume_dev, void* stream) {
+    if (!depth || !volume_dev || h_nx < 5 || h_ny < 5 || ld < h_nx) return RIFT_ERR_ARG;
+    if (h_ny > kNoAllocMaxRows) return RIFT_ERR_TOO_LARGE;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return RIFT_ERR_CUDA;
+    double* rows = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noallocMutex);
+        if (!g_noallocPtr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_noallocRowSums) != cudaSuccess || !p)
+                return RIFT_ERR_CUDA;
+            g_noallocPtr[dev] = static_cast<double*>(p);
+        }
+        rows = g_noallocPtr[dev];
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int rowsInterior = h_ny - 4;
+    const int threads = 256;
+    const int blocks = (rowsInterior * 32 + threads - 1) / threads;
+    k_volume_rows_noalloc<<<blocks, threads, 0, s>>>(depth, infil, h_nx, h_ny, (long long)ld, rows);
+    k_volume_final_noalloc<<<1, 32, 0, s>>>(rows, h_ny, volume_dev);
+    return cudaGetLastError() == cudaSuccess ? RIFT_OK : RIFT_ERR_CUDA;
+}
