@@ -135,7 +135,10 @@ def device_timed_run(sim, steps):
     return ms, act_total, done, stage_ms, stage_act
 
 
-def run_ours(args):
+def run_ours(args, device=0, sync=None):
+    """One replica's bench line.  `sync` (multi-rank runs) is called on both
+    sides of the device-timed region: a barrier over the ranks plus a device
+    synchronize."""
     cfg = args.config
     case = make_case(cfg, args.N)
     interior = (case.h_nx - 4) * (case.h_ny - 4)
@@ -143,7 +146,7 @@ def run_ours(args):
 
     # ---- e2e through the C ABI with host buffers ----------------------------
     t0 = time.perf_counter()
-    sim = capi.Sim(case)
+    sim = capi.Sim(case, device=device).set_schedule(args.schedule)
     sim.setup()
     t_setup = time.perf_counter() - t0
     spin_up(sim, spin)
@@ -169,7 +172,11 @@ def run_ours(args):
     for _ in range(args.warmup):
         sim.step()
     clocks = ClockSampler().start()
+    if sync:
+        sync()
     ms, active_cells, done, stage_ms, stage_cells = device_timed_run(sim, args.steps)
+    if sync:
+        sync()
     clk = clocks.stop()
     steps = int(done)
     value = interior * steps / (ms * 1e-3)
@@ -208,14 +215,41 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_kind": peak_kind, "bytes_per_active_cell_update": bytes_per,
-                     "kernel": "k_stage (both RK stages, fused)"},
+                     "kernel": "RK stages 1+2 (k_march<1>, k_march<2> or k_stage<1>, "
+                               "k_stage<2>; one schedule runs, the other exits at entry)"},
         "clocks": clk,
-        "gpu_launches": steps * (7 if case.flags & synth.RAIN_GRID else 6),
+        "gpu_launches": steps * launches_per_step(case.flags),
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, snap, args)
     sim.close()
     return line
+
+
+def launches_per_step(flags):
+    """Kernels one step's graph launches: k_track (gridded rain or surge),
+    k_grow, the speed/dt kernel and the stage kernels of both schedules (the
+    schedule not chosen for the step exits at entry), k_commit in Euler mode."""
+    n = 1 + 2 + 2 + (1 if flags & synth.EULER else 2)
+    if flags & (synth.RAIN_GRID | synth.SURGE_GRID):
+        n += 1
+    return n
+
+
+def combine_replicas(line, world, allreduce_max):
+    """Whole-job line of a replicas-only run from this rank's line.  Every rank
+    ran the same workload on its own GPU: the job's time is the slowest rank's
+    (max over ranks) and the value counts the cell updates of all ranks.
+    `allreduce_max` maps a list of floats to their element-wise max over ranks."""
+    ms_max, inv_e2e = allreduce_max([line["ms_per_step"], 1.0 / line["e2e"]["value"]])
+    out = dict(line)
+    cells = line["config"]["cells"]
+    out["ms_per_step"] = ms_max
+    out["value"] = world * cells / (ms_max * 1e-3)
+    out["e2e"] = dict(line["e2e"], value=world / inv_e2e)
+    out["n_gpus"] = world
+    out["gpu_launches"] = line["gpu_launches"] * world
+    return out
 
 
 def cpu_baseline(case, snap, args, seconds=15.0):
@@ -294,6 +328,8 @@ def main():
     ap.add_argument("--spinup", type=float, default=None)
     ap.add_argument("--ref-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--schedule", type=int, default=-1,
+                    help="march kernels from this many active strips up (-1: engine default)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -306,16 +342,22 @@ def main():
         # replicas only: every rank runs the same workload on its own GPU
         import torch
         import torch.distributed as dist
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
         dist.init_process_group("nccl")
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         args.cpu_baseline = args.cpu_baseline and rank == 0
-        dist.barrier()
-        line = run_ours(args)
-        t = torch.tensor([line["ms_per_step"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+
+        def sync():
+            dist.barrier()
+            torch.cuda.synchronize()
+
+        def allreduce_max(vals):
+            t = torch.tensor(vals, dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return t.tolist()
+
+        line = combine_replicas(run_ours(args, device=local, sync=sync), world, allreduce_max)
         if rank == 0:
-            line["ms_per_step"] = float(t.item())
-            line["value"] = line["value"] * world
             print(json.dumps(line))
         dist.destroy_process_group()
         return

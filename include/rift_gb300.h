@@ -177,6 +177,13 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total,
                    double* active_total, double* steps_done, double* stage_ms,
                    double* active_cells);
 
+/* Kernel schedule (no reference counterpart; the reference launches one CTA
+ * per active tile): from march_min_strips active strips of 7 x 2 tiles
+ * upward the step runs the column-march kernels, below it the per-tile
+ * kernels.  Both give the same results.  -1 restores the default (one strip
+ * per resident march CTA); 0 forces the march, a huge value the tiles. */
+int rift_set_schedule(rift_handle* h, int32_t march_min_strips);
+
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
 

@@ -260,7 +260,7 @@ int main(int argc, char** argv) {
     size_t height = (size_t)nBY * BR_, height_p1 = height + 1;
     // The reference kernels touch up to two rows past the allocated height and
     // two columns past the width (ComputeFluxes_k on the last tile row and
-    // column; A15 in the reference register).  Every pitched array here gets
+    // column, past the allocation).  Every pitched array here gets
     // PAD extra rows and columns so those accesses stay inside this
     // allocation; the reference's arithmetic on interior cells never reads
     // them.

@@ -264,7 +264,7 @@ void refreshMap(rift_oracle* o, int which) {
 }
 
 // ApplyBoundariesX_k / ApplyBoundariesY_k (grid.cu:1325-1406): critical-depth
-// outflow ghosts; X clamps HL at epsilon, Y does not (A4); corners untouched.
+// outflow ghosts; X clamps HL at epsilon, Y does not; corners untouched.
 void applyBoundaries(rift_oracle* o) {
     const FM& m = o->m;
     const int nx = o->nx, ny = o->ny;
@@ -321,7 +321,7 @@ void grow(rift_oracle* o) {
             for (int b = 1; b < o->gridSize; b++)
                 if (!o->prev_active[b]) tracked.push_back(b);
         }
-        // A9: the Track kernels take rows from blockY*BLOCK_COLS (16, not 14).
+        // The Track kernels take rows from blockY*BLOCK_COLS (16, not 14).
         auto track = [&](int which, bool surge) {
             std::vector<uint8_t> setw(o->gridSize, 0);
             for (int b : tracked) {
@@ -347,7 +347,7 @@ void grow(rift_oracle* o) {
         if (rg) track(RIFT_MAP_RAIN, false);
         if (sg) track(RIFT_MAP_SURGE, true);
     }
-    // Grow_k: 4-neighbour dilation, false outside the tile grid.  A8: tile 0
+    // Grow_k: 4-neighbour dilation, false outside the tile grid.  Tile 0
     // encodes as 0 either way and so is always kept by is_nonnegative.
     for (int bY = 0; bY < nBY; bY++)
         for (int bX = 0; bX < nBX; bX++) {
@@ -362,7 +362,7 @@ void grow(rift_oracle* o) {
 
 // ComputeFluxes_k (grid.cu:564-839) over the active tiles.  Fluxes read the
 // unclamped w of every cell; the w = BC clamp of grid.cu:748-749 is applied
-// after all tiles are done (the reference races here, A13).
+// after all tiles are done (in the reference neighbours may read either value).
 void computeFluxes(rift_oracle* o, double dtArg) {
     const FM& m = o->m;
     const int nx = o->nx, ny = o->ny, nBX = o->nBX;
@@ -484,7 +484,7 @@ void computeFluxes(rift_oracle* o, double dtArg) {
 }
 
 // Simulator::ComputeTimestep (simulator.cu:540-566): max over ALL tiles,
-// stale entries of inactive tiles included (A5).
+// stale entries of inactive tiles included.
 void computeTimestep(rift_oracle* o) {
     const FM& m = o->m;
     double mxv = *std::max_element(o->mx.begin(), o->mx.end());
@@ -622,7 +622,8 @@ void integrate2(rift_oracle* o) {
 }
 
 // Simulator::UpdateSource (simulator.cu:500-538) for device-style series:
-// interpolate at float(t), then divide the float rate in place (A11).
+// interpolate at float(t), then divide the float rate in place (every step,
+// so outside the CSV time range the rate keeps shrinking).
 void updateSeries(rift_oracle* o) {
     const float tf = (float)o->t;
     if (o->series[2].on) {

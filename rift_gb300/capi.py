@@ -71,6 +71,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
     ns["set_map_factor"] = _sig(lib, p + "set_map_factor", C.c_int, [_P, C.c_int32, C.c_double])
     ns["set_map_times"] = _sig(lib, p + "set_map_times", C.c_int,
                                [_P, C.c_int32, C.c_double, C.c_double])
+    if hasattr(lib, p + "set_schedule"):
+        ns["set_schedule"] = _sig(lib, p + "set_schedule", C.c_int, [_P, C.c_int32])
     ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
     ns["step"] = _sig(lib, p + "step", C.c_int, [_P, _D, _D])
     ns["run"] = _sig(lib, p + "run", C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _I])
@@ -209,6 +211,13 @@ class Sim:
 
     def set_map_times(self, which, t0, t1):
         self._check(self.f["set_map_times"](self.h, which, t0, t1), "set_map_times")
+
+    def set_schedule(self, march_min_strips):
+        """Kernel schedule: march kernels from this many active strips up
+        (-1 default, 0 always march, a huge value always per-tile)."""
+        if "set_schedule" in self.f:
+            self._check(self.f["set_schedule"](self.h, march_min_strips), "set_schedule")
+        return self
 
     # -- stepping ---------------------------------------------------------
     def step(self):

@@ -24,6 +24,7 @@
 
 #include "../../include/rift_gb300.h"
 #include "rift_kernels.cuh"
+#include "rift_march.cuh"
 
 using namespace rift;
 
@@ -52,7 +53,12 @@ PFN_encodeTiled getEncodeTiled() {
 struct rift_handle {
     rift_grid_desc g{};
     int nx = 0, ny = 0, nBX = 0, nBY = 0, gridSize = 0, pitch = 0, rows = 0;
-    int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0;
+    int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0, gridMarch = 0;
+    int nSX = 0, nSY = 0;
+    int marchMin = 0;  // active strips from which the march kernels run
+    int* strips = nullptr;
+    uint8_t* stripFlag = nullptr;
+    CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
     cudaStream_t stream = nullptr;
     float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
     float *FA = nullptr, *FB = nullptr, *hmax = nullptr, *qmax = nullptr, *twet = nullptr;
@@ -140,6 +146,11 @@ Params makeParams(rift_handle* h) {
     P.act = h->act;
     P.deact = h->deact;
     P.inact = h->inact;
+    P.strips = h->strips;
+    P.stripFlag = h->stripFlag;
+    P.nSX = h->nSX;
+    P.nSY = h->nSY;
+    P.marchMin = h->marchMin;
     P.mx = h->mx;
     P.my = h->my;
     P.srcIdx = h->srcIdx;
@@ -154,12 +165,13 @@ Params makeParams(rift_handle* h) {
     return P;
 }
 
-int encodeMap(rift_handle* h, CUtensorMap* tm, float* base, int nfields) {
+int encodeMap(rift_handle* h, CUtensorMap* tm, float* base, int nfields, int boxW = SW,
+              int boxH = SH) {
     PFN_encodeTiled enc = getEncodeTiled();
     if (!enc) return fail(h, RIFT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->rows, (cuuint64_t)nfields};
     cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)h->plane() * 4};
-    cuuint32_t box[3] = {(cuuint32_t)SW, (cuuint32_t)SH, (cuuint32_t)nfields};
+    cuuint32_t box[3] = {(cuuint32_t)boxW, (cuuint32_t)boxH, (cuuint32_t)nfields};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -182,12 +194,18 @@ void enqueueStep(rift_handle* h) {
     if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
         k_track<<<h->gridTrack, NT, 0, s>>>(P);
     k_grow<<<1, GROW_T, 0, s>>>(P);
+    // per-tile and march variants of each pass; the device keeps one of them
+    // (useMarch) and the other returns at once
     k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
+    k_march<0><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
     k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
-    if (!h->has(RIFT_F_EULER))
+    k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+    if (!h->has(RIFT_F_EULER)) {
         k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
-    else
+        k_march<2><<<h->gridMarch, MT, 0, s>>>(h->tmBm, h->tmEm, P);
+    } else {
         k_commit<<<h->gridStage, NT, 0, s>>>(P);
+    }
 }
 
 int buildGraph(rift_handle* h) {
@@ -394,12 +412,26 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     std::memset(h->hst, 0, sizeof(DevState));
     CUDA_TRY(h, cudaMalloc(&h->volPartial, 2 * 1024 * sizeof(double)));
     if ((r = encodeMap(h, &h->tmA, h->A, 3)) || (r = encodeMap(h, &h->tmB, h->B, 3)) ||
-        (r = encodeMap(h, &h->tmE, h->E, 4)))
+        (r = encodeMap(h, &h->tmE, h->E, 4)) ||
+        (r = encodeMap(h, &h->tmAm, h->A, 3, MBOXW, MRC)) ||
+        (r = encodeMap(h, &h->tmBm, h->B, 3, MBOXW, MRC)) ||
+        (r = encodeMap(h, &h->tmEm, h->E, 4, MBOXW, MRC)))
         return r;
+    h->nSX = (h->nBX + STRIP_TX - 1) / STRIP_TX;
+    h->nSY = (h->nBY + STRIP_TY - 1) / STRIP_TY;
+    const int NS = h->nSX * h->nSY;
+    CUDA_TRY(h, cudaMalloc(&h->strips, (size_t)NS * 4));
+    CUDA_TRY(h, cudaMalloc(&h->stripFlag, NS));
+    CUDA_TRY(h, cudaMemset(h->stripFlag, 0, NS));
     int occ = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_stage<1>, NT, 0);
     if (occ < 1) occ = 1;
     h->gridStage = std::max(1, std::min(G, h->numSMs * occ));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_march<2>, MT, 0);
+    if (occ < 1) occ = 1;
+    h->gridMarch = std::max(1, std::min(NS, h->numSMs * occ));
+    // the march pays off once every resident march CTA has a strip of its own
+    h->marchMin = h->numSMs * occ;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_speed_dt, NT, 0);
     if (occ < 1) occ = 1;
     h->gridSpeed = std::max(1, std::min(G, h->numSMs * occ));
@@ -604,6 +636,15 @@ int rift_set_map_factor(rift_handle* h, int32_t which, double factor) {
     if (rc) return rc;
     h->hst->factor[which] = (float)factor;
     return pushState(h);
+}
+
+int rift_set_schedule(rift_handle* h, int32_t march_min_strips) {
+    if (!h) return RIFT_ERR_ARG;
+    int occ = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_march<2>, MT, 0);
+    h->marchMin = march_min_strips >= 0 ? march_min_strips : h->numSMs * std::max(occ, 1);
+    destroyGraph(h);
+    return RIFT_OK;
 }
 
 int rift_set_map_times(rift_handle* h, int32_t which, double t0, double t1) {
@@ -896,12 +937,16 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
             k_track<<<h->gridTrack, NT, 0, s>>>(P);
         k_grow<<<1, GROW_T, 0, s>>>(P);
         k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
+        k_march<0><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
         CUDA_TRY(h, cudaEventRecord(e0, s));
         k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
-        if (!h->has(RIFT_F_EULER))
+        k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+        if (!h->has(RIFT_F_EULER)) {
             k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
-        else
+            k_march<2><<<h->gridMarch, MT, 0, s>>>(h->tmBm, h->tmEm, P);
+        } else {
             k_commit<<<h->gridStage, NT, 0, s>>>(P);
+        }
         CUDA_TRY(h, cudaEventRecord(e1, s));
         CUDA_TRY(h, cudaEventSynchronize(e1));
         float sm = 0.f;
@@ -930,7 +975,8 @@ void rift_destroy(rift_handle* h) {
     for (int k = 0; k < 3; k++)
         for (int q = 0; q < 2; q++)
             if (h->maps[k][q]) cudaFree(h->maps[k][q]);
-    for (void* p : {(void*)h->wet, (void*)h->prevAct, (void*)h->act, (void*)h->deact,
+    for (void* p : {(void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
+                    (void*)h->act, (void*)h->deact,
                     (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,
                     (void*)h->srcTileList, (void*)h->st, (void*)h->volPartial})
         if (p) cudaFree(p);

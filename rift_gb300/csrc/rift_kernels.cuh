@@ -11,7 +11,7 @@
 //               with warp ballots and one block scan per 1024 tiles
 //   k_speed_dt: per-tile local-speed maxima on U^n (the speed output of the
 //               first ComputeFluxes, grid.cu:813-838), the max over every
-//               tile (stale speeds of inactive tiles included, A5) and, in
+//               tile (stale speeds of inactive tiles included) and, in
 //               the last CTA, dt and t (Simulator::ComputeTimestep,
 //               simulator.cu:540-566); also re-syncs the stage buffer of
 //               tiles that just went inactive
@@ -40,6 +40,8 @@ constexpr int SW = TW + 4;      // staged block width  (2-cell halo)
 constexpr int SH = TH + 4;      // staged block height
 constexpr int NT = 256;         // threads per tile CTA
 constexpr int GROW_T = 1024;    // threads of the single-CTA grow kernel
+constexpr int STRIP_TX = 7;     // march work item: 7 x 2 tiles = 112 x 28 cells
+constexpr int STRIP_TY = 2;
 constexpr int MAX_SERIES = 4096;
 
 // flag bits, identical to include/rift_gb300.h
@@ -61,11 +63,12 @@ struct DevState {
     int map_timed[3];
     float rain_rate;   // uniform rates, m/s, as the reference's float rates
     float drain_rate;
-    float ser_interp[3];  // Source::interpolated_rate state (A11)
+    float ser_interp[3];  // Source::interpolated_rate state, divided in place each step
     float factor[3];      // map interpolation factors
     unsigned max_bits[2];
     unsigned ticket;
     int nActive, nDeact, nInact;
+    int nStrips;       // strips of the march kernels holding an active tile
     int stop;
     int steps_done;
     unsigned long long activeCells;  // interior cells of active tiles, summed over steps
@@ -99,6 +102,10 @@ struct Params {
     int* act;          // active tiles that hold interior cells
     int* deact;
     int* inact;
+    int* strips;       // march work items (strip ids) holding an active tile
+    uint8_t* stripFlag;
+    int nSX, nSY;      // strip grid (strips of 7 x 2 tiles)
+    int marchMin;      // active strips from which the march kernels run
     float* mx;
     float* my;
     const int* srcIdx;      // flat h-grid indices j*nx+i
@@ -225,9 +232,95 @@ __device__ __forceinline__ float blockMax(float v, float* red) {
     __syncthreads();
     float r = 0.f;
     if (threadIdx.x == 0)
-        for (int k = 0; k < NT / 32; k++) r = fmaxf(r, red[k]);
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) r = fmaxf(r, red[k]);
     return r;
 }
+
+// Stale speed maxima of the tiles that are not active this step, over this
+// thread's grid-stride slice of the tile grid.
+__device__ __forceinline__ void staleMax(const Params& P, float& amx, float& amy) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < P.gridSize; b += gridDim.x * blockDim.x)
+        if (!P.prevAct[b]) {
+            amx = fmaxf(amx, P.mx[b]);
+            amy = fmaxf(amy, P.my[b]);
+        }
+}
+
+// Simulator::ComputeTimestep (simulator.cu:540-566) on device: block max of
+// stale and new tile speeds, one atomic per CTA; the last CTA to finish turns
+// the maxima into dt with the reference's rounding points (fmaxf on the
+// scaled maxima, FP64 division) and advances t.  tmx/tmy are the CTA's new
+// tile maxima, held by thread 0.
+__device__ __forceinline__ void finishDt(const Params& P, float amx, float amy, float tmx,
+                                         float tmy, float* red0, float* red1, bool* last) {
+    DevState* st = P.st;
+    const int tid = threadIdx.x;
+    float bmx = blockMax(fmaxf(amx, tid == 0 ? tmx : 0.f), red0);
+    float bmy = blockMax(fmaxf(amy, tid == 0 ? tmy : 0.f), red1);
+    if (tid == 0) {
+        // speeds are non-negative: their bit patterns order like the values
+        atomicMax(&st->max_bits[0], __float_as_uint(bmx));
+        atomicMax(&st->max_bits[1], __float_as_uint(bmy));
+        __threadfence();
+        *last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (*last && tid == 0) {
+        __threadfence();
+        double maxx = (double)__uint_as_float(atomicOr(&st->max_bits[0], 0u));
+        double maxy = (double)__uint_as_float(atomicOr(&st->max_bits[1], 0u));
+        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
+        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
+        double dt = cx < cy ? cx : cy;
+        if (st->t == 0.0) dt = (double)0.000001f;
+        st->dt_old = st->dt;
+        st->dt = dt;
+        st->t = st->t + dt;
+    }
+}
+
+// Re-sync U* with U^n on the tiles that went inactive this step (interior
+// cells and the ghost cells they own): the stage kernels read U* in the halo
+// of active tiles, and for an inactive tile U* = U^n.
+__device__ __forceinline__ void resyncDeactivated(const Params& P) {
+    const int nDe = P.st->nDeact;
+    const int tid = threadIdx.x;
+    for (int k = blockIdx.x; k < nDe; k += gridDim.x) {
+        const int tile = P.deact[k];
+        const int bX = tile % P.nBX, bY = tile / P.nBX;
+        for (int q = tid; q < TW * TH; q += blockDim.x) {
+            const int i = bX * TW + q % TW + 2, j = bY * TH + q / TW + 2;
+            auto cp = [&](int jj, int ii) {
+                for (int f = 0; f < 3; f++) P.B[cidx(P, f, jj, ii)] = P.A[cidx(P, f, jj, ii)];
+            };
+            if (i < P.nx && j < P.ny) cp(j, i);
+            if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
+                if (i == 2) {
+                    cp(j, 0);
+                    cp(j, 1);
+                }
+                if (i == P.nx - 3) {
+                    cp(j, P.nx - 2);
+                    cp(j, P.nx - 1);
+                }
+                if (j == 2) {
+                    cp(0, i);
+                    cp(1, i);
+                }
+                if (j == P.ny - 3) {
+                    cp(P.ny - 2, i);
+                    cp(P.ny - 1, i);
+                }
+            }
+        }
+    }
+}
+
+// Schedule: the march kernels (strips of 7 x 2 tiles) run when at least
+// P.marchMin strips hold active tiles; below that the per-tile kernels, whose
+// finer work items keep a sparse or small grid spread over the GPU.  Both
+// are launched every step; the one not chosen returns at once.
+__device__ __forceinline__ bool useMarch(const Params& P) { return P.st->nStrips >= P.marchMin; }
 
 // Thread 0 issues the TMA loads of one tile's staged block into `b`.
 __device__ __forceinline__ void issueTile(TileBuf& b, uint64_t* bar, const CUtensorMap* tmIn,
@@ -259,9 +352,14 @@ __device__ __forceinline__ bool tileAcquire(StageSmem& S, const CUtensorMap* tmI
                                             const CUtensorMap* tmE, const Params& P, int b,
                                             uint32_t* ph, int kNext, int nAct) {
     bool ok = mbar_wait_bounded(&S.bar[b], ph[b]);
+    if (!__syncthreads_and(ok)) {
+        // error path: one more bounded wait for the copy still in flight, so
+        // that no TMA write lands after the CTA has left
+        mbar_wait_bounded(&S.bar[b], ph[b]);
+        return false;
+    }
     ph[b] ^= 1u;
-    ok = __syncthreads_and(ok);
-    if (ok && threadIdx.x == 0 && kNext < nAct)
+    if (threadIdx.x == 0 && kNext < nAct)
         issueTile(S.buf[b ^ 1], &S.bar[b ^ 1], tmIn, tmE, P, P.act[kNext]);
     return ok;
 }
@@ -269,7 +367,7 @@ __device__ __forceinline__ bool tileAcquire(StageSmem& S, const CUtensorMap* tmI
 // ---------------------------------------------------------------- sources
 // Uniform sources of Simulator::UpdateSource (simulator.cu:500-538): each CSV
 // series is interpolated at float(t) (source.cc:65-73) and its float state
-// divided in place (A11).  IEEE float ops (_rn intrinsics) keep the host's
+// divided in place every step.  IEEE float ops (_rn intrinsics) keep the host's
 // arithmetic (no contraction, exact division).
 __device__ __forceinline__ float seriesInterp(const float* T, const float* R, int n, float t,
                                               float cur) {
@@ -320,7 +418,8 @@ __device__ void beginStep(const Params& P, DevState* s) {
 
 // ---------------------------------------------------------------- k_track
 // TrackRainfall_k / TrackSurge_k over the tiles that were inactive after the
-// previous Grow.  A9: the rows come from blockY * BLOCK_COLS (16), not 14.
+// previous Grow.  The rows come from blockY * BLOCK_COLS (16), not 14, as in
+// the reference.
 __global__ void __launch_bounds__(NT) k_track(Params P) {
     const DevState* s = P.st;
     if (s->t >= s->t_stop) return;
@@ -354,7 +453,7 @@ __global__ void __launch_bounds__(NT) k_track(Params P) {
 
 // ---------------------------------------------------------------- k_grow
 // Single CTA.  active(t) = wet(t) | wet(4-neighbours), false outside the tile
-// grid; tile 0 is always kept (A8: it encodes as 0, never negative).  One
+// grid; tile 0 is always kept (the reference encodes it as 0, never negative).  One
 // block scan per 1024 tiles compacts (ascending) the active tiles that hold
 // interior cells, the inactive tiles other than tile 0 (tracked next step)
 // and the tiles that went from active to inactive.  Active tiles without
@@ -377,6 +476,9 @@ __global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
     if (stop) return;
     const int nBX = P.nBX, nBY = P.nBY;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nStripsAll = P.nSX * P.nSY;
+    for (int q = threadIdx.x; q < nStripsAll; q += GROW_T) P.stripFlag[q] = 0;
+    __syncthreads();
     int base[3] = {0, 0, 0};
     unsigned long long myCells = 0ull;
     for (int b0 = 0; b0 < P.gridSize; b0 += GROW_T) {
@@ -391,6 +493,7 @@ __global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
             const bool interior = i0 <= P.nx - 3 && j0 <= P.ny - 3;
             if (v && interior) {
                 flag[0] = 1;
+                P.stripFlag[(bY / STRIP_TY) * P.nSX + bX / STRIP_TX] = 1;
                 int ci = min(P.nx - 3, i0 + TW - 1) - i0 + 1;
                 int cj = min(P.ny - 3, j0 + TH - 1) - j0 + 1;
                 myCells += (unsigned long long)(ci * cj);
@@ -430,11 +533,34 @@ __global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
     }
     for (int o = 16; o > 0; o >>= 1) myCells += __shfl_xor_sync(0xffffffffu, myCells, o);
     if (lane == 0) atomicAdd(&cellSum, myCells);
-    __syncthreads();
+    // compaction of the strips (work items of the march kernels), ascending
+    int baseS = 0;
+    for (int q0 = 0; q0 < nStripsAll; q0 += GROW_T) {
+        const int q = q0 + threadIdx.x;
+        const int f = (q < nStripsAll && P.stripFlag[q]) ? 1 : 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        const int inWarp = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) wsum[0][w] = __popc(bal);
+        __syncthreads();
+        if (w == 0) {
+            int v0 = wsum[0][lane], x = v0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            wsum[0][lane] = x - v0;
+            if (lane == 31) wsum[0][32] = x;
+        }
+        __syncthreads();
+        if (f) P.strips[baseS + wsum[0][w] + inWarp] = q;
+        baseS += wsum[0][32];
+        __syncthreads();
+    }
     if (threadIdx.x == 0) {
         s->nActive = base[0];
         s->nDeact = base[1];
         s->nInact = base[2];
+        s->nStrips = baseS;
         s->activeCells += cellSum;
     }
 }
@@ -442,7 +568,7 @@ __global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
 // ------------------------------------------------------------- k_speed_dt
 // Per-tile speed maxima of U^n over the scheduled active tiles (what the
 // first ComputeFluxes of a step writes to mx/my, grid.cu:813-838); the max
-// over all tiles, stale entries of inactive tiles included (A5); in the last
+// over all tiles, stale entries of inactive tiles included; in the last
 // CTA, dt with the reference's rounding points (fmaxf of the scaled maxima,
 // FP64 division) and t += dt.  Also re-syncs U* with U^n on tiles that went
 // inactive this step (interior cells and the ghost cells they own).
@@ -451,18 +577,13 @@ __global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtenso
     __shared__ StageSmem S;
     __shared__ bool last;
     DevState* st = P.st;
-    if (st->stop) return;
+    if (st->stop || useMarch(P)) return;
     const int tid = threadIdx.x;
     const int nAct = st->nActive;
     tilePrologue(S, &tmA, &tmE, P, nAct);
     const float kappa = P.kappa;
-    // stale speeds of tiles that are not active this step
     float amx = 0.f, amy = 0.f;
-    for (int b = blockIdx.x * NT + tid; b < P.gridSize; b += gridDim.x * NT)
-        if (!P.prevAct[b]) {
-            amx = fmaxf(amx, P.mx[b]);
-            amy = fmaxf(amy, P.my[b]);
-        }
+    staleMax(P, amx, amy);
     uint32_t ph[2] = {0u, 0u};
     int bsel = 0;
     float tmx = 0.f, tmy = 0.f;  // thread 0: max of this CTA's new tile speeds
@@ -527,66 +648,14 @@ __global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtenso
         }
         __syncthreads();
     }
-    // dt: block max of stale + new speeds, one atomic per CTA, last CTA finishes
     __syncthreads();
-    float bmx = blockMax(fmaxf(amx, tid == 0 ? tmx : 0.f), S.red[0]);
-    float bmy = blockMax(fmaxf(amy, tid == 0 ? tmy : 0.f), S.red[1]);
-    if (tid == 0) {
-        // speeds are non-negative: their bit patterns order like the values
-        atomicMax(&st->max_bits[0], __float_as_uint(bmx));
-        atomicMax(&st->max_bits[1], __float_as_uint(bmy));
-        __threadfence();
-        last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (last && tid == 0) {
-        __threadfence();
-        double maxx = (double)__uint_as_float(atomicOr(&st->max_bits[0], 0u));
-        double maxy = (double)__uint_as_float(atomicOr(&st->max_bits[1], 0u));
-        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
-        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
-        double dt = cx < cy ? cx : cy;
-        if (st->t == 0.0) dt = (double)0.000001f;
-        st->dt_old = st->dt;
-        st->dt = dt;
-        st->t = st->t + dt;
-    }
-    // re-sync U* with U^n on tiles that went inactive
-    const int nDe = st->nDeact;
-    for (int k = blockIdx.x; k < nDe; k += gridDim.x) {
-        const int tile = P.deact[k];
-        const int bX = tile % P.nBX, bY = tile / P.nBX;
-        if (tid < TW * TH) {
-            const int i = bX * TW + tid % TW + 2, j = bY * TH + tid / TW + 2;
-            auto cp = [&](int jj, int ii) {
-                for (int f = 0; f < 3; f++) P.B[cidx(P, f, jj, ii)] = P.A[cidx(P, f, jj, ii)];
-            };
-            if (i < P.nx && j < P.ny) cp(j, i);
-            if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
-                if (i == 2) {
-                    cp(j, 0);
-                    cp(j, 1);
-                }
-                if (i == P.nx - 3) {
-                    cp(j, P.nx - 2);
-                    cp(j, P.nx - 1);
-                }
-                if (j == 2) {
-                    cp(0, i);
-                    cp(1, i);
-                }
-                if (j == P.ny - 3) {
-                    cp(P.ny - 2, i);
-                    cp(P.ny - 1, i);
-                }
-            }
-        }
-    }
+    finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
+    resyncDeactivated(P);
 }
 
 // ---------------------------------------------------------------- k_stage
 // Ghost cells owned by interior cell (j, i): critical-depth outflow
-// (ApplyBoundariesX_k: clamped at epsilon; ApplyBoundariesY_k: not, A4).
+// (ApplyBoundariesX_k: clamped at epsilon; ApplyBoundariesY_k: not).
 // The ghost's reference elevation is that of the interior cell it copies,
 // so its depth is the critical depth itself.
 __device__ __forceinline__ void writeGhosts(const Params& P, float* U, int j, int i, float h,
@@ -629,7 +698,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
                                               const __grid_constant__ CUtensorMap tmE, Params P) {
     __shared__ StageSmem S;
     const DevState* st = P.st;
-    if (st->stop) return;
+    if (st->stop || useMarch(P)) return;
     const int tid = threadIdx.x;
     const int nAct = st->nActive;
     tilePrologue(S, &tmIn, &tmE, P, nAct);

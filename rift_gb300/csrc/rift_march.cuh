@@ -1,0 +1,476 @@
+// rift_march.cuh -- the two fused RK stages as a column march over strips.
+//
+// Work item: a strip of 7 x 2 reference tiles (112 x 28 cells).  A CTA of
+// four warps walks the strip row by row.  Lane l of warp w holds column
+// 28w + l - 2 of the strip; lanes 2..29 own their column, lanes 0, 1, 30, 31
+// supply the x halo (the warps overlap by four columns).  Per output row:
+//   - the y reconstruction of the row above and the flux through the row's
+//     north face come from registers rolled down the column (no recompute,
+//     no shared memory);
+//   - the x reconstruction takes its neighbours by warp shuffle, the flux
+//     through the east face takes the east neighbour's west-face values by
+//     shuffle, and the west-face flux is the west neighbour's east-face flux;
+//   - the cell update (sources, friction, RK stage, outputs, ghost cells) is
+//     the same arithmetic as grid.cu's Integrate kernels.
+// Rows arrive in shared memory through TMA: 4-row chunks of the 120-column
+// block of (h, hu, hv) and of the four face-elevation offsets, a 3-slot ring
+// refilled as the march moves up (one barrier per chunk).
+// A cell is updated only when its reference tile is active, so results and
+// tile flags are those of the per-tile schedule of the reference.
+#pragma once
+#include "rift_kernels.cuh"
+
+namespace rift {
+
+constexpr int MW = 4;                              // warps per CTA
+constexpr int MT = MW * 32;                        // threads per CTA
+constexpr int MOWN = 28;                           // owned columns per warp
+constexpr int MCOLS = STRIP_TX * TW;               // 112 columns per strip
+constexpr int MBOXW = 120;                         // staged columns [112 sx - 4, 112 sx + 116)
+constexpr int MRC = 4;                             // rows per staged chunk
+constexpr int MNSLOT = 3;                          // chunk ring depth
+constexpr int MHR = STRIP_TY * TH;                 // 28 output rows per strip
+constexpr int MNROWS = MHR + 4;                    // 32 staged rows (2-row halo each side)
+constexpr int MNCHUNK = (MNROWS + MRC - 1) / MRC;  // 8 chunks
+static_assert(MW * MOWN == MCOLS, "strip width");
+static_assert(MNROWS % MRC == 0, "whole chunks");
+constexpr unsigned FULL = 0xffffffffu;
+
+struct __align__(128) MarchSlot {
+    float s[3][MRC][MBOXW];  // h, hu, hv     (5760 B)
+    float e[4][MRC][MBOXW];  // eW, eE, eS, eN (7680 B)
+};
+static_assert(sizeof(MarchSlot) % 128 == 0, "TMA destination alignment");
+static_assert(offsetof(MarchSlot, e) % 128 == 0, "TMA destination alignment");
+constexpr uint32_t MBYTES_S = 3 * MRC * MBOXW * 4;
+constexpr uint32_t MBYTES_E = 4 * MRC * MBOXW * 4;
+
+struct __align__(128) MarchSmem {
+    MarchSlot slot[MNSLOT];
+    uint64_t bar[MNSLOT];
+    unsigned tmx[STRIP_TX * STRIP_TY];
+    unsigned tmy[STRIP_TX * STRIP_TY];
+    int twet[STRIP_TX * STRIP_TY];
+    int tact[STRIP_TX * STRIP_TY];
+};
+
+struct Row {  // one staged row at this lane's column
+    float h, u, v, eW, eE, eS, eN;
+};
+
+__device__ __forceinline__ Row loadRow(const MarchSlot& S, int r, int col) {
+    Row x;
+    x.h = S.s[0][r][col];
+    x.u = S.s[1][r][col];
+    x.v = S.s[2][r][col];
+    x.eW = S.e[0][r][col];
+    x.eE = S.e[1][r][col];
+    x.eS = S.e[2][r][col];
+    x.eN = S.e[3][r][col];
+    return x;
+}
+
+// y reconstruction of row c between rows m (below) and p (above)
+__device__ __forceinline__ Rec constructY(const Row& m, const Row& c, const Row& p) {
+    return construct(c.h, c.u, c.v, p.h, p.u, p.v, m.h, m.u, m.v, c.eS, c.eN, c.eN - p.eS,
+                     m.eN - c.eS);
+}
+
+__device__ __forceinline__ void issueChunk(MarchSmem& S, int slot, const CUtensorMap* tmIn,
+                                           const CUtensorMap* tmE, int xs, int ys) {
+    fence_proxy_async();
+    mbar_expect_tx(&S.bar[slot], MBYTES_S + MBYTES_E);
+    tma_load_3d(&S.slot[slot].s[0][0][0], tmIn, &S.bar[slot], xs, ys, 0);
+    tma_load_3d(&S.slot[slot].e[0][0][0], tmE, &S.bar[slot], xs, ys, 0);
+}
+
+// Error path of a timed-out ring wait on chunk c: wait, bounded, for the
+// chunks still in flight (c .. c+MNSLOT-1), so that no TMA write lands after
+// the CTA has left.  `par` holds the slots' parities before chunk c's wait.
+__device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
+    for (int k = c; k < c + MNSLOT && k < MNCHUNK; k++)
+        mbar_wait_bounded(&S.bar[k % MNSLOT], (par >> (k % MNSLOT)) & 1u);
+}
+
+// Step-wide constants of a stage kernel.
+struct StageConsts {
+    float kappa, dtNew, dtSrc, invDtSrc, rainU, drainU, fac0, fac1, fac2;
+    double tNew;
+    uint32_t fl;
+    bool euler;
+    float* Uout;
+    const float* Fin;
+    float* Fout;
+};
+
+template <int STAGE>
+__device__ __forceinline__ StageConsts stageConsts(const Params& P) {
+    const DevState* st = P.st;
+    StageConsts C;
+    C.kappa = P.kappa;
+    C.fl = P.flags;
+    C.euler = (P.flags & F_EULER) != 0;
+    C.dtNew = (float)st->dt;
+    // source clamps use the dt passed to ComputeFluxes: the previous dt in
+    // stage 1 (simulator.cu:786-792), the new one in stage 2
+    C.dtSrc = (STAGE == 1) ? (float)st->dt_old : C.dtNew;
+    C.invDtSrc = 1.f / C.dtSrc;
+    C.tNew = st->t;
+    C.rainU = st->rain_rate;
+    C.drainU = st->drain_rate;
+    C.fac0 = st->factor[0];
+    C.fac1 = st->factor[1];
+    C.fac2 = st->factor[2];
+    C.Uout = (STAGE == 1) ? P.B : P.A;
+    C.Fin = (STAGE == 1) ? P.FA : P.FB;
+    C.Fout = (STAGE == 1) ? P.FB : P.FA;
+    return C;
+}
+
+// Sources, friction, the RK stage, outputs and ghost cells of interior cell
+// (j, i) of `tile`, given its flux divergence (dh, dhu, dhv) and its staged
+// state and face offsets.  Returns the cell's vote for the tile wet flag.
+// pre: centre values loaded one row ahead -- stage 1: Manning n; stage 2:
+// U^n (h, hu, hv) of the cell.
+template <int STAGE>
+__device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
+                                           int i, float dh, float dhu, float dhv, float hC,
+                                           float hu0, float hv0, float eW, float eE, float eS,
+                                           float eN, const float* pre) {
+    const uint32_t fl = C.fl;
+    const size_t c = cidx(P, 0, j, i);
+    // bed-slope source, grid.cu:701,751-752
+    const float S1 = -kG * hC * ((eE - eW) * P.inv_dx);
+    const float S2 = -kG * hC * ((eN - eS) * P.inv_dy);
+    // mass sources, grid.cu:763-807
+    float S0 = 0.f;
+    if (fl & F_RAIN_U) S0 += C.rainU;
+    float rainG = 0.f;
+    if (fl & F_RAIN_G) {
+        rainG = mapValue(P, 0, c, C.fac0);
+        S0 += rainG;
+    }
+    const float cap = hC * C.invDtSrc;
+    if (fl & F_DRAIN_U) S0 -= (C.drainU > cap) ? cap : C.drainU;
+    if (fl & F_DRAIN_G) {
+        float d = mapValue(P, 1, c, C.fac1);
+        S0 -= (d > cap) ? cap : d;
+    }
+    bool srcCell = false;
+    if (P.nsrc > 0) {
+        const int flat = j * P.nx + i;
+        for (int q = P.srcTileStart[tile]; q < P.srcTileStart[tile + 1]; q++) {
+            int sidx = P.srcTileList[q];
+            if (P.srcIdx[sidx] == flat) {
+                S0 += P.srcRate[sidx];
+                srcCell = true;
+            }
+        }
+    }
+    float dF = 0.f, Fc = 0.f;
+    if (fl & F_INFIL) {
+        Fc = C.Fin[c];
+        dF = greenAmpt(P.K[c], Fc, P.psiDtheta, C.dtSrc, hC);
+        S0 -= dF;
+    }
+    dh += S0;
+    dhu += S1;
+    dhv += S2;
+    const float hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
+    const float dtNew = C.dtNew;
+    float hN, huN, hvN;
+    bool wetCell = false;
+    if (STAGE == 1) {
+        // Integrate_1_k (grid.cu:856-922)
+        const float G = manningG(pre[0], hu0, hv0, hC, C.kappa);
+        if (fl & F_SURGE) {
+            float sg = mapValue(P, 2, c, C.fac2);
+            if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
+        }
+        hN = hc + dh * dtNew;
+        const float den = 1.f / (1.f - dtNew * G);
+        huN = (hu0 + dhu * dtNew) * den;
+        hvN = (hv0 + dhv * dtNew) * den;
+        hN = (hN > kEps) ? hN : 0.f;
+        if (fl & F_INFIL) C.Fout[c] = Fc + dF * dtNew;
+        if (C.euler) {
+            // Euler-mode outputs and wet flags (grid.cu:926-1023)
+            const float uC = huN * velFactor(hN, C.kappa), vC = hvN * velFactor(hN, C.kappa);
+            if (fl & F_SAVE_MAX) {
+                float hm = P.hmax[c];
+                if (hN > hm) P.tpeak[c] = (float)C.tNew;
+                if (hN > 0.0762f) P.tdry[c] = (float)C.tNew;
+                P.hmax[c] = fmaxf(hm, hN);
+                P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
+            }
+            if (fl & F_SAVE_ARR) {
+                if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)C.tNew;
+            }
+            wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
+                      ((fl & F_RAIN_G) && rainG > 0.f);
+            if (fl & F_SURGE) {
+                float sg = mapValue(P, 2, c, C.fac2);
+                if (sg != P.nodata && sg > 0.f) wetCell = true;
+            }
+        }
+    } else {
+        // Integrate_2_k (grid.cu:1043-1171)
+        const float hOld = pre[0];
+        const float hOc = (hOld > kEps) ? hOld : 0.f;
+        hN = 0.5f * (hOc + hc + dh * dtNew);
+        huN = 0.5f * (pre[1] + hu0 + dhu * dtNew);
+        hvN = 0.5f * (pre[2] + hv0 + dhv * dtNew);
+        hN = (hN > kEps) ? hN : 0.f;
+        if (fl & F_INFIL) C.Fout[c] = 0.5f * (P.FA[c] + Fc + dF * dtNew);
+        if (fl & F_SAVE_MAX) {
+            const float uC = huN * velFactor(hN, C.kappa);
+            const float vC = hvN * velFactor(hN, C.kappa);
+            P.hmax[c] = fmaxf(P.hmax[c], hN);
+            P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
+        }
+        if (fl & F_SAVE_ARR) {
+            if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)C.tNew;
+        }
+        wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
+                  ((fl & F_RAIN_G) && rainG > 0.f);
+    }
+    C.Uout[cidx(P, 0, j, i)] = hN;
+    C.Uout[cidx(P, 1, j, i)] = huN;
+    C.Uout[cidx(P, 2, j, i)] = hvN;
+    writeGhosts(P, C.Uout, j, i, hN, huN, hvN);
+    return wetCell;
+}
+
+// STAGE 0: reads U^n (A) -> tile speed maxima, dt and t (the speed output of
+//          the first ComputeFluxes and ComputeTimestep), re-sync of U* on
+//          tiles that went inactive.
+// STAGE 1: reads U^n (A) -> writes U* (B), F* (FB).
+// STAGE 2: reads U* (B) and U^n (A) at the cell -> writes U^{n+1} (A),
+//          F^{n+1} (FA), outputs, tile wet flags and tile speeds.
+template <int STAGE>
+__global__ void __launch_bounds__(MT) k_march(const __grid_constant__ CUtensorMap tmIn,
+                                              const __grid_constant__ CUtensorMap tmE, Params P) {
+    __shared__ MarchSmem S;
+    __shared__ bool last;
+    if (P.st->stop || !useMarch(P)) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nItems = P.st->nStrips;
+    const StageConsts C = stageConsts<STAGE == 0 ? 1 : STAGE>(P);
+    float amx = 0.f, amy = 0.f, tmxAll = 0.f, tmyAll = 0.f;
+    if (STAGE == 0) staleMax(P, amx, amy);
+    if (tid == 0) {
+        prefetch_tmap(&tmIn);
+        prefetch_tmap(&tmE);
+        for (int k = 0; k < MNSLOT; k++) mbar_init(&S.bar[k], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t par = 0u;                          // wait parity, one bit per ring slot
+    const int lc = MOWN * warp + lane - 2;      // column relative to the strip's first interior column
+    const int col = lc + 6;                     // staged column
+    const bool owned = lane >= 2 && lane <= 29;
+    const int tcol = owned ? lc / TW : 0;       // tile column inside the strip
+    const float kappa = C.kappa;
+
+    for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
+        const int strip = P.strips[item];
+        const int sx = strip % P.nSX, sy = strip / P.nSX;
+        const int X0 = MCOLS * sx + 2, Y0 = MHR * sy + 2;
+        const int xs = MCOLS * sx - 4, ys = Y0 - 2;
+        const int i = X0 + lc;
+        __syncthreads();  // the previous item no longer reads the ring or the tile tables
+        if (tid < STRIP_TX * STRIP_TY) {
+            const int bx = STRIP_TX * sx + tid % STRIP_TX, by = STRIP_TY * sy + tid / STRIP_TX;
+            int a = 0;
+            if (bx < P.nBX && by < P.nBY)
+                a = P.prevAct[by * P.nBX + bx] && (bx * TW + 2 <= P.nx - 3) &&
+                    (by * TH + 2 <= P.ny - 3);
+            S.tact[tid] = a;
+            S.tmx[tid] = 0u;
+            S.tmy[tid] = 0u;
+            S.twet[tid] = 0;
+        }
+        if (tid == 0)
+            for (int c = 0; c < MNSLOT; c++) issueChunk(S, c, &tmIn, &tmE, xs, ys + c * MRC);
+        bool ok = mbar_wait_bounded(&S.bar[0], par & 1u);
+        if (!__syncthreads_and(ok)) {
+            marchDrain(S, par, 0);
+            if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
+            return;
+        }
+        par ^= 1u;
+        // prologue: staged rows 0..3; y reconstruction of rows 1 and 2 and the
+        // flux through the south face of row 2 (the first output row)
+        const Row r0 = loadRow(S.slot[0], 0, col);
+        const Row r1 = loadRow(S.slot[0], 1, col);
+        Row cur = loadRow(S.slot[0], 2, col);
+        Row nxt = loadRow(S.slot[0], 3, col);
+        float fS0 = 0.f, fS1 = 0.f, fS2 = 0.f, yPh, yPu, yPv;
+        if (STAGE == 0) {
+            const RecN y2 = constructN(cur.h, cur.v, nxt.h, nxt.v, r1.h, r1.v, cur.eS, cur.eN,
+                                       cur.eN - nxt.eS, r1.eN - cur.eS);
+            yPh = y2.hP;
+            yPv = y2.qP;
+            yPu = 0.f;
+        } else {
+            const Rec y1 = constructY(r0, r1, cur);
+            const Rec y2 = constructY(r1, cur, nxt);
+            float f[3];
+            faceFlux<1>(y1.hP, y1.uP, y1.vP, y2.hM, y2.uM, y2.vM, kappa, f);
+            fS0 = f[0];
+            fS1 = f[1];
+            fS2 = f[2];
+            yPh = y2.hP;
+            yPu = y2.uP;
+            yPv = y2.vP;
+        }
+        // centre values of the first output row, loaded ahead of use
+        const bool colIn = owned && i <= P.nx - 3;
+        float pre[3] = {0.f, 0.f, 0.f}, nextPre[3] = {0.f, 0.f, 0.f};
+        if (STAGE != 0 && colIn && Y0 <= P.ny - 3) {
+            if (STAGE == 1) {
+                pre[0] = P.nman[cidx(P, 0, Y0, i)];
+            } else {
+                pre[0] = P.A[cidx(P, 0, Y0, i)];
+                pre[1] = P.A[cidx(P, 1, Y0, i)];
+                pre[2] = P.A[cidx(P, 2, Y0, i)];
+            }
+        }
+        float accMx = 0.f, accMy = 0.f;
+        bool accWet = false;
+#pragma unroll 1
+        for (int R = 2; R <= MHR + 1; R++) {
+            const int lead = R + 2;
+            if (lead % MRC == 0) {  // entering chunk c: refill the slot chunk c-1 used
+                const int c = lead / MRC;
+                __syncthreads();
+                if (tid == 0 && c - 1 + MNSLOT < MNCHUNK)
+                    issueChunk(S, (c - 1) % MNSLOT, &tmIn, &tmE, xs, ys + (c - 1 + MNSLOT) * MRC);
+                const int sl = c % MNSLOT;
+                bool ok2 = mbar_wait_bounded(&S.bar[sl], (par >> sl) & 1u);
+                if (!__syncthreads_and(ok2)) {
+                    marchDrain(S, par, c);
+                    if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
+                    return;
+                }
+                par ^= (1u << sl);
+            }
+            const Row ld = loadRow(S.slot[(lead / MRC) % MNSLOT], lead % MRC, col);
+            const int j = Y0 + R - 2;
+            // centre values of the next output row, in flight during this one
+            if (STAGE != 0 && colIn && j + 1 <= P.ny - 3) {
+                if (STAGE == 1) {
+                    nextPre[0] = P.nman[cidx(P, 0, j + 1, i)];
+                } else {
+                    nextPre[0] = P.A[cidx(P, 0, j + 1, i)];
+                    nextPre[1] = P.A[cidx(P, 1, j + 1, i)];
+                    nextPre[2] = P.A[cidx(P, 2, j + 1, i)];
+                }
+            }
+            const int tslot = ((R - 2) / TH) * STRIP_TX + tcol;
+            const bool cellOn = colIn && S.tact[tslot] && j <= P.ny - 3;
+            float spx, spy;
+            if (STAGE == 0) {
+                // speeds only: depth + normal momentum reconstructions
+                const RecN yn = constructN(nxt.h, nxt.v, ld.h, ld.v, cur.h, cur.v, nxt.eS, nxt.eN,
+                                           nxt.eN - ld.eS, cur.eN - nxt.eS);
+                spy = faceSpeed(yPh, yPv, yn.hM, yn.qM, kappa);
+                const float hm = __shfl_up_sync(FULL, cur.h, 1), hp = __shfl_down_sync(FULL, cur.h, 1);
+                const float um = __shfl_up_sync(FULL, cur.u, 1), up = __shfl_down_sync(FULL, cur.u, 1);
+                const float eEm = __shfl_up_sync(FULL, cur.eE, 1);
+                const float eWp = __shfl_down_sync(FULL, cur.eW, 1);
+                const RecN xr = constructN(cur.h, cur.u, hp, up, hm, um, cur.eW, cur.eE,
+                                           cur.eE - eWp, eEm - cur.eW);
+                const float rh = __shfl_down_sync(FULL, xr.hM, 1);
+                const float rq = __shfl_down_sync(FULL, xr.qM, 1);
+                spx = faceSpeed(xr.hP, xr.qP, rh, rq, kappa);
+                yPh = yn.hP;
+                yPv = yn.qP;
+            } else {
+                // y: reconstruction of row R+1, flux through the north face of row R
+                const Rec yn = constructY(cur, nxt, ld);
+                float fN[3];
+                spy = faceFlux<1>(yPh, yPu, yPv, yn.hM, yn.uM, yn.vM, kappa, fN);
+                // x: reconstruction of row R, neighbours by shuffle
+                const float hm = __shfl_up_sync(FULL, cur.h, 1), hp = __shfl_down_sync(FULL, cur.h, 1);
+                const float um = __shfl_up_sync(FULL, cur.u, 1), up = __shfl_down_sync(FULL, cur.u, 1);
+                const float vm = __shfl_up_sync(FULL, cur.v, 1), vp = __shfl_down_sync(FULL, cur.v, 1);
+                const float eEm = __shfl_up_sync(FULL, cur.eE, 1);
+                const float eWp = __shfl_down_sync(FULL, cur.eW, 1);
+                const Rec xr = construct(cur.h, cur.u, cur.v, hp, up, vp, hm, um, vm, cur.eW,
+                                         cur.eE, cur.eE - eWp, eEm - cur.eW);
+                const float rh = __shfl_down_sync(FULL, xr.hM, 1);
+                const float ru = __shfl_down_sync(FULL, xr.uM, 1);
+                const float rv = __shfl_down_sync(FULL, xr.vM, 1);
+                float fE[3];
+                spx = faceFlux<0>(xr.hP, xr.uP, xr.vP, rh, ru, rv, kappa, fE);
+                const float fW0 = __shfl_up_sync(FULL, fE[0], 1);
+                const float fW1 = __shfl_up_sync(FULL, fE[1], 1);
+                const float fW2 = __shfl_up_sync(FULL, fE[2], 1);
+                if (cellOn) {
+                    const float dh = -(fE[0] - fW0) * P.inv_dx - (fN[0] - fS0) * P.inv_dy;
+                    const float dhu = -(fE[1] - fW1) * P.inv_dx - (fN[1] - fS1) * P.inv_dy;
+                    const float dhv = -(fE[2] - fW2) * P.inv_dx - (fN[2] - fS2) * P.inv_dy;
+                    const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
+                    accWet |= cellUpdate<STAGE>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
+                                                cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre);
+                }
+                fS0 = fN[0];
+                fS1 = fN[1];
+                fS2 = fN[2];
+                yPh = yn.hP;
+                yPu = yn.uP;
+                yPv = yn.vP;
+            }
+            if (cellOn) {
+                accMx = fmaxf(accMx, spx);
+                accMy = fmaxf(accMy, spy);
+            }
+            if ((R - 2) % TH == TH - 1) {  // last row of a tile row: fold into the tile
+                if (owned) {
+                    if (STAGE != 1) {
+                        atomicMax(&S.tmx[tslot], __float_as_uint(accMx));
+                        atomicMax(&S.tmy[tslot], __float_as_uint(accMy));
+                    }
+                    if ((STAGE == 2 || C.euler) && accWet) atomicOr(&S.twet[tslot], 1);
+                }
+                accMx = 0.f;
+                accMy = 0.f;
+                accWet = false;
+            }
+            pre[0] = nextPre[0];
+            pre[1] = nextPre[1];
+            pre[2] = nextPre[2];
+            cur = nxt;
+            nxt = ld;
+        }
+        __syncthreads();
+        if (tid < STRIP_TX * STRIP_TY && S.tact[tid]) {
+            const int bx = STRIP_TX * sx + tid % STRIP_TX, by = STRIP_TY * sy + tid / STRIP_TX;
+            const int b = by * P.nBX + bx;
+            if (STAGE != 0 && (STAGE == 2 || C.euler))
+                P.wet[b] = (uint8_t)((!(C.fl & F_TILE_ACC)) || S.twet[tid]);
+            if (STAGE != 1) {
+                P.mx[b] = __uint_as_float(S.tmx[tid]);
+                P.my[b] = __uint_as_float(S.tmy[tid]);
+            }
+        }
+        if (STAGE == 0) {  // thread 0 keeps this CTA's maximum of new tile speeds
+            __syncthreads();
+            if (tid == 0)
+                for (int k = 0; k < STRIP_TX * STRIP_TY; k++)
+                    if (S.tact[k]) {
+                        tmxAll = fmaxf(tmxAll, __uint_as_float(S.tmx[k]));
+                        tmyAll = fmaxf(tmyAll, __uint_as_float(S.tmy[k]));
+                    }
+        }
+    }
+    if (STAGE == 0) {
+        __syncthreads();
+        __shared__ float red[2][MT / 32];
+        finishDt(P, amx, amy, tmxAll, tmyAll, red[0], red[1], &last);
+        resyncDeactivated(P);
+    }
+}
+
+}  // namespace rift

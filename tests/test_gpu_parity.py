@@ -26,9 +26,13 @@ def _close(a, b, what):
     assert d.max() <= MAX_TOL, f"{what}: max {d.max()}"
 
 
-def _run_against_golden(engine_api, name):
+SCHEDULES = {"auto": -1, "march": 0, "tiles": 1 << 30}
+
+
+def _run_against_golden(engine_api, name, schedule="auto"):
     fx, case = FX.load(name)
-    eng = FX.start(capi.Sim(case, api=engine_api), fx)
+    eng = capi.Sim(case, api=engine_api).set_schedule(SCHEDULES[schedule])
+    eng = FX.start(eng, fx)
     step = 0
     log = fx["steps_log"]
     for s in FX.dumps(fx):
@@ -52,9 +56,12 @@ def _run_against_golden(engine_api, name):
             assert np.array_equal(FX.interior(tw) < 0, FX.interior(ref["twet"]) < 0), name
 
 
+@pytest.mark.parametrize("schedule", ["tiles", "march"])
 @pytest.mark.parametrize("name", FX.CASES)
-def test_engine_matches_reference_kernels(engine_api, name):
-    _run_against_golden(engine_api, name)
+def test_engine_matches_reference_kernels(engine_api, name, schedule):
+    """Both kernel schedules (per-tile and column march) against the
+    reference kernels."""
+    _run_against_golden(engine_api, name, schedule)
 
 
 @pytest.mark.parametrize("name", ["rain", "front", "gridrain_surge", "h0_infil_src", "euler"])
@@ -66,7 +73,10 @@ def test_one_step_from_identical_snapshot(engine_api, oracle_api, name):
     ref = FX.ref_state(fx, s)
     runs = []
     for api, mode in ((engine_api, None), (oracle_api, 0)):
-        sim = FX.start(capi.Sim(case, api=api, create_mode=mode), fx)
+        sim = capi.Sim(case, api=api, create_mode=mode)
+        if mode is None:
+            sim.set_schedule(0)  # the march kernels (the tiles run in the golden test)
+        sim = FX.start(sim, fx)
         sim.set_state(ref["t"], ref["dt"], ref["w"], ref["hu"], ref["hv"], ref.get("F"),
                       ref["wet"], ref["active"], ref["mx"], ref["my"])
         sim.step()

@@ -27,7 +27,7 @@ def test_limiter_probe_bit_exact(oracle_api):
     li = np.array([lib.rift_oracle_limiter(*v) for v in zip(d["a"], d["b"], d["c"])])
     assert np.array_equal(mm.view(np.uint64), d["minmod"].view(np.uint64))
     assert np.array_equal(li.view(np.uint64), d["limiter"].view(np.uint64))
-    # A1: the reference limiter never returns a negative slope
+    # the reference limiter never returns a negative slope (low-word signf)
     assert (d["minmod"] >= 0).all()
     assert set(np.unique(d["signf"])) <= {0.0, 1.0, 1.0 + 2.0 ** -21}
 
