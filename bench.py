@@ -146,7 +146,7 @@ def run_ours(args, device=0, sync=None):
 
     # ---- e2e through the C ABI with host buffers ----------------------------
     t0 = time.perf_counter()
-    sim = capi.Sim(case, device=device).set_schedule(args.schedule)
+    sim = capi.Sim(case, device=device).set_schedule(args.schedule).set_persistent(args.persistent)
     sim.setup()
     t_setup = time.perf_counter() - t0
     spin_up(sim, spin)
@@ -174,16 +174,29 @@ def run_ours(args, device=0, sync=None):
     clocks = ClockSampler().start()
     if sync:
         sync()
+    p0, g0 = sim.path_stats()
     ms, active_cells, done, stage_ms, stage_cells = device_timed_run(sim, args.steps)
+    p1, g1 = sim.path_stats()
     if sync:
         sync()
     clk = clocks.stop()
+    persist_steps, graph_steps = p1 - p0, g1 - g0
     steps = int(done)
     value = interior * steps / (ms * 1e-3)
     active_rate = active_cells / (ms * 1e-3)
     peak, peak_kind = peaks()
     bytes_per = 4 * WORDS[cfg]
-    achieved = stage_cells * bytes_per / (stage_ms * 1e-3) / 1e9 if stage_ms > 0 else None
+    if persist_steps > 0 and graph_steps == 0:
+        # one cooperative launch ran every timed step: the kernel is the step
+        kernel = ("k_persist (whole step in one cooperative launch: grow, speeds + dt, "
+                  "RK stages 1+2)")
+        achieved = active_cells * bytes_per / (ms * 1e-3) / 1e9
+        launches = 1
+    else:
+        kernel = ("RK stages 1+2 (k_march<1>, k_march<2> or k_stage<1>, k_stage<2>; one "
+                  "schedule runs, the other exits at entry)")
+        achieved = stage_cells * bytes_per / (stage_ms * 1e-3) / 1e9 if stage_ms > 0 else None
+        launches = graph_steps * launches_per_step(case.flags) + (1 if persist_steps else 0)
     traffic = None
     prof = os.path.join(ROOT, "profiles", f"traffic_config{cfg}.json")
     if os.path.exists(prof):
@@ -215,10 +228,10 @@ def run_ours(args, device=0, sync=None):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_kind": peak_kind, "bytes_per_active_cell_update": bytes_per,
-                     "kernel": "RK stages 1+2 (k_march<1>, k_march<2> or k_stage<1>, "
-                               "k_stage<2>; one schedule runs, the other exits at entry)"},
+                     "kernel": kernel},
         "clocks": clk,
-        "gpu_launches": steps * launches_per_step(case.flags),
+        "gpu_launches": launches,
+        "path": {"persistent_steps": persist_steps, "graph_steps": graph_steps},
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, snap, args)
@@ -228,9 +241,10 @@ def run_ours(args, device=0, sync=None):
 
 def launches_per_step(flags):
     """Kernels one step's graph launches: k_track (gridded rain or surge),
-    k_grow, the speed/dt kernel and the stage kernels of both schedules (the
-    schedule not chosen for the step exits at entry), k_commit in Euler mode."""
-    n = 1 + 2 + 2 + (1 if flags & synth.EULER else 2)
+    the two grow passes, the speed/dt kernel and the stage kernels of both
+    schedules (the schedule not chosen for the step exits at entry), k_commit
+    in Euler mode."""
+    n = 2 + 2 + 2 + (1 if flags & synth.EULER else 2)
     if flags & (synth.RAIN_GRID | synth.SURGE_GRID):
         n += 1
     return n
@@ -330,6 +344,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--schedule", type=int, default=-1,
                     help="march kernels from this many active strips up (-1: engine default)")
+    ap.add_argument("--persistent", type=int, default=-1,
+                    help="persistent step loop while at most this many tiles are active "
+                         "(-1: engine default, 0: off)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -166,6 +166,18 @@ int rift_get_time(rift_handle* h, double* t, double* dt);
  * volume check in simulator.cu:609-637. */
 int rift_volume(rift_handle* h, double* volume);
 
+/* Volume ledger (replaces the check_volume accounting of
+ * Simulator::UpdateSource / setSourceValue / RunSimulation,
+ * simulator.cu:524-530, 819-820, 892-897): `volume` as rift_volume, `added`
+ * the FP64 sum since rift_init of the volume (depth x cells) the sources
+ * applied -- per step, dt x (uniform rain rate x interior cells + point
+ * source rates + interior sum of the gridded rain map at the step's
+ * factor).  The reference adds uniform rain with the previous step's dt;
+ * this ledger uses the dt the step applied, so that with no outflow,
+ * drain, infiltration or clamping, volume - volume(init) = added up to the
+ * FP32 rounding of the state. */
+int rift_mass_ledger(rift_handle* h, double* volume, double* added);
+
 /* Measurement entry point (no reference counterpart; the reference only
  * prints a wall-clock Mcells/s line, simulator.cu:836-841): nsteps step-graph
  * replays timed with CUDA events on the handle's stream (ms_total; summed
@@ -183,6 +195,17 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total,
  * kernels.  Both give the same results.  -1 restores the default (one strip
  * per resident march CTA); 0 forces the march, a huge value the tiles. */
 int rift_set_schedule(rift_handle* h, int32_t march_min_strips);
+
+/* Persistent step loop (no reference counterpart): while at most
+ * max_active_tiles tiles are active, rift_run / rift_step run their steps
+ * in one cooperative launch whose phases are separated by grid barriers,
+ * with the per-tile arithmetic of the per-step kernels.  -1 restores the
+ * default (the march threshold in tiles), 0 turns it off.
+ * RIFT_ERR_UNSUPPORTED when the device has no cooperative launch. */
+int rift_set_persistent(rift_handle* h, int32_t max_active_tiles);
+
+/* Steps run so far by the persistent launch and by the per-step graph. */
+int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_steps);
 
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);

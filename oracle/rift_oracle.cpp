@@ -209,6 +209,7 @@ struct rift_oracle {
     bool first_grow = true;
     double t = 0.0, dt = 0.0;
     double rain_rate = 0.0, drain_rate = 0.0;
+    double v_added = 0.0;  // volume ledger, see rift_oracle_mass_ledger
     std::vector<int32_t> src_idx;
     std::vector<double> src_rate;
     Map maps[3];
@@ -660,6 +661,14 @@ void oneStep(rift_oracle* o) {
     grow(o);
     computeFluxes(o, o->dt);
     computeTimestep(o);
+    // volume the sources add over this step (each rate applies for dt)
+    double add = 0.0;
+    if (o->has(RIFT_F_RAIN_UNIFORM)) add += o->rain_rate * (double)(o->nx - 4) * (o->ny - 4);
+    for (double r : o->src_rate) add += r;
+    if (o->has(RIFT_F_RAIN_GRID) && o->maps[RIFT_MAP_RAIN].set)
+        for (int j = 2; j < o->ny - 2; j++)
+            for (int i = 2; i < o->nx - 2; i++) add += o->cur_map[RIFT_MAP_RAIN][o->c(j, i)];
+    o->v_added += add * o->dt;
     integrate1(o);
     applyBoundaries(o);
     if (!o->has(RIFT_F_EULER)) {
@@ -737,6 +746,7 @@ int rift_oracle_upload_static(rift_oracle* o, const double* BX, const double* BY
 int rift_oracle_init(rift_oracle* o, double t0) {
     if (!o || !o->have_static) return RIFT_ERR_STATE;
     const int nx = o->nx, ny = o->ny;
+    o->v_added = 0.0;
     for (int j = 2; j < ny; j++)
         for (int i = 2; i < nx; i++) {
             size_t id = o->c(j, i);
@@ -936,6 +946,13 @@ int rift_oracle_volume(rift_oracle* o, double* volume) {
         }
     *volume = s;
     return RIFT_OK;
+}
+
+int rift_oracle_mass_ledger(rift_oracle* o, double* volume, double* added) {
+    if (!o || !volume || !added) return RIFT_ERR_ARG;
+    int rc = rift_oracle_volume(o, volume);
+    *added = o->v_added;
+    return rc;
 }
 
 int rift_oracle_get_tile_grid(rift_oracle* o, int32_t* nBX, int32_t* nBY) {

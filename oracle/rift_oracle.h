@@ -61,6 +61,7 @@ int rift_oracle_set_state(rift_oracle* o, double t, double dt_prev, const double
                           const double* mx, const double* my);
 int rift_oracle_get_time(rift_oracle* o, double* t, double* dt);
 int rift_oracle_volume(rift_oracle* o, double* volume);
+int rift_oracle_mass_ledger(rift_oracle* o, double* volume, double* added);
 int rift_oracle_get_tile_grid(rift_oracle* o, int32_t* nBX, int32_t* nBY);
 int rift_oracle_set_threads(int32_t n);
 const char* rift_oracle_last_error(rift_oracle* o);

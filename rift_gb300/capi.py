@@ -51,8 +51,8 @@ def exported_symbols():
     """Entry points of include/rift_gb300.h (without the prefix)."""
     return ["create", "upload_static", "init", "set_uniform_rates", "set_point_sources",
             "set_map", "set_map_factor", "set_map_times", "step", "run", "set_series", "get_field", "get_tiles",
-            "get_tile_speeds", "set_state", "get_time", "volume", "get_tile_grid", "last_error",
-            "destroy"]
+            "get_tile_speeds", "set_state", "get_time", "volume", "mass_ledger", "get_tile_grid",
+            "last_error", "destroy"]
 
 
 def bind(lib, prefix: str, create_has_mode: bool = False):
@@ -73,6 +73,10 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                [_P, C.c_int32, C.c_double, C.c_double])
     if hasattr(lib, p + "set_schedule"):
         ns["set_schedule"] = _sig(lib, p + "set_schedule", C.c_int, [_P, C.c_int32])
+    if hasattr(lib, p + "set_persistent"):
+        ns["set_persistent"] = _sig(lib, p + "set_persistent", C.c_int, [_P, C.c_int32])
+        ns["get_path_stats"] = _sig(lib, p + "get_path_stats", C.c_int,
+                                    [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)])
     ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
     ns["step"] = _sig(lib, p + "step", C.c_int, [_P, _D, _D])
     ns["run"] = _sig(lib, p + "run", C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _I])
@@ -83,6 +87,7 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                            [_P, C.c_double, C.c_double, _D, _D, _D, _D, _U8, _I, C.c_int32, _D, _D])
     ns["get_time"] = _sig(lib, p + "get_time", C.c_int, [_P, _D, _D])
     ns["volume"] = _sig(lib, p + "volume", C.c_int, [_P, _D])
+    ns["mass_ledger"] = _sig(lib, p + "mass_ledger", C.c_int, [_P, _D, _D])
     ns["get_tile_grid"] = _sig(lib, p + "get_tile_grid", C.c_int, [_P, _I, _I])
     ns["last_error"] = _sig(lib, p + "last_error", C.c_char_p, [_P])
     ns["destroy"] = _sig(lib, p + "destroy", None, [_P])
@@ -219,6 +224,19 @@ class Sim:
             self._check(self.f["set_schedule"](self.h, march_min_strips), "set_schedule")
         return self
 
+    def set_persistent(self, max_active_tiles):
+        """Persistent cooperative step loop while at most this many tiles are
+        active (-1 default, 0 off)."""
+        if "set_persistent" in self.f:
+            self._check(self.f["set_persistent"](self.h, max_active_tiles), "set_persistent")
+        return self
+
+    def path_stats(self):
+        """(steps run by the persistent launch, steps run by the per-step graph)."""
+        a, b = C.c_int64(), C.c_int64()
+        self._check(self.f["get_path_stats"](self.h, C.byref(a), C.byref(b)), "get_path_stats")
+        return a.value, b.value
+
     # -- stepping ---------------------------------------------------------
     def step(self):
         t, dt = C.c_double(), C.c_double()
@@ -259,6 +277,12 @@ class Sim:
         v = C.c_double()
         self._check(self.f["volume"](self.h, C.byref(v)), "volume")
         return v.value
+
+    def mass_ledger(self):
+        """(volume, volume added by the sources since init), FP64."""
+        v, a = C.c_double(), C.c_double()
+        self._check(self.f["mass_ledger"](self.h, C.byref(v), C.byref(a)), "mass_ledger")
+        return v.value, a.value
 
     def set_state(self, t, dt_prev, w, hu, hv, F=None, wet=None, active=None, mx=None, my=None):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None

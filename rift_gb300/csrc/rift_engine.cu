@@ -23,8 +23,10 @@
 #include <vector>
 
 #include "../../include/rift_gb300.h"
+#include "rift_grow.cuh"
 #include "rift_kernels.cuh"
 #include "rift_march.cuh"
+#include "rift_persist.cuh"
 
 using namespace rift;
 
@@ -56,6 +58,13 @@ struct rift_handle {
     int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0, gridMarch = 0;
     int nSX = 0, nSY = 0;
     int marchMin = 0;  // active strips from which the march kernels run
+    int gridGrow = 0;      // CTAs of the two grow passes of the graph path
+    int gridPersist = 0;   // CTAs of the cooperative step kernel (0: unavailable)
+    int persistMax = 0;    // it runs while the active tiles are at most this many
+    GridBar* gbar = nullptr;
+    int* growCnt = nullptr;
+    unsigned long long* growCells = nullptr;
+    long long persistSteps = 0, graphSteps = 0;  // steps run by each path (diagnostics)
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
     CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
@@ -151,6 +160,10 @@ Params makeParams(rift_handle* h) {
     P.nSX = h->nSX;
     P.nSY = h->nSY;
     P.marchMin = h->marchMin;
+    P.persistMax = h->persistMax;
+    P.gbar = h->gbar;
+    P.growCnt = h->growCnt;
+    P.growCells = h->growCells;
     P.mx = h->mx;
     P.my = h->my;
     P.srcIdx = h->srcIdx;
@@ -193,7 +206,8 @@ void enqueueStep(rift_handle* h) {
     cudaStream_t s = h->stream;
     if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
         k_track<<<h->gridTrack, NT, 0, s>>>(P);
-    k_grow<<<1, GROW_T, 0, s>>>(P);
+    k_grow_a<<<h->gridGrow, NT, 0, s>>>(P);
+    k_grow_b<<<h->gridGrow, NT, 0, s>>>(P);
     // per-tile and march variants of each pass; the device keeps one of them
     // (useMarch) and the other returns at once
     k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
@@ -221,13 +235,23 @@ int buildGraph(rift_handle* h) {
 int pullState(rift_handle* h) {
     CUDA_TRY(h, cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    if (h->hst->error) return fail(h, RIFT_ERR_CUDA, "device wait timed out (TMA barrier)");
+    if (h->hst->error)
+        return fail(h, RIFT_ERR_CUDA,
+                    (h->hst->error & ERR_BARRIER_TIMEOUT) ? "device wait timed out (grid barrier)"
+                                                          : "device wait timed out (TMA barrier)");
     return RIFT_OK;
 }
 
 int pushState(rift_handle* h) {
     CUDA_TRY(h, cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
+// Stream-ordered push for the step path: the host leaves the pinned mirror
+// alone until the pull that ends the call, so no wait is needed here.
+int pushStateAsync(rift_handle* h) {
+    CUDA_TRY(h, cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, h->stream));
     return RIFT_OK;
 }
 
@@ -437,6 +461,20 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     h->gridSpeed = std::max(1, std::min(G, h->numSMs * occ));
     h->gridTrack = std::max(1, std::min(G, h->numSMs * 4));
     h->gridDt = std::max(1, std::min((G + 255) / 256, h->numSMs * 2));
+    // the cooperative step kernel: every CTA resident at once
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    occ = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_persist, NT, 0);
+    if (coop && occ > 0) {
+        h->gridPersist = std::min(h->numSMs * occ, PERSIST_MAX_CTAS);
+        CUDA_TRY(h, cudaMalloc(&h->gbar, sizeof(GridBar)));
+    }
+    h->gridGrow = std::max(1, std::min(NS, h->numSMs * 4));
+    const int growCTAs = std::max(h->gridGrow, h->gridPersist);
+    CUDA_TRY(h, cudaMalloc(&h->growCnt, (size_t)growCTAs * GROW_LISTS * sizeof(int)));
+    CUDA_TRY(h, cudaMalloc(&h->growCells, (size_t)growCTAs * sizeof(unsigned long long)));
+    h->persistMax = h->gridPersist > 0 ? h->marchMin * STRIP_TX * STRIP_TY : 0;
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return RIFT_OK;
 }
@@ -514,6 +552,8 @@ int rift_init(rift_handle* h, double t0) {
     }
     h->hst->rain_rate = keepRain;
     h->hst->drain_rate = keepDrain;
+    h->hst->rain_sum[0] = keep.rain_sum[0];
+    h->hst->rain_sum[1] = keep.rain_sum[1];
     int rc = uploadState(h, H, U, V, wet, actf, inact);
     if (rc) return rc;
     const size_t pl = h->plane() * 4;
@@ -612,20 +652,31 @@ int rift_set_map(rift_handle* h, int32_t which, const double* t0map, const doubl
         }
     std::vector<float> tmp(N);
     int rc;
+    // interior sums of the maps as the device holds them (rain volume ledger)
+    auto interiorSum = [&]() {
+        double sum = 0.0;
+        for (int j = 2; j < h->ny - 2; j++)
+            for (int i = 2; i < h->nx - 2; i++) sum += (double)tmp[hidx(h, j, i)];
+        return sum;
+    };
+    double sums[2] = {0.0, 0.0};
     for (size_t c = 0; c < N; c++) tmp[c] = (float)t0map[c];
+    sums[0] = interiorSum();
     if ((rc = upField(h, h->maps[which][0], tmp))) return rc;
     if (t1map) {
         for (size_t c = 0; c < N; c++) tmp[c] = (float)t1map[c];
+        sums[1] = interiorSum();
         if ((rc = upField(h, h->maps[which][1], tmp))) return rc;
     }
     if (h->mapMode[which] != newMode) destroyGraph(h);
     h->mapMode[which] = newMode;
-    if (h->inited) {
-        if ((rc = pullState(h))) return rc;
-        h->hst->factor[which] = (float)factor;
-        return pushState(h);
-    }
+    if (h->inited && (rc = pullState(h))) return rc;
     h->hst->factor[which] = (float)factor;
+    if (which == RIFT_MAP_RAIN) {
+        h->hst->rain_sum[0] = sums[0];
+        h->hst->rain_sum[1] = sums[1];
+    }
+    if (h->inited) return pushState(h);
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return RIFT_OK;
 }
@@ -644,6 +695,18 @@ int rift_set_schedule(rift_handle* h, int32_t march_min_strips) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_march<2>, MT, 0);
     h->marchMin = march_min_strips >= 0 ? march_min_strips : h->numSMs * std::max(occ, 1);
     destroyGraph(h);
+    return RIFT_OK;
+}
+
+int rift_set_persistent(rift_handle* h, int32_t max_active_tiles) {
+    if (!h) return RIFT_ERR_ARG;
+    if (h->gridPersist == 0) {
+        h->persistMax = 0;
+        return max_active_tiles > 0 ? fail(h, RIFT_ERR_UNSUPPORTED, "no cooperative launch")
+                                    : RIFT_OK;
+    }
+    h->persistMax = max_active_tiles >= 0 ? max_active_tiles
+                                          : h->marchMin * STRIP_TX * STRIP_TY;
     return RIFT_OK;
 }
 
@@ -675,19 +738,70 @@ int rift_set_series(rift_handle* h, int32_t which, const float* times, const flo
     return RIFT_OK;
 }
 
+namespace {
+
+// One cooperative launch of the step loop for at most `nsteps` steps.
+int launchPersist(rift_handle* h, int nsteps) {
+    CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream));
+    Params P = makeParams(h);
+    void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
+    CUDA_TRY(h, cudaLaunchCooperativeKernel((const void*)k_persist, dim3(h->gridPersist),
+                                            dim3(NT), args, 0, h->stream));
+    return RIFT_OK;
+}
+
+// Runs up to `nsteps` steps (state pushed, t_stop set; the host mirror of
+// the device state current).  While the active set is small the cooperative
+// step kernel runs the steps in one launch; once the active tiles outnumber
+// persistMax it leaves at a step boundary and the per-step graph (tile or
+// march kernels, chosen on the device) continues, in chunks of
+// kGraphChunk steps after which the host looks at the active count again.
+constexpr int kGraphChunk = 64;
+
+int runSteps(rift_handle* h, int nsteps, bool* mirrorCurrent) {
+    int rc;
+    int left = nsteps;
+    *mirrorCurrent = false;
+    while (left > 0) {
+        if (h->persistMax > 0 && h->hst->nActive <= h->persistMax) {
+            const int before = h->hst->steps_done;
+            if ((rc = launchPersist(h, left)) || (rc = pullState(h))) return rc;
+            *mirrorCurrent = true;
+            const int ran = h->hst->steps_done - before;
+            h->persistSteps += ran;
+            left -= ran;
+            if (!h->hst->persistExit) break;  // all steps done, or t_stop reached
+        }
+        if (left <= 0) break;
+        const int chunk = h->persistMax > 0 ? std::min(left, kGraphChunk) : left;
+        if ((rc = buildGraph(h))) return rc;
+        for (int k = 0; k < chunk; k++) CUDA_TRY(h, cudaGraphLaunch(h->graphExec, h->stream));
+        h->graphSteps += chunk;
+        left -= chunk;
+        *mirrorCurrent = false;
+        if (left > 0) {
+            if ((rc = pullState(h))) return rc;
+            *mirrorCurrent = true;
+            if (h->hst->stop) break;
+        }
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    return RIFT_OK;
+}
+
+}  // namespace
+
 int rift_run(rift_handle* h, int32_t nsteps, double t_stop, double* t, double* dt,
              int32_t* steps_done) {
     if (!h || nsteps < 0) return RIFT_ERR_ARG;
     if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
-    int rc = pullState(h);
-    if (rc) return rc;
+    // every entry point leaves the pinned mirror equal to the device state
     h->hst->t_stop = t_stop;
     h->hst->steps_done = 0;
-    if ((rc = pushState(h))) return rc;
-    if ((rc = buildGraph(h))) return rc;
-    for (int k = 0; k < nsteps; k++) CUDA_TRY(h, cudaGraphLaunch(h->graphExec, h->stream));
-    CUDA_TRY(h, cudaGetLastError());
-    if ((rc = pullState(h))) return rc;
+    int rc;
+    bool current = false;
+    if ((rc = pushStateAsync(h)) || (rc = runSteps(h, nsteps, &current))) return rc;
+    if (!current && (rc = pullState(h))) return rc;
     if (t) *t = h->hst->t;
     if (dt) *dt = h->hst->dt;
     if (steps_done) *steps_done = h->hst->steps_done;
@@ -794,7 +908,7 @@ int rift_get_tiles(rift_handle* h, uint8_t* wet, int32_t* active, int32_t* n_act
     int rc = pullState(h);
     if (rc) return rc;
     std::vector<uint8_t> flags(h->gridSize);
-    // the active set of the last step is prevAct (k_grow keeps it per tile)
+    // the active set of the last step is prevAct (the grow keeps it per tile)
     CUDA_TRY(h, cudaMemcpyAsync(flags.data(), h->prevAct, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
     if (wet) CUDA_TRY(h, cudaMemcpyAsync(wet, h->wet, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -875,6 +989,14 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
     return pushState(h);
 }
 
+int rift_mass_ledger(rift_handle* h, double* volume, double* added) {
+    if (!h || !volume || !added) return RIFT_ERR_ARG;
+    int rc = rift_volume(h, volume);
+    if (rc || (rc = pullState(h))) return rc;
+    *added = h->hst->v_added;
+    return RIFT_OK;
+}
+
 int rift_volume(rift_handle* h, double* volume) {
     if (!h || !volume) return RIFT_ERR_ARG;
     Params P = makeParams(h);
@@ -916,7 +1038,8 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     CUDA_TRY(h, cudaEventCreate(&e1));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     CUDA_TRY(h, cudaEventRecord(e0, h->stream));
-    for (int k = 0; k < nsteps; k++) CUDA_TRY(h, cudaGraphLaunch(h->graphExec, h->stream));
+    bool current = false;
+    if ((rc = runSteps(h, nsteps, &current))) return rc;
     CUDA_TRY(h, cudaEventRecord(e1, h->stream));
     CUDA_TRY(h, cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -935,7 +1058,8 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     for (int k = 0; k < M; k++) {
         if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
             k_track<<<h->gridTrack, NT, 0, s>>>(P);
-        k_grow<<<1, GROW_T, 0, s>>>(P);
+        k_grow_a<<<h->gridGrow, NT, 0, s>>>(P);
+        k_grow_b<<<h->gridGrow, NT, 0, s>>>(P);
         k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
         k_march<0><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
         CUDA_TRY(h, cudaEventRecord(e0, s));
@@ -963,6 +1087,13 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     return RIFT_OK;
 }
 
+int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_steps) {
+    if (!h) return RIFT_ERR_ARG;
+    if (persist_steps) *persist_steps = h->persistSteps;
+    if (graph_steps) *graph_steps = h->graphSteps;
+    return RIFT_OK;
+}
+
 const char* rift_last_error(rift_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
 void rift_destroy(rift_handle* h) {
@@ -975,7 +1106,8 @@ void rift_destroy(rift_handle* h) {
     for (int k = 0; k < 3; k++)
         for (int q = 0; q < 2; q++)
             if (h->maps[k][q]) cudaFree(h->maps[k][q]);
-    for (void* p : {(void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
+    for (void* p : {(void*)h->gbar, (void*)h->growCnt, (void*)h->growCells,
+                    (void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
                     (void*)h->act, (void*)h->deact,
                     (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,
                     (void*)h->srcTileList, (void*)h->st, (void*)h->volPartial})

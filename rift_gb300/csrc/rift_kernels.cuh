@@ -4,11 +4,12 @@
 //   k_track   : re-wet inactive tiles under gridded rain / surge
 //               (TrackRainfall_k / TrackSurge_k, grid.cu:1224-1276); only
 //               when a gridded rain or surge series is on
-//   k_grow    : start of step (stop test, uniform-source interpolation of
+//   k_grow_a/b: start of step (stop test, uniform-source interpolation of
 //               simulator.cu:500-538), then the 4-neighbour dilation of the
 //               wet tiles and the on-device compaction of the active /
-//               inactive / deactivated tile lists (Grow, grid.cu:1188-1322)
-//               with warp ballots and one block scan per 1024 tiles
+//               inactive / deactivated tile lists and of the march strips
+//               (Grow, grid.cu:1188-1322), chunked over the CTAs
+//               (rift_grow.cuh)
 //   k_speed_dt: per-tile local-speed maxima on U^n (the speed output of the
 //               first ComputeFluxes, grid.cu:813-838), the max over every
 //               tile (stale speeds of inactive tiles included) and, in
@@ -39,7 +40,6 @@ constexpr int TH = 14;          // tile height (BLOCK_ROWS, grid.cu:18)
 constexpr int SW = TW + 4;      // staged block width  (2-cell halo)
 constexpr int SH = TH + 4;      // staged block height
 constexpr int NT = 256;         // threads per tile CTA
-constexpr int GROW_T = 1024;    // threads of the single-CTA grow kernel
 constexpr int STRIP_TX = 7;     // march work item: 7 x 2 tiles = 112 x 28 cells
 constexpr int STRIP_TY = 2;
 constexpr int MAX_SERIES = 4096;
@@ -51,6 +51,7 @@ constexpr uint32_t F_RAIN_U = 1u << 0, F_RAIN_G = 1u << 1, F_DRAIN_U = 1u << 2,
                    F_TILE_ACC = 1u << 9, F_POINT = 1u << 10, F_H_INIT = 1u << 11;
 
 constexpr int ERR_TMA_TIMEOUT = 1;
+constexpr int ERR_BARRIER_TIMEOUT = 2;
 
 // Device-resident scalars of the run (one per handle).
 struct DevState {
@@ -70,8 +71,11 @@ struct DevState {
     int nActive, nDeact, nInact;
     int nStrips;       // strips of the march kernels holding an active tile
     int stop;
+    int persistExit;   // the persistent kernel left because the active set grew
     int steps_done;
     unsigned long long activeCells;  // interior cells of active tiles, summed over steps
+    double v_added;    // volume (depth x cells) the sources added since init
+    double rain_sum[2];  // interior sums of the two rain maps (volume ledger)
     int error;
     int err_info;
 };
@@ -98,7 +102,7 @@ struct Params {
     const float* map1[3];
     int mapMode[3];    // 0 none, 1 hold, 2 interpolate
     uint8_t* wet;
-    uint8_t* prevAct;  // active set of the current step (after k_grow)
+    uint8_t* prevAct;  // active set of the current step (after the grow)
     int* act;          // active tiles that hold interior cells
     int* deact;
     int* inact;
@@ -106,6 +110,10 @@ struct Params {
     uint8_t* stripFlag;
     int nSX, nSY;      // strip grid (strips of 7 x 2 tiles)
     int marchMin;      // active strips from which the march kernels run
+    int persistMax;    // the persistent step kernel runs while active tiles <= this
+    struct GridBar* gbar;            // grid barrier of the persistent kernel
+    int* growCnt;                    // [CTA][4] list counts of the chunked grow
+    unsigned long long* growCells;   // [CTA] interior cells of active tiles
     float* mx;
     float* my;
     const int* srcIdx;      // flat h-grid indices j*nx+i
@@ -276,6 +284,17 @@ __device__ __forceinline__ void finishDt(const Params& P, float amx, float amy, 
         st->dt_old = st->dt;
         st->dt = dt;
         st->t = st->t + dt;
+        // volume ledger: both RK stages (or the Euler stage) apply each
+        // source rate of this step for dt -- uniform rain on every interior
+        // cell, the point sources, the gridded rain map at this step's factor
+        double add = 0.0;
+        if (P.flags & F_RAIN_U) add += (double)st->rain_rate * (double)(P.nx - 4) * (P.ny - 4);
+        for (int k = 0; k < P.nsrc; k++) add += (double)P.srcRate[k];
+        if ((P.flags & F_RAIN_G) && P.mapMode[0] != 0) {
+            add += st->rain_sum[0];
+            if (P.mapMode[0] == 2) add += (double)st->factor[0] * (st->rain_sum[1] - st->rain_sum[0]);
+        }
+        st->v_added += add * dt;
     }
 }
 
@@ -332,17 +351,23 @@ __device__ __forceinline__ void issueTile(TileBuf& b, uint64_t* bar, const CUten
     tma_load_3d(&b.e[0][0][0], tmE, bar, bX * TW, bY * TH, 0);
 }
 
-// Prologue shared by the tile kernels: barriers and the first tile's load.
-__device__ __forceinline__ void tilePrologue(StageSmem& S, const CUtensorMap* tmIn,
-                                             const CUtensorMap* tmE, const Params& P, int nAct) {
+// Barriers of the tile buffers and the tensor-map prefetch (once per kernel).
+__device__ __forceinline__ void tileInit(StageSmem& S, const CUtensorMap* tmIn,
+                                         const CUtensorMap* tmE) {
     if (threadIdx.x == 0) {
         prefetch_tmap(tmIn);
         prefetch_tmap(tmE);
         mbar_init(&S.bar[0], 1);
         mbar_init(&S.bar[1], 1);
         fence_mbar_init();
-        if ((int)blockIdx.x < nAct) issueTile(S.buf[0], &S.bar[0], tmIn, tmE, P, P.act[blockIdx.x]);
     }
+}
+
+// Start of a tile loop: the CTA's first tile into buffer 0.
+__device__ __forceinline__ void tileFirst(StageSmem& S, const CUtensorMap* tmIn,
+                                          const CUtensorMap* tmE, const Params& P, int nAct) {
+    if (threadIdx.x == 0 && (int)blockIdx.x < nAct)
+        issueTile(S.buf[0], &S.bar[0], tmIn, tmE, P, P.act[blockIdx.x]);
     __syncthreads();
 }
 
@@ -420,9 +445,8 @@ __device__ void beginStep(const Params& P, DevState* s) {
 // TrackRainfall_k / TrackSurge_k over the tiles that were inactive after the
 // previous Grow.  The rows come from blockY * BLOCK_COLS (16), not 14, as in
 // the reference.
-__global__ void __launch_bounds__(NT) k_track(Params P) {
+__device__ __forceinline__ void trackTiles(const Params& P) {
     const DevState* s = P.st;
-    if (s->t >= s->t_stop) return;
     const int n = s->nInact;
     float fac0 = s->factor[0], fac2 = s->factor[2];
     if (s->map_timed[0]) fac0 = (float)((s->t - s->map_t0[0]) / (s->map_t1[0] - s->map_t0[0]));
@@ -451,118 +475,9 @@ __global__ void __launch_bounds__(NT) k_track(Params P) {
     }
 }
 
-// ---------------------------------------------------------------- k_grow
-// Single CTA.  active(t) = wet(t) | wet(4-neighbours), false outside the tile
-// grid; tile 0 is always kept (the reference encodes it as 0, never negative).  One
-// block scan per 1024 tiles compacts (ascending) the active tiles that hold
-// interior cells, the inactive tiles other than tile 0 (tracked next step)
-// and the tiles that went from active to inactive.  Active tiles without
-// interior cells (the reference computes them and writes mx = my = 0) get
-// their zero speeds here and are not scheduled.
-__global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
-    DevState* s = P.st;
-    __shared__ int stop;
-    __shared__ int wsum[3][33];
-    __shared__ unsigned long long cellSum;
-    if (threadIdx.x == 0) {
-        stop = (s->t >= s->t_stop) ? 1 : 0;
-        if (stop)
-            s->stop = 1;
-        else
-            beginStep(P, s);
-        cellSum = 0ull;
-    }
-    __syncthreads();
-    if (stop) return;
-    const int nBX = P.nBX, nBY = P.nBY;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int nStripsAll = P.nSX * P.nSY;
-    for (int q = threadIdx.x; q < nStripsAll; q += GROW_T) P.stripFlag[q] = 0;
-    __syncthreads();
-    int base[3] = {0, 0, 0};
-    unsigned long long myCells = 0ull;
-    for (int b0 = 0; b0 < P.gridSize; b0 += GROW_T) {
-        const int b = b0 + threadIdx.x;
-        int flag[3] = {0, 0, 0};  // scheduled active, deactivated, inactive
-        bool v = false;
-        if (b < P.gridSize) {
-            const int bX = b % nBX, bY = b / nBX;
-            v = P.wet[b] || (bX > 0 && P.wet[b - 1]) || (bX < nBX - 1 && P.wet[b + 1]) ||
-                (bY > 0 && P.wet[b - nBX]) || (bY < nBY - 1 && P.wet[b + nBX]) || b == 0;
-            const int i0 = bX * TW + 2, j0 = bY * TH + 2;
-            const bool interior = i0 <= P.nx - 3 && j0 <= P.ny - 3;
-            if (v && interior) {
-                flag[0] = 1;
-                P.stripFlag[(bY / STRIP_TY) * P.nSX + bX / STRIP_TX] = 1;
-                int ci = min(P.nx - 3, i0 + TW - 1) - i0 + 1;
-                int cj = min(P.ny - 3, j0 + TH - 1) - j0 + 1;
-                myCells += (unsigned long long)(ci * cj);
-            } else if (v) {
-                P.mx[b] = 0.f;
-                P.my[b] = 0.f;
-            }
-            flag[1] = (P.prevAct[b] && !v) ? 1 : 0;
-            flag[2] = (!v && b != 0) ? 1 : 0;
-        }
-        unsigned bal[3];
-        int inWarp[3];
-        for (int q = 0; q < 3; q++) {
-            bal[q] = __ballot_sync(0xffffffffu, flag[q]);
-            inWarp[q] = __popc(bal[q] & ((1u << lane) - 1u));
-            if (lane == 0) wsum[q][w] = __popc(bal[q]);
-        }
-        __syncthreads();
-        if (w < 3) {  // warp q scans list q's 32 warp totals
-            int v0 = wsum[w][lane], x = v0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            wsum[w][lane] = x - v0;
-            if (lane == 31) wsum[w][32] = x;
-        }
-        __syncthreads();
-        if (b < P.gridSize) {
-            if (flag[0]) P.act[base[0] + wsum[0][w] + inWarp[0]] = b;
-            if (flag[1]) P.deact[base[1] + wsum[1][w] + inWarp[1]] = b;
-            if (flag[2]) P.inact[base[2] + wsum[2][w] + inWarp[2]] = b;
-            P.prevAct[b] = (uint8_t)(v ? 1 : 0);
-        }
-        for (int q = 0; q < 3; q++) base[q] += wsum[q][32];
-        __syncthreads();
-    }
-    for (int o = 16; o > 0; o >>= 1) myCells += __shfl_xor_sync(0xffffffffu, myCells, o);
-    if (lane == 0) atomicAdd(&cellSum, myCells);
-    // compaction of the strips (work items of the march kernels), ascending
-    int baseS = 0;
-    for (int q0 = 0; q0 < nStripsAll; q0 += GROW_T) {
-        const int q = q0 + threadIdx.x;
-        const int f = (q < nStripsAll && P.stripFlag[q]) ? 1 : 0;
-        const unsigned bal = __ballot_sync(0xffffffffu, f);
-        const int inWarp = __popc(bal & ((1u << lane) - 1u));
-        if (lane == 0) wsum[0][w] = __popc(bal);
-        __syncthreads();
-        if (w == 0) {
-            int v0 = wsum[0][lane], x = v0;
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (lane >= o) x += y;
-            }
-            wsum[0][lane] = x - v0;
-            if (lane == 31) wsum[0][32] = x;
-        }
-        __syncthreads();
-        if (f) P.strips[baseS + wsum[0][w] + inWarp] = q;
-        baseS += wsum[0][32];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        s->nActive = base[0];
-        s->nDeact = base[1];
-        s->nInact = base[2];
-        s->nStrips = baseS;
-        s->activeCells += cellSum;
-    }
+__global__ void __launch_bounds__(NT) k_track(Params P) {
+    if (P.st->t >= P.st->t_stop) return;
+    trackTiles(P);
 }
 
 // ------------------------------------------------------------- k_speed_dt
@@ -572,28 +487,23 @@ __global__ void __launch_bounds__(GROW_T) k_grow(Params P) {
 // CTA, dt with the reference's rounding points (fmaxf of the scaled maxima,
 // FP64 division) and t += dt.  Also re-syncs U* with U^n on tiles that went
 // inactive this step (interior cells and the ghost cells they own).
-__global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtensorMap tmA,
-                                                 const __grid_constant__ CUtensorMap tmE, Params P) {
-    __shared__ StageSmem S;
-    __shared__ bool last;
+// Tile loop of the speed pass over the scheduled active tiles; thread 0
+// keeps the CTA's maximum of the new tile speeds.  False after a TMA
+// timeout (error recorded).
+__device__ bool speedTiles(StageSmem& S, const CUtensorMap* tmA, const CUtensorMap* tmE,
+                           const Params& P, int nAct, uint32_t* ph, float& tmx, float& tmy) {
     DevState* st = P.st;
-    if (st->stop || useMarch(P)) return;
     const int tid = threadIdx.x;
-    const int nAct = st->nActive;
-    tilePrologue(S, &tmA, &tmE, P, nAct);
     const float kappa = P.kappa;
-    float amx = 0.f, amy = 0.f;
-    staleMax(P, amx, amy);
-    uint32_t ph[2] = {0u, 0u};
+    tileFirst(S, tmA, tmE, P, nAct);
     int bsel = 0;
-    float tmx = 0.f, tmy = 0.f;  // thread 0: max of this CTA's new tile speeds
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];
         int bX, bY, i0, j0;
         tileOrigin(P, tile, bX, bY, i0, j0);
-        if (!tileAcquire(S, &tmA, &tmE, P, bsel, ph, k + gridDim.x, nAct)) {
+        if (!tileAcquire(S, tmA, tmE, P, bsel, ph, k + gridDim.x, nAct)) {
             if (tid == 0) atomicOr(&st->error, ERR_TMA_TIMEOUT);
-            return;
+            return false;
         }
         const TileBuf& T = S.buf[bsel];
         float spx = 0.f, spy = 0.f;
@@ -648,6 +558,20 @@ __global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtenso
         }
         __syncthreads();
     }
+    return true;
+}
+
+__global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtensorMap tmA,
+                                                 const __grid_constant__ CUtensorMap tmE, Params P) {
+    __shared__ StageSmem S;
+    __shared__ bool last;
+    if (P.st->stop || useMarch(P)) return;
+    tileInit(S, &tmA, &tmE);
+    float amx = 0.f, amy = 0.f;
+    staleMax(P, amx, amy);
+    uint32_t ph[2] = {0u, 0u};
+    float tmx = 0.f, tmy = 0.f;
+    if (!speedTiles(S, &tmA, &tmE, P, P.st->nActive, ph, tmx, tmy)) return;
     __syncthreads();
     finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
     resyncDeactivated(P);
@@ -693,15 +617,14 @@ __device__ __forceinline__ void writeGhosts(const Params& P, float* U, int j, in
 // STAGE 1: reads U^n (A) -> writes U* (B), F* (FB).
 // STAGE 2: reads U* (B) with halo and U^n (A) at the cell -> writes U^{n+1}
 //          (A), F^{n+1} (FA), outputs, tile wet flags and tile speeds.
+// Tile loop of RK stage STAGE over the scheduled active tiles.  False after
+// a TMA timeout (error recorded).
 template <int STAGE>
-__global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMap tmIn,
-                                              const __grid_constant__ CUtensorMap tmE, Params P) {
-    __shared__ StageSmem S;
+__device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensorMap* tmE,
+                           const Params& P, int nAct, uint32_t* ph) {
     const DevState* st = P.st;
-    if (st->stop || useMarch(P)) return;
     const int tid = threadIdx.x;
-    const int nAct = st->nActive;
-    tilePrologue(S, &tmIn, &tmE, P, nAct);
+    tileFirst(S, tmIn, tmE, P, nAct);
     const float kappa = P.kappa;
     const uint32_t fl = P.flags;
     const bool euler = (fl & F_EULER) != 0;
@@ -717,15 +640,14 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
     const float* Fin = (STAGE == 1) ? P.FA : P.FB;
     float* Fout = (STAGE == 1) ? P.FB : P.FA;
 
-    uint32_t ph[2] = {0u, 0u};
     int bsel = 0;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];
         int bX, bY, i0, j0;
         tileOrigin(P, tile, bX, bY, i0, j0);
-        if (!tileAcquire(S, &tmIn, &tmE, P, bsel, ph, k + gridDim.x, nAct)) {
+        if (!tileAcquire(S, tmIn, tmE, P, bsel, ph, k + gridDim.x, nAct)) {
             if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
-            return;
+            return false;
         }
         const TileBuf& T = S.buf[bsel];
         // ---- x reconstruction: cells i0-1 .. i0+16 on the 14 tile rows
@@ -926,6 +848,17 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
         }
         __syncthreads();
     }
+    return true;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMap tmIn,
+                                              const __grid_constant__ CUtensorMap tmE, Params P) {
+    __shared__ StageSmem S;
+    if (P.st->stop || useMarch(P)) return;
+    tileInit(S, &tmIn, &tmE);
+    uint32_t ph[2] = {0u, 0u};
+    stageTiles<STAGE>(S, &tmIn, &tmE, P, P.st->nActive, ph);
 }
 
 // ---------------------------------------------------------------- k_commit
@@ -933,10 +866,7 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
 // result, written to the stage buffer so that no CTA reads a halo cell
 // another CTA is updating, is copied back over U^n for the active tiles
 // (interior cells and the ghost cells they own), together with F.
-__global__ void __launch_bounds__(NT) k_commit(Params P) {
-    const DevState* st = P.st;
-    if (st->stop) return;
-    const int nAct = st->nActive;
+__device__ __forceinline__ void commitTiles(const Params& P, int nAct) {
     const int tid = threadIdx.x;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x) {
         const int tile = P.act[k];
@@ -966,6 +896,11 @@ __global__ void __launch_bounds__(NT) k_commit(Params P) {
             cp(P.ny - 1, i);
         }
     }
+}
+
+__global__ void __launch_bounds__(NT) k_commit(Params P) {
+    if (P.st->stop) return;
+    commitTiles(P, P.st->nActive);
 }
 
 // ---------------------------------------------------------------- volume

@@ -1,0 +1,147 @@
+// rift_persist.cuh -- the whole step loop in one cooperative launch.
+//
+// For a small or mostly dry grid the step is a chain of short phases, and
+// separate kernel launches spend more time starting and draining than
+// working.  k_persist runs many steps in one cooperative launch (all CTAs
+// resident), the phases separated by a grid barrier:
+//   [track]  re-wet inactive tiles under gridded rain / surge
+//   grow A   each CTA counts the list entries of its chunk of strips
+//   grow B   each CTA writes its chunk of the lists (rift_grow.cuh)
+//   speed    tile speeds of U^n, dt and t (last CTA), U* re-sync
+//   stage 1  RK stage 1 (per-tile code of k_stage<1>)
+//   stage 2  RK stage 2, or the Euler commit
+// The phases run the same device functions as the per-tile kernels, so the
+// results are identical.  The kernel leaves at a step boundary when
+// t >= t_stop, after the requested number of steps, or when the active set
+// has outgrown P.persistMax (the host then continues with the per-step
+// launches, whose march kernels suit a dense grid).
+//
+// Every wait is bounded: a grid barrier gives up after ~2^22 polls, records
+// ERR_BARRIER_TIMEOUT and the kernel returns; no TMA copy is in flight at a
+// barrier (each tile loop consumes every load it issues).
+#pragma once
+#include "rift_grow.cuh"
+#include "rift_kernels.cuh"
+
+namespace rift {
+
+constexpr int GB_GROUP = 16;    // CTAs per first-level barrier counter
+constexpr int GB_MAXGROUPS = 128;
+constexpr int PERSIST_MAX_CTAS = GB_GROUP * GB_MAXGROUPS;
+
+// Two-level combining barrier: each counter on its own 128-byte line.
+struct GridBar {
+    unsigned grp[GB_MAXGROUPS][32];
+    unsigned top[32];
+    unsigned gen[32];
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+// Grid-wide barrier with release/acquire at GPU scope.  The last CTA of a
+// group resets the group counter and arrives at the top counter; the last
+// group resets that and advances the generation word, which every CTA's
+// thread 0 polls.  After the barrier, TMA loads (async proxy) see the
+// generic-proxy writes made before it.  False after a timeout.
+__device__ bool gridSync(GridBar* gb, unsigned& gen, DevState* st) {
+    __syncthreads();
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        const unsigned nb = gridDim.x, g = blockIdx.x / GB_GROUP;
+        const unsigned ng = (nb + GB_GROUP - 1) / GB_GROUP;
+        const unsigned gsz = min((unsigned)GB_GROUP, nb - g * GB_GROUP);
+        __threadfence();
+        if (atomicAdd(&gb->grp[g][0], 1u) == gsz - 1) {
+            atomicExch(&gb->grp[g][0], 0u);
+            __threadfence();
+            if (atomicAdd(&gb->top[0], 1u) == ng - 1) {
+                atomicExch(&gb->top[0], 0u);
+                __threadfence();
+                atomicAdd(&gb->gen[0], 1u);
+            }
+        }
+        ok = 0;
+        for (int it = 0; it < (1 << 22); ++it) {
+            if (ld_acquire_gpu(&gb->gen[0]) != gen) {
+                ok = 1;
+                break;
+            }
+            __nanosleep(32);
+        }
+        gen += 1u;
+        __threadfence();
+        fence_proxy_async_global();
+        if (!ok) atomicOr(&st->error, ERR_BARRIER_TIMEOUT);
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
+// The step loop.  maxSteps: steps to attempt in this launch.
+__global__ void __launch_bounds__(NT) k_persist(const __grid_constant__ CUtensorMap tmA,
+                                                const __grid_constant__ CUtensorMap tmB,
+                                                const __grid_constant__ CUtensorMap tmE, Params P,
+                                                int maxSteps) {
+    __shared__ StageSmem S;
+    __shared__ GrowSmem G;
+    __shared__ bool last;
+    DevState* st = P.st;
+    const int tid = threadIdx.x;
+    const uint32_t fl = P.flags;
+    const bool track = (fl & (F_RAIN_G | F_SURGE)) != 0;
+    tileInit(S, &tmA, &tmE);
+    if (tid == 0) prefetch_tmap(&tmB);
+    uint32_t ph[2] = {0u, 0u};
+    unsigned gen = 0u;
+    int nActPrev = 0;
+    if (blockIdx.x == 0 && tid == 0) st->persistExit = 0;
+#define RIFT_SYNC()                          \
+    if (!gridSync(P.gbar, gen, st)) return; \
+    (void)0
+    for (int step = 0; step < maxSteps; step++) {
+        // every CTA reads the same t (written before the last barrier)
+        if (st->t >= st->t_stop) {
+            if (blockIdx.x == 0 && tid == 0) st->stop = 1;
+            return;
+        }
+        if (step > 0 && nActPrev > P.persistMax) {
+            if (blockIdx.x == 0 && tid == 0) st->persistExit = 1;
+            return;
+        }
+        if (track) {
+            trackTiles(P);
+            RIFT_SYNC();
+        }
+        if (blockIdx.x == 0 && tid == 0) beginStep(P, st);
+        growCount(P, G);
+        RIFT_SYNC();
+        const int nAct = growWrite(P, G);
+        nActPrev = nAct;
+        RIFT_SYNC();
+        // speeds of U^n, dt, t, U* re-sync (k_speed_dt)
+        float amx = 0.f, amy = 0.f, tmx = 0.f, tmy = 0.f;
+        staleMax(P, amx, amy);
+        if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
+        __syncthreads();
+        finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
+        resyncDeactivated(P);
+        RIFT_SYNC();
+        if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph)) return;
+        RIFT_SYNC();
+        if (!(fl & F_EULER)) {
+            if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph)) return;
+        } else {
+            commitTiles(P, nAct);
+        }
+        RIFT_SYNC();
+    }
+#undef RIFT_SYNC
+}
+
+}  // namespace rift

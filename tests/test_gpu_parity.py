@@ -26,13 +26,19 @@ def _close(a, b, what):
     assert d.max() <= MAX_TOL, f"{what}: max {d.max()}"
 
 
-SCHEDULES = {"auto": -1, "march": 0, "tiles": 1 << 30}
+# (march threshold in strips, persistent-loop threshold in tiles)
+SCHEDULES = {"auto": (-1, -1), "tiles": (1 << 30, 0), "march": (0, 0),
+             "persist": (1 << 30, 1 << 30)}
+
+
+def _scheduled(sim, schedule):
+    march, persist = SCHEDULES[schedule]
+    return sim.set_schedule(march).set_persistent(persist)
 
 
 def _run_against_golden(engine_api, name, schedule="auto"):
     fx, case = FX.load(name)
-    eng = capi.Sim(case, api=engine_api).set_schedule(SCHEDULES[schedule])
-    eng = FX.start(eng, fx)
+    eng = FX.start(_scheduled(capi.Sim(case, api=engine_api), schedule), fx)
     step = 0
     log = fx["steps_log"]
     for s in FX.dumps(fx):
@@ -54,18 +60,44 @@ def _run_against_golden(engine_api, name, schedule="auto"):
         if "twet" in ref:
             tw = eng.field("TWET")
             assert np.array_equal(FX.interior(tw) < 0, FX.interior(ref["twet"]) < 0), name
+    return eng
 
 
-@pytest.mark.parametrize("schedule", ["tiles", "march"])
+@pytest.mark.parametrize("schedule", ["tiles", "march", "persist"])
 @pytest.mark.parametrize("name", FX.CASES)
 def test_engine_matches_reference_kernels(engine_api, name, schedule):
-    """Both kernel schedules (per-tile and column march) against the
-    reference kernels."""
-    _run_against_golden(engine_api, name, schedule)
+    """Every kernel schedule (per-tile kernels, column march, persistent
+    cooperative loop) against the reference kernels."""
+    eng = _run_against_golden(engine_api, name, schedule)
+    persist_steps, graph_steps = eng.path_stats()
+    if schedule == "persist":
+        assert graph_steps == 0 and persist_steps > 0
+    else:
+        assert persist_steps == 0 and graph_steps > 0
 
 
+def test_persistent_hands_over_to_graph(engine_api):
+    """A persistent threshold below the active-tile count makes the loop
+    leave after its first step and the per-step graph finish the run with
+    the same results as the graph alone."""
+    fx, case = FX.load("rain")
+    runs = []
+    for persist in (1, 0):
+        eng = FX.start(_scheduled(capi.Sim(case, api=engine_api), "tiles").set_persistent(persist),
+                       fx)
+        eng.run(12)
+        runs.append((eng.tiles(), eng.field("W"), eng.time(), eng.path_stats()))
+    (w1, a1), W1, t1, st1 = runs[0]
+    (w0, a0), W0, t0, st0 = runs[1]
+    assert st1[0] >= 1 and st1[1] >= 1 and st1[0] + st1[1] == 12
+    assert np.array_equal(w1, w0) and np.array_equal(a1, a0)
+    assert abs(t1[0] - t0[0]) <= 1e-6 * max(1.0, t0[0])
+    _close(W1, W0, "persistent then graph vs graph")
+
+
+@pytest.mark.parametrize("schedule", ["tiles", "march", "persist"])
 @pytest.mark.parametrize("name", ["rain", "front", "gridrain_surge", "h0_infil_src", "euler"])
-def test_one_step_from_identical_snapshot(engine_api, oracle_api, name):
+def test_one_step_from_identical_snapshot(engine_api, oracle_api, name, schedule):
     """From the reference's own state at a dumped step, one engine step and one
     oracle step give identical tile sets and depths within tolerance."""
     fx, case = FX.load(name)
@@ -75,7 +107,7 @@ def test_one_step_from_identical_snapshot(engine_api, oracle_api, name):
     for api, mode in ((engine_api, None), (oracle_api, 0)):
         sim = capi.Sim(case, api=api, create_mode=mode)
         if mode is None:
-            sim.set_schedule(0)  # the march kernels (the tiles run in the golden test)
+            _scheduled(sim, schedule)
         sim = FX.start(sim, fx)
         sim.set_state(ref["t"], ref["dt"], ref["w"], ref["hu"], ref["hv"], ref.get("F"),
                       ref["wet"], ref["active"], ref["mx"], ref["my"])
