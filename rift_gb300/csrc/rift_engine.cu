@@ -740,13 +740,18 @@ int rift_set_series(rift_handle* h, int32_t which, const float* times, const flo
 
 namespace {
 
-// One cooperative launch of the step loop for at most `nsteps` steps.
+// One cooperative launch of the step loop for at most `nsteps` steps.  The
+// grid is a whole number of CTAs per SM, enough for one active tile per CTA
+// at the last known count (up to full occupancy): a smaller grid makes each
+// grid barrier cheaper.
 int launchPersist(rift_handle* h, int nsteps) {
     CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream));
     Params P = makeParams(h);
+    const int perSM = (std::max(h->hst->nActive, 1) + h->numSMs - 1) / h->numSMs;
+    const int grid = std::min(h->gridPersist, h->numSMs * perSM);
     void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
-    CUDA_TRY(h, cudaLaunchCooperativeKernel((const void*)k_persist, dim3(h->gridPersist),
-                                            dim3(NT), args, 0, h->stream));
+    CUDA_TRY(h, cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0,
+                                            h->stream));
     return RIFT_OK;
 }
 

@@ -645,6 +645,27 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
         const int tile = P.act[k];
         int bX, bY, i0, j0;
         tileOrigin(P, tile, bX, bY, i0, j0);
+        // the cell's own global inputs, loaded while the staged block is in
+        // flight: stage 1 Manning n, stage 2 U^n; F and K with infiltration
+        float pre0 = 0.f, pre1 = 0.f, pre2 = 0.f, preF = 0.f, preFA = 0.f, preK = 0.f;
+        {
+            const int ip = i0 + tid % TW, jp = j0 + tid / TW;
+            if (tid < TH * TW && ip <= P.nx - 3 && jp <= P.ny - 3) {
+                const size_t c = cidx(P, 0, jp, ip);
+                if (STAGE == 1) {
+                    pre0 = P.nman[c];
+                } else {
+                    pre0 = P.A[c];
+                    pre1 = P.A[cidx(P, 1, jp, ip)];
+                    pre2 = P.A[cidx(P, 2, jp, ip)];
+                }
+                if (fl & F_INFIL) {
+                    preF = Fin[c];
+                    preK = P.K[c];
+                    if (STAGE == 2) preFA = P.FA[c];
+                }
+            }
+        }
         if (!tileAcquire(S, tmIn, tmE, P, bsel, ph, k + gridDim.x, nAct)) {
             if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
             return false;
@@ -764,8 +785,8 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
                 }
                 float dF = 0.f, Fc = 0.f;
                 if (fl & F_INFIL) {
-                    Fc = Fin[c];
-                    dF = greenAmpt(P.K[c], Fc, P.psiDtheta, dtSrc, hC);
+                    Fc = preF;
+                    dF = greenAmpt(preK, Fc, P.psiDtheta, dtSrc, hC);
                     S0 -= dF;
                 }
                 dh += S0;
@@ -775,7 +796,7 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
                 float hN, huN, hvN;
                 if (STAGE == 1) {
                     // Integrate_1_k (grid.cu:856-922)
-                    const float G = manningG(P.nman[c], hu0, hv0, hC, kappa);
+                    const float G = manningG(pre0, hu0, hv0, hC, kappa);
                     if (fl & F_SURGE) {
                         float sg = mapValue(P, 2, c, fac2);
                         if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
@@ -808,13 +829,13 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
                     }
                 } else {
                     // Integrate_2_k (grid.cu:1043-1171)
-                    const float hOld = P.A[cidx(P, 0, j, i)];
+                    const float hOld = pre0;
                     const float hOc = (hOld > kEps) ? hOld : 0.f;
                     hN = 0.5f * (hOc + hc + dh * dtNew);
-                    huN = 0.5f * (P.A[cidx(P, 1, j, i)] + hu0 + dhu * dtNew);
-                    hvN = 0.5f * (P.A[cidx(P, 2, j, i)] + hv0 + dhv * dtNew);
+                    huN = 0.5f * (pre1 + hu0 + dhu * dtNew);
+                    hvN = 0.5f * (pre2 + hv0 + dhv * dtNew);
                     hN = (hN > kEps) ? hN : 0.f;
-                    if (fl & F_INFIL) Fout[c] = 0.5f * (P.FA[c] + Fc + dF * dtNew);
+                    if (fl & F_INFIL) Fout[c] = 0.5f * (preFA + Fc + dF * dtNew);
                     if (fl & F_SAVE_MAX) {
                         const float uC = huN * velFactor(hN, kappa);
                         const float vC = hvN * velFactor(hN, kappa);
