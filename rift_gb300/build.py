@@ -1,4 +1,6 @@
-"""In-tree build of the CUDA engine (sm_103a) into rift_gb300/_lib/."""
+"""In-tree build into rift_gb300/_lib/: the CUDA engine (sm_103a,
+librift_gb300.so), the host drop-in layer above its C ABI (librift_host.so)
+and the command-line driver (rift-sim)."""
 from __future__ import annotations
 
 import os
@@ -21,6 +23,38 @@ def _stale(out, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+HOST_SRC = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(LIB_DIR, "librift_host.so")
+HOST_CLI = os.path.join(LIB_DIR, "rift-sim")
+HOST_SOURCES = ["host_io.cpp", "grid_series.cpp", "simulator.cpp"]
+HOST_DEPS = HOST_SOURCES + ["host_internal.hpp", "grid_series.hpp", "rift_sim_main.cpp"]
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{cmd[0]} failed:\n{r.stdout}\n{r.stderr}")
+    return r
+
+
+def build_host(force: bool = False) -> str:
+    """librift_host.so (linked to the engine, found next to it at run time)
+    and the rift-sim driver."""
+    build(force=force)
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    deps = [os.path.join(HOST_SRC, d) for d in HOST_DEPS]
+    deps += [os.path.join(inc, "rift_host.h"), os.path.join(inc, "rift_gb300.h"), LIB]
+    rpath = ["-Wl,-rpath,$ORIGIN", f"-L{LIB_DIR}", "-lrift_gb300"]
+    if force or _stale(HOST_LIB, deps):
+        _run(["g++", *HOST_FLAGS, "-shared", "-o", HOST_LIB,
+              *[os.path.join(HOST_SRC, s) for s in HOST_SOURCES], *rpath])
+    if force or _stale(HOST_CLI, deps + [HOST_LIB]):
+        _run(["g++", *HOST_FLAGS, "-o", HOST_CLI, os.path.join(HOST_SRC, "rift_sim_main.cpp"),
+              f"-L{LIB_DIR}", "-lrift_host", "-lrift_gb300", "-Wl,-rpath,$ORIGIN"])
+    return HOST_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIB_DIR, exist_ok=True)
     deps = [os.path.join(SRC, d) for d in DEPS]
@@ -29,9 +63,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cmd = ["nvcc", *ARCH, *FLAGS, "-o", LIB, *[os.path.join(SRC, s) for s in SOURCES]]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed:\n{r.stdout}\n{r.stderr}")
+        r = _run(cmd)
         if verbose:
             print(r.stderr)
     return LIB
@@ -39,3 +71,4 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
 if __name__ == "__main__":
     print(build(force=True, verbose=True))
+    print(build_host(force=True))

@@ -1,5 +1,6 @@
-"""The C-ABI library loads and exports every entry point include/rift_gb300.h
-declares (no device calls)."""
+"""The C-ABI libraries load and export every entry point include/*.h declares
+(no device calls): the engine (rift_gb300.h) and the host layer
+(rift_host.h)."""
 import ctypes
 import os
 import re
@@ -9,8 +10,8 @@ from rift_gb300 import build as eb
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "rift_gb300.h")).read()
+def declared_symbols(header="rift_gb300.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     return sorted(set(re.findall(r"\b(rift_[a-z_0-9]+)\s*\(", src)))
 
 
@@ -22,11 +23,19 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, n), n
 
 
+def test_host_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(eb.build_host())
+    names = declared_symbols("rift_host.h")
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+
+
 def test_product_has_no_cpu_fallback():
     """The package never loads the oracle: no reference to it in product code."""
     pkg = os.path.join(ROOT, "rift_gb300")
     for dirpath, _, files in os.walk(pkg):
         for f in files:
-            if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+            if f.endswith((".py", ".cu", ".cuh", ".h", ".hpp", ".cpp")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "rift_oracle" not in txt, f
