@@ -68,14 +68,56 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """SM clock and clock-event reasons sampled during the timed region:
+    NVML through ctypes every millisecond (a timed region of a few ms still
+    gets samples), else nvidia-smi every 100 ms.  Reads only."""
+
+    # nvmlClocksEventReason* bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
 
     def __init__(self):
-        self.samples = []
+        self.samples = []  # (sm_mhz, reason bits)
+        self.sm_max = None
         self._stop = threading.Event()
+        self._thread = None
         self._proc = None
 
+    def _nvml(self):
+        nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit")
+        idx = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        dev = ctypes.c_void_p()
+        if not idx.isdigit() or nv.nvmlDeviceGetHandleByIndex_v2(int(idx), ctypes.byref(dev)) != 0:
+            if nv.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(dev)) != 0:
+                raise OSError("nvmlDeviceGetHandleByIndex")
+        mx = ctypes.c_uint()
+        if nv.nvmlDeviceGetMaxClockInfo(dev, 1, ctypes.byref(mx)) == 0:  # NVML_CLOCK_SM
+            self.sm_max = float(mx.value)
+        reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        return nv, dev, reasons
+
     def start(self):
+        try:
+            nv, dev, reasons = self._nvml()
+
+            def loop():
+                clk, bits = ctypes.c_uint(), ctypes.c_ulonglong()
+                while not self._stop.is_set():
+                    if nv.nvmlDeviceGetClockInfo(dev, 1, ctypes.byref(clk)) == 0 and \
+                            reasons(dev, ctypes.byref(bits)) == 0:
+                        self.samples.append((float(clk.value), int(bits.value)))
+                    time.sleep(0.001)
+
+            self._thread = threading.Thread(target=loop, daemon=True)
+            self._thread.start()
+        except Exception:
+            self._start_smi()
+        return self
+
+    def _start_smi(self):
         q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
@@ -83,18 +125,24 @@ class ClockSampler:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", "-i", "0", f"--query-gpu={q}", "--format=csv,noheader,nounits",
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            threading.Thread(target=self._read, daemon=True).start()
+            threading.Thread(target=self._read_smi, daemon=True).start()
         except Exception:
             self._proc = None
-        return self
 
-    def _read(self):
+    def _read_smi(self):
+        bits = (0x8, 0x40, 0x20, 0x4)
         for line in self._proc.stdout:
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 6:
-                self.samples.append(parts)
+            if len(parts) >= 6 and parts[0].replace(".", "").isdigit():
+                if parts[1].replace(".", "").isdigit():
+                    self.sm_max = float(parts[1])
+                b = sum(bit for bit, v in zip(bits, parts[2:6]) if v.lower() == "active")
+                self.samples.append((float(parts[0]), b))
 
     def stop(self):
+        self._stop.set()
+        if self._thread:
+            self._thread.join(timeout=2)
         if self._proc:
             self._proc.terminate()
             try:
@@ -102,14 +150,11 @@ class ClockSampler:
             except Exception:
                 pass
         if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4)
-                          if s[2 + k].lower() == "active"})
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons}
+            return {"sm_mhz": None, "sm_max_mhz": self.sm_max, "reasons": ["unsampled"]}
+        reasons = sorted({name for _, b in self.samples for bit, name in self.REASONS.items()
+                          if b & bit})
+        return {"sm_mhz": float(np.median([c for c, _ in self.samples])),
+                "sm_max_mhz": self.sm_max, "reasons": reasons, "samples": len(self.samples)}
 
 
 def spin_up(sim, t_target, chunk=2000):
@@ -197,11 +242,15 @@ def run_ours(args, device=0, sync=None):
                   "schedule runs, the other exits at entry)")
         achieved = stage_cells * bytes_per / (stage_ms * 1e-3) / 1e9 if stage_ms > 0 else None
         launches = graph_steps * launches_per_step(case.flags) + (1 if persist_steps else 0)
+    # DRAM bytes (read + write) of the reported kernel per launch, from the
+    # ncu capture summarised under profiles/ (per step there)
     traffic = None
     prof = os.path.join(ROOT, "profiles", f"traffic_config{cfg}.json")
-    if os.path.exists(prof):
+    if os.path.exists(prof) and args.N is None:
         try:
-            traffic = json.load(open(prof)).get("bytes_per_step")
+            rec = json.load(open(prof))
+            if rec.get("kernel") == ("k_persist" if launches == 1 else "stages"):
+                traffic = rec["bytes_per_step"] * (steps if launches == 1 else 1)
         except Exception:
             traffic = None
     line = {
