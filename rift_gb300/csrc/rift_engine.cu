@@ -748,8 +748,10 @@ namespace {
 int launchPersist(rift_handle* h, int nsteps) {
     CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream));
     Params P = makeParams(h);
-    const int perSM = (std::max(h->hst->nActive, 1) + h->numSMs - 1) / h->numSMs;
-    const int grid = std::min(h->gridPersist, h->numSMs * perSM);
+    // before the first step the count is unknown: full occupancy
+    const int perSM = h->hst->nActive > 0 ? (h->hst->nActive + h->numSMs - 1) / h->numSMs
+                                          : h->gridPersist / h->numSMs;
+    const int grid = std::max(1, std::min(h->gridPersist, h->numSMs * perSM));
     void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
     CUDA_TRY(h, cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0,
                                             h->stream));

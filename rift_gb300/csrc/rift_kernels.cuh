@@ -614,6 +614,300 @@ __device__ __forceinline__ void writeGhosts(const Params& P, float* U, int j, in
     }
 }
 
+// Step-wide constants of a stage kernel.
+struct StageConsts {
+    float kappa, dtNew, dtSrc, invDtSrc, rainU, drainU, fac0, fac1, fac2;
+    double tNew;
+    uint32_t fl;
+    bool euler;
+    float* Uout;
+    const float* Fin;
+    float* Fout;
+};
+
+template <int STAGE>
+__device__ __forceinline__ StageConsts stageConsts(const Params& P) {
+    const DevState* st = P.st;
+    StageConsts C;
+    C.kappa = P.kappa;
+    C.fl = P.flags;
+    C.euler = (P.flags & F_EULER) != 0;
+    C.dtNew = (float)st->dt;
+    // source clamps use the dt passed to ComputeFluxes: the previous dt in
+    // stage 1 (simulator.cu:786-792), the new one in stage 2
+    C.dtSrc = (STAGE == 1) ? (float)st->dt_old : C.dtNew;
+    C.invDtSrc = 1.f / C.dtSrc;
+    C.tNew = st->t;
+    C.rainU = st->rain_rate;
+    C.drainU = st->drain_rate;
+    C.fac0 = st->factor[0];
+    C.fac1 = st->factor[1];
+    C.fac2 = st->factor[2];
+    C.Uout = (STAGE == 1) ? P.B : P.A;
+    C.Fin = (STAGE == 1) ? P.FA : P.FB;
+    C.Fout = (STAGE == 1) ? P.FB : P.FA;
+    return C;
+}
+
+// Sources, friction, the RK stage, outputs and ghost cells of interior cell
+// (j, i) of `tile`, given its flux divergence (dh, dhu, dhv) and its staged
+// state and face offsets.  Returns the cell's vote for the tile wet flag.
+// pre: the cell's own inputs loaded ahead of use -- stage 1: Manning n;
+// stage 2: U^n (h, hu, hv); with PREF also pre[3] = F entering the stage,
+// pre[4] = K, pre[5] = F^n (stage 2), else those are read here.
+template <int STAGE, bool PREF = false>
+__device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
+                                           int i, float dh, float dhu, float dhv, float hC,
+                                           float hu0, float hv0, float eW, float eE, float eS,
+                                           float eN, const float* pre) {
+    const uint32_t fl = C.fl;
+    const size_t c = cidx(P, 0, j, i);
+    // bed-slope source, grid.cu:701,751-752
+    const float S1 = -kG * hC * ((eE - eW) * P.inv_dx);
+    const float S2 = -kG * hC * ((eN - eS) * P.inv_dy);
+    // mass sources, grid.cu:763-807
+    float S0 = 0.f;
+    if (fl & F_RAIN_U) S0 += C.rainU;
+    float rainG = 0.f;
+    if (fl & F_RAIN_G) {
+        rainG = mapValue(P, 0, c, C.fac0);
+        S0 += rainG;
+    }
+    const float cap = hC * C.invDtSrc;
+    if (fl & F_DRAIN_U) S0 -= (C.drainU > cap) ? cap : C.drainU;
+    if (fl & F_DRAIN_G) {
+        float d = mapValue(P, 1, c, C.fac1);
+        S0 -= (d > cap) ? cap : d;
+    }
+    bool srcCell = false;
+    if (P.nsrc > 0) {
+        const int flat = j * P.nx + i;
+        for (int q = P.srcTileStart[tile]; q < P.srcTileStart[tile + 1]; q++) {
+            int sidx = P.srcTileList[q];
+            if (P.srcIdx[sidx] == flat) {
+                S0 += P.srcRate[sidx];
+                srcCell = true;
+            }
+        }
+    }
+    float dF = 0.f, Fc = 0.f;
+    if (fl & F_INFIL) {
+        Fc = PREF ? pre[3] : C.Fin[c];
+        dF = greenAmpt(PREF ? pre[4] : P.K[c], Fc, P.psiDtheta, C.dtSrc, hC);
+        S0 -= dF;
+    }
+    dh += S0;
+    dhu += S1;
+    dhv += S2;
+    const float hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
+    const float dtNew = C.dtNew;
+    float hN, huN, hvN;
+    bool wetCell = false;
+    if (STAGE == 1) {
+        // Integrate_1_k (grid.cu:856-922)
+        const float G = manningG(pre[0], hu0, hv0, hC, C.kappa);
+        if (fl & F_SURGE) {
+            float sg = mapValue(P, 2, c, C.fac2);
+            if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
+        }
+        hN = hc + dh * dtNew;
+        const float den = 1.f / (1.f - dtNew * G);
+        huN = (hu0 + dhu * dtNew) * den;
+        hvN = (hv0 + dhv * dtNew) * den;
+        hN = (hN > kEps) ? hN : 0.f;
+        if (fl & F_INFIL) C.Fout[c] = Fc + dF * dtNew;
+        if (C.euler) {
+            // Euler-mode outputs and wet flags (grid.cu:926-1023)
+            const float uC = huN * velFactor(hN, C.kappa), vC = hvN * velFactor(hN, C.kappa);
+            if (fl & F_SAVE_MAX) {
+                float hm = P.hmax[c];
+                if (hN > hm) P.tpeak[c] = (float)C.tNew;
+                if (hN > 0.0762f) P.tdry[c] = (float)C.tNew;
+                P.hmax[c] = fmaxf(hm, hN);
+                P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
+            }
+            if (fl & F_SAVE_ARR) {
+                if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)C.tNew;
+            }
+            wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
+                      ((fl & F_RAIN_G) && rainG > 0.f);
+            if (fl & F_SURGE) {
+                float sg = mapValue(P, 2, c, C.fac2);
+                if (sg != P.nodata && sg > 0.f) wetCell = true;
+            }
+        }
+    } else {
+        // Integrate_2_k (grid.cu:1043-1171)
+        const float hOld = pre[0];
+        const float hOc = (hOld > kEps) ? hOld : 0.f;
+        hN = 0.5f * (hOc + hc + dh * dtNew);
+        huN = 0.5f * (pre[1] + hu0 + dhu * dtNew);
+        hvN = 0.5f * (pre[2] + hv0 + dhv * dtNew);
+        hN = (hN > kEps) ? hN : 0.f;
+        if (fl & F_INFIL) C.Fout[c] = 0.5f * ((PREF ? pre[5] : P.FA[c]) + Fc + dF * dtNew);
+        if (fl & F_SAVE_MAX) {
+            const float uC = huN * velFactor(hN, C.kappa);
+            const float vC = hvN * velFactor(hN, C.kappa);
+            P.hmax[c] = fmaxf(P.hmax[c], hN);
+            P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
+        }
+        if (fl & F_SAVE_ARR) {
+            if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)C.tNew;
+        }
+        wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
+                  ((fl & F_RAIN_G) && rainG > 0.f);
+    }
+    C.Uout[cidx(P, 0, j, i)] = hN;
+    C.Uout[cidx(P, 1, j, i)] = huN;
+    C.Uout[cidx(P, 2, j, i)] = hvN;
+    writeGhosts(P, C.Uout, j, i, hN, huN, hvN);
+    return wetCell;
+}
+
+// Flux divergence of every interior cell of a staged tile (the ComputeFluxes_k
+// sweeps, grid.cu:659-746): x reconstruction of cells i0-1 .. i0+16 on the
+// 14 tile rows and the 17 x faces, then the y reconstruction of rows
+// j0-1 .. j0+14 and the 15 y faces.  Thread tid < 224 gets the divergence of
+// cell (tid / 16, tid % 16); with SPEEDS, spx / spy get the local speed of
+// the east / north face of that cell (0 outside the interior).
+template <bool SPEEDS>
+__device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, const Params& P, int i0,
+                                            int j0, float& dh, float& dhu, float& dhv, float& spx,
+                                            float& spy) {
+    const int tid = threadIdx.x;
+    const float kappa = P.kappa;
+    if (tid < TH * (TW + 2)) {
+        int r = tid / (TW + 2), c = tid % (TW + 2);
+        int sr = r + 2, sc = c + 1;
+        Rec R = construct(T.in[0][sr][sc], T.in[1][sr][sc], T.in[2][sr][sc], T.in[0][sr][sc + 1],
+                          T.in[1][sr][sc + 1], T.in[2][sr][sc + 1], T.in[0][sr][sc - 1],
+                          T.in[1][sr][sc - 1], T.in[2][sr][sc - 1], T.e[0][sr][sc], T.e[1][sr][sc],
+                          T.e[1][sr][sc] - T.e[0][sr][sc + 1], T.e[1][sr][sc - 1] - T.e[0][sr][sc]);
+        S.rec.x.P[0][r][c] = R.hP;
+        S.rec.x.P[1][r][c] = R.uP;
+        S.rec.x.P[2][r][c] = R.vP;
+        S.rec.x.M[0][r][c] = R.hM;
+        S.rec.x.M[1][r][c] = R.uM;
+        S.rec.x.M[2][r][c] = R.vM;
+    }
+    __syncthreads();
+    spx = 0.f;
+    spy = 0.f;
+    // face f lies between reconstructed cells f and f+1: the east face of
+    // tile column f-1
+    if (tid < TH * (TW + 1)) {
+        int r = tid / (TW + 1), f = tid % (TW + 1);
+        float fx[3];
+        float sp = faceFlux<0>(S.rec.x.P[0][r][f], S.rec.x.P[1][r][f], S.rec.x.P[2][r][f],
+                               S.rec.x.M[0][r][f + 1], S.rec.x.M[1][r][f + 1],
+                               S.rec.x.M[2][r][f + 1], kappa, fx);
+        S.FX[0][r][f] = fx[0];
+        S.FX[1][r][f] = fx[1];
+        S.FX[2][r][f] = fx[2];
+        if (SPEEDS && f >= 1 && i0 + f - 1 <= P.nx - 3 && j0 + r <= P.ny - 3) spx = sp;
+    }
+    __syncthreads();
+    const int tx = tid % TW, ty = tid / TW;
+    dh = dhu = dhv = 0.f;
+    if (tid < TH * TW) {
+        dh = -(S.FX[0][ty][tx + 1] - S.FX[0][ty][tx]) * P.inv_dx;
+        dhu = -(S.FX[1][ty][tx + 1] - S.FX[1][ty][tx]) * P.inv_dx;
+        dhv = -(S.FX[2][ty][tx + 1] - S.FX[2][ty][tx]) * P.inv_dx;
+    }
+    if (tid < (TH + 2) * TW) {
+        int r = tid / TW, c = tid % TW;
+        int sr = r + 1, sc = c + 2;
+        Rec R = construct(T.in[0][sr][sc], T.in[1][sr][sc], T.in[2][sr][sc], T.in[0][sr + 1][sc],
+                          T.in[1][sr + 1][sc], T.in[2][sr + 1][sc], T.in[0][sr - 1][sc],
+                          T.in[1][sr - 1][sc], T.in[2][sr - 1][sc], T.e[2][sr][sc], T.e[3][sr][sc],
+                          T.e[3][sr][sc] - T.e[2][sr + 1][sc], T.e[3][sr - 1][sc] - T.e[2][sr][sc]);
+        S.rec.y.P[0][r][c] = R.hP;
+        S.rec.y.P[1][r][c] = R.uP;
+        S.rec.y.P[2][r][c] = R.vP;
+        S.rec.y.M[0][r][c] = R.hM;
+        S.rec.y.M[1][r][c] = R.uM;
+        S.rec.y.M[2][r][c] = R.vM;
+    }
+    __syncthreads();
+    if (tid < (TH + 1) * TW) {
+        int r = tid / TW, c = tid % TW;
+        float fy[3];
+        float sp = faceFlux<1>(S.rec.y.P[0][r][c], S.rec.y.P[1][r][c], S.rec.y.P[2][r][c],
+                               S.rec.y.M[0][r + 1][c], S.rec.y.M[1][r + 1][c],
+                               S.rec.y.M[2][r + 1][c], kappa, fy);
+        S.FY[0][r][c] = fy[0];
+        S.FY[1][r][c] = fy[1];
+        S.FY[2][r][c] = fy[2];
+        // face r is the north face of tile row r-1
+        if (SPEEDS && r >= 1 && i0 + c <= P.nx - 3 && j0 + r - 1 <= P.ny - 3) spy = sp;
+    }
+    __syncthreads();
+    if (tid < TH * TW) {
+        dh += -(S.FY[0][ty + 1][tx] - S.FY[0][ty][tx]) * P.inv_dy;
+        dhu += -(S.FY[1][ty + 1][tx] - S.FY[1][ty][tx]) * P.inv_dy;
+        dhv += -(S.FY[2][ty + 1][tx] - S.FY[2][ty][tx]) * P.inv_dy;
+    }
+}
+
+// The cell's own global inputs for cellUpdate<STAGE, true> (pre[0..5]),
+// loaded while the staged block is in flight.
+template <int STAGE>
+__device__ __forceinline__ void tilePrefetch(const Params& P, const StageConsts& C, int i0, int j0,
+                                             float (&pre)[6]) {
+    const int tid = threadIdx.x;
+    for (int q = 0; q < 6; q++) pre[q] = 0.f;
+    const int ip = i0 + tid % TW, jp = j0 + tid / TW;
+    if (tid < TH * TW && ip <= P.nx - 3 && jp <= P.ny - 3) {
+        const size_t c = cidx(P, 0, jp, ip);
+        if (STAGE == 1) {
+            pre[0] = P.nman[c];
+        } else {
+            pre[0] = P.A[c];
+            pre[1] = P.A[cidx(P, 1, jp, ip)];
+            pre[2] = P.A[cidx(P, 2, jp, ip)];
+        }
+        if (C.fl & F_INFIL) {
+            pre[3] = C.Fin[c];
+            pre[4] = P.K[c];
+            if (STAGE == 2) pre[5] = P.FA[c];
+        }
+    }
+}
+
+// Update of the interior cell of thread tid < 224 of a staged tile from its
+// divergence; returns its wet vote.
+template <int STAGE>
+__device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConsts& C,
+                                               const TileBuf& T, int tile, int i0, int j0, float dh,
+                                               float dhu, float dhv, const float (&pre)[6]) {
+    const int tid = threadIdx.x;
+    const int tx = tid % TW, ty = tid / TW;
+    const int i = i0 + tx, j = j0 + ty;
+    if (tid >= TH * TW || i > P.nx - 3 || j > P.ny - 3) return false;
+    const int r = ty + 2, c = tx + 2;
+    return cellUpdate<STAGE, true>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][r][c], T.in[1][r][c],
+                                   T.in[2][r][c], T.e[0][r][c], T.e[1][r][c], T.e[2][r][c],
+                                   T.e[3][r][c], pre);
+}
+
+// Tile flags (stage 2, or stage 1 in Euler mode) and stage-2 tile speeds.
+template <int STAGE>
+__device__ __forceinline__ void tileFlags(const Params& P, const StageConsts& C, StageSmem& S,
+                                          int tile, bool wetCell, float spx, float spy) {
+    if (STAGE == 2 || C.euler) {
+        bool any = __syncthreads_or(wetCell);
+        if (threadIdx.x == 0) P.wet[tile] = (uint8_t)((!(C.fl & F_TILE_ACC)) || any);
+    }
+    if (STAGE == 2) {
+        float mxv = blockMax(spx, S.red[0]);
+        float myv = blockMax(spy, S.red[1]);
+        if (threadIdx.x == 0) {
+            P.mx[tile] = mxv;
+            P.my[tile] = myv;
+        }
+    }
+}
+
 // STAGE 1: reads U^n (A) -> writes U* (B), F* (FB).
 // STAGE 2: reads U* (B) with halo and U^n (A) at the cell -> writes U^{n+1}
 //          (A), F^{n+1} (FA), outputs, tile wet flags and tile speeds.
@@ -622,251 +916,25 @@ __device__ __forceinline__ void writeGhosts(const Params& P, float* U, int j, in
 template <int STAGE>
 __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensorMap* tmE,
                            const Params& P, int nAct, uint32_t* ph) {
-    const DevState* st = P.st;
     const int tid = threadIdx.x;
     tileFirst(S, tmIn, tmE, P, nAct);
-    const float kappa = P.kappa;
-    const uint32_t fl = P.flags;
-    const bool euler = (fl & F_EULER) != 0;
-    const float dtNew = (float)st->dt;
-    // source clamps use the dt passed to ComputeFluxes: the previous dt in
-    // stage 1 (simulator.cu:786-792), the new one in stage 2
-    const float dtSrc = (STAGE == 1) ? (float)st->dt_old : dtNew;
-    const float invDtSrc = 1.f / dtSrc;
-    const double tNew = st->t;
-    const float rainU = st->rain_rate, drainU = st->drain_rate;
-    const float fac0 = st->factor[0], fac1 = st->factor[1], fac2 = st->factor[2];
-    float* Uout = (STAGE == 1) ? P.B : P.A;
-    const float* Fin = (STAGE == 1) ? P.FA : P.FB;
-    float* Fout = (STAGE == 1) ? P.FB : P.FA;
-
+    const StageConsts C = stageConsts<STAGE>(P);
     int bsel = 0;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];
         int bX, bY, i0, j0;
         tileOrigin(P, tile, bX, bY, i0, j0);
-        // the cell's own global inputs, loaded while the staged block is in
-        // flight: stage 1 Manning n, stage 2 U^n; F and K with infiltration
-        float pre0 = 0.f, pre1 = 0.f, pre2 = 0.f, preF = 0.f, preFA = 0.f, preK = 0.f;
-        {
-            const int ip = i0 + tid % TW, jp = j0 + tid / TW;
-            if (tid < TH * TW && ip <= P.nx - 3 && jp <= P.ny - 3) {
-                const size_t c = cidx(P, 0, jp, ip);
-                if (STAGE == 1) {
-                    pre0 = P.nman[c];
-                } else {
-                    pre0 = P.A[c];
-                    pre1 = P.A[cidx(P, 1, jp, ip)];
-                    pre2 = P.A[cidx(P, 2, jp, ip)];
-                }
-                if (fl & F_INFIL) {
-                    preF = Fin[c];
-                    preK = P.K[c];
-                    if (STAGE == 2) preFA = P.FA[c];
-                }
-            }
-        }
+        float pre[6];
+        tilePrefetch<STAGE>(P, C, i0, j0, pre);
         if (!tileAcquire(S, tmIn, tmE, P, bsel, ph, k + gridDim.x, nAct)) {
             if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
             return false;
         }
         const TileBuf& T = S.buf[bsel];
-        // ---- x reconstruction: cells i0-1 .. i0+16 on the 14 tile rows
-        if (tid < TH * (TW + 2)) {
-            int r = tid / (TW + 2), c = tid % (TW + 2);
-            int sr = r + 2, sc = c + 1;
-            Rec R = construct(T.in[0][sr][sc], T.in[1][sr][sc], T.in[2][sr][sc],
-                              T.in[0][sr][sc + 1], T.in[1][sr][sc + 1], T.in[2][sr][sc + 1],
-                              T.in[0][sr][sc - 1], T.in[1][sr][sc - 1], T.in[2][sr][sc - 1],
-                              T.e[0][sr][sc], T.e[1][sr][sc],
-                              T.e[1][sr][sc] - T.e[0][sr][sc + 1],
-                              T.e[1][sr][sc - 1] - T.e[0][sr][sc]);
-            S.rec.x.P[0][r][c] = R.hP;
-            S.rec.x.P[1][r][c] = R.uP;
-            S.rec.x.P[2][r][c] = R.vP;
-            S.rec.x.M[0][r][c] = R.hM;
-            S.rec.x.M[1][r][c] = R.uM;
-            S.rec.x.M[2][r][c] = R.vM;
-        }
-        __syncthreads();
-        // ---- x faces: face f between reconstructed cells f and f+1
-        float spx = 0.f, spy = 0.f;
-        if (tid < TH * (TW + 1)) {
-            int r = tid / (TW + 1), f = tid % (TW + 1);
-            float fx[3];
-            float sp = faceFlux<0>(S.rec.x.P[0][r][f], S.rec.x.P[1][r][f], S.rec.x.P[2][r][f],
-                                   S.rec.x.M[0][r][f + 1], S.rec.x.M[1][r][f + 1],
-                                   S.rec.x.M[2][r][f + 1], kappa, fx);
-            S.FX[0][r][f] = fx[0];
-            S.FX[1][r][f] = fx[1];
-            S.FX[2][r][f] = fx[2];
-            // face f is the east face of tile column f-1
-            if (STAGE == 2 && f >= 1 && i0 + f - 1 <= P.nx - 3 && j0 + r <= P.ny - 3) spx = sp;
-        }
-        __syncthreads();
-        const bool cellThread = tid < TH * TW;
-        const int tx = tid % TW, ty = tid / TW;
-        float dh = 0.f, dhu = 0.f, dhv = 0.f;
-        if (cellThread) {
-            dh = -(S.FX[0][ty][tx + 1] - S.FX[0][ty][tx]) * P.inv_dx;
-            dhu = -(S.FX[1][ty][tx + 1] - S.FX[1][ty][tx]) * P.inv_dx;
-            dhv = -(S.FX[2][ty][tx + 1] - S.FX[2][ty][tx]) * P.inv_dx;
-        }
-        // ---- y reconstruction: rows j0-1 .. j0+14 of the 16 tile columns
-        if (tid < (TH + 2) * TW) {
-            int r = tid / TW, c = tid % TW;
-            int sr = r + 1, sc = c + 2;
-            Rec R = construct(T.in[0][sr][sc], T.in[1][sr][sc], T.in[2][sr][sc],
-                              T.in[0][sr + 1][sc], T.in[1][sr + 1][sc], T.in[2][sr + 1][sc],
-                              T.in[0][sr - 1][sc], T.in[1][sr - 1][sc], T.in[2][sr - 1][sc],
-                              T.e[2][sr][sc], T.e[3][sr][sc],
-                              T.e[3][sr][sc] - T.e[2][sr + 1][sc],
-                              T.e[3][sr - 1][sc] - T.e[2][sr][sc]);
-            S.rec.y.P[0][r][c] = R.hP;
-            S.rec.y.P[1][r][c] = R.uP;
-            S.rec.y.P[2][r][c] = R.vP;
-            S.rec.y.M[0][r][c] = R.hM;
-            S.rec.y.M[1][r][c] = R.uM;
-            S.rec.y.M[2][r][c] = R.vM;
-        }
-        __syncthreads();
-        if (tid < (TH + 1) * TW) {
-            int r = tid / TW, c = tid % TW;
-            float fy[3];
-            float sp = faceFlux<1>(S.rec.y.P[0][r][c], S.rec.y.P[1][r][c], S.rec.y.P[2][r][c],
-                                   S.rec.y.M[0][r + 1][c], S.rec.y.M[1][r + 1][c],
-                                   S.rec.y.M[2][r + 1][c], kappa, fy);
-            S.FY[0][r][c] = fy[0];
-            S.FY[1][r][c] = fy[1];
-            S.FY[2][r][c] = fy[2];
-            if (STAGE == 2 && r >= 1 && i0 + c <= P.nx - 3 && j0 + r - 1 <= P.ny - 3) spy = sp;
-        }
-        __syncthreads();
-        bool wetCell = false;
-        if (cellThread) {
-            dh += -(S.FY[0][ty + 1][tx] - S.FY[0][ty][tx]) * P.inv_dy;
-            dhu += -(S.FY[1][ty + 1][tx] - S.FY[1][ty][tx]) * P.inv_dy;
-            dhv += -(S.FY[2][ty + 1][tx] - S.FY[2][ty][tx]) * P.inv_dy;
-            const int i = i0 + tx, j = j0 + ty;
-            if (i <= P.nx - 3 && j <= P.ny - 3) {
-                const size_t c = cidx(P, 0, j, i);
-                const float hC = T.in[0][ty + 2][tx + 2];
-                const float hu0 = T.in[1][ty + 2][tx + 2];
-                const float hv0 = T.in[2][ty + 2][tx + 2];
-                const float eW = T.e[0][ty + 2][tx + 2], eE = T.e[1][ty + 2][tx + 2];
-                const float eS = T.e[2][ty + 2][tx + 2], eN = T.e[3][ty + 2][tx + 2];
-                // bed-slope source, grid.cu:701,751-752
-                const float S1 = -kG * hC * ((eE - eW) * P.inv_dx);
-                const float S2 = -kG * hC * ((eN - eS) * P.inv_dy);
-                // mass sources, grid.cu:763-807
-                float S0 = 0.f;
-                if (fl & F_RAIN_U) S0 += rainU;
-                float rainG = 0.f;
-                if (fl & F_RAIN_G) {
-                    rainG = mapValue(P, 0, c, fac0);
-                    S0 += rainG;
-                }
-                const float cap = hC * invDtSrc;
-                if (fl & F_DRAIN_U) S0 -= (drainU > cap) ? cap : drainU;
-                if (fl & F_DRAIN_G) {
-                    float d = mapValue(P, 1, c, fac1);
-                    S0 -= (d > cap) ? cap : d;
-                }
-                bool srcCell = false;
-                if (P.nsrc > 0) {
-                    const int flat = j * P.nx + i;
-                    for (int q = P.srcTileStart[tile]; q < P.srcTileStart[tile + 1]; q++) {
-                        int sidx = P.srcTileList[q];
-                        if (P.srcIdx[sidx] == flat) {
-                            S0 += P.srcRate[sidx];
-                            srcCell = true;
-                        }
-                    }
-                }
-                float dF = 0.f, Fc = 0.f;
-                if (fl & F_INFIL) {
-                    Fc = preF;
-                    dF = greenAmpt(preK, Fc, P.psiDtheta, dtSrc, hC);
-                    S0 -= dF;
-                }
-                dh += S0;
-                dhu += S1;
-                dhv += S2;
-                const float hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
-                float hN, huN, hvN;
-                if (STAGE == 1) {
-                    // Integrate_1_k (grid.cu:856-922)
-                    const float G = manningG(pre0, hu0, hv0, hC, kappa);
-                    if (fl & F_SURGE) {
-                        float sg = mapValue(P, 2, c, fac2);
-                        if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
-                    }
-                    hN = hc + dh * dtNew;
-                    const float den = 1.f / (1.f - dtNew * G);
-                    huN = (hu0 + dhu * dtNew) * den;
-                    hvN = (hv0 + dhv * dtNew) * den;
-                    hN = (hN > kEps) ? hN : 0.f;
-                    if (fl & F_INFIL) Fout[c] = Fc + dF * dtNew;
-                    if (euler) {
-                        // Euler-mode outputs and wet flags (grid.cu:926-1023)
-                        const float uC = huN * velFactor(hN, kappa), vC = hvN * velFactor(hN, kappa);
-                        if (fl & F_SAVE_MAX) {
-                            float hm = P.hmax[c];
-                            if (hN > hm) P.tpeak[c] = (float)tNew;
-                            if (hN > 0.0762f) P.tdry[c] = (float)tNew;
-                            P.hmax[c] = fmaxf(hm, hN);
-                            P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
-                        }
-                        if (fl & F_SAVE_ARR) {
-                            if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)tNew;
-                        }
-                        wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && rainU > 0.f) ||
-                                  ((fl & F_RAIN_G) && rainG > 0.f);
-                        if (fl & F_SURGE) {
-                            float sg = mapValue(P, 2, c, fac2);
-                            if (sg != P.nodata && sg > 0.f) wetCell = true;
-                        }
-                    }
-                } else {
-                    // Integrate_2_k (grid.cu:1043-1171)
-                    const float hOld = pre0;
-                    const float hOc = (hOld > kEps) ? hOld : 0.f;
-                    hN = 0.5f * (hOc + hc + dh * dtNew);
-                    huN = 0.5f * (pre1 + hu0 + dhu * dtNew);
-                    hvN = 0.5f * (pre2 + hv0 + dhv * dtNew);
-                    hN = (hN > kEps) ? hN : 0.f;
-                    if (fl & F_INFIL) Fout[c] = 0.5f * (preFA + Fc + dF * dtNew);
-                    if (fl & F_SAVE_MAX) {
-                        const float uC = huN * velFactor(hN, kappa);
-                        const float vC = hvN * velFactor(hN, kappa);
-                        P.hmax[c] = fmaxf(P.hmax[c], hN);
-                        P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
-                    }
-                    if (fl & F_SAVE_ARR) {
-                        if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)tNew;
-                    }
-                    wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && rainU > 0.f) ||
-                              ((fl & F_RAIN_G) && rainG > 0.f);
-                }
-                Uout[cidx(P, 0, j, i)] = hN;
-                Uout[cidx(P, 1, j, i)] = huN;
-                Uout[cidx(P, 2, j, i)] = hvN;
-                writeGhosts(P, Uout, j, i, hN, huN, hvN);
-            }
-        }
-        // ---- tile flags and speeds
-        if (STAGE == 2 || euler) {
-            bool any = __syncthreads_or(wetCell);
-            if (tid == 0) P.wet[tile] = (uint8_t)((!(fl & F_TILE_ACC)) || any);
-        }
-        if (STAGE == 2) {
-            float mxv = blockMax(spx, S.red[0]);
-            float myv = blockMax(spy, S.red[1]);
-            if (tid == 0) {
-                P.mx[tile] = mxv;
-                P.my[tile] = myv;
-            }
-        }
+        float dh, dhu, dhv, spx, spy;
+        tileFluxDiv<STAGE == 2>(S, T, P, i0, j0, dh, dhu, dhv, spx, spy);
+        const bool wetCell = tileCellUpdate<STAGE>(P, C, T, tile, i0, j0, dh, dhu, dhv, pre);
+        tileFlags<STAGE>(P, C, S, tile, wetCell, spx, spy);
         __syncthreads();
     }
     return true;

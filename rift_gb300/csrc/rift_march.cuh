@@ -92,155 +92,6 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
         mbar_wait_bounded(&S.bar[k % MNSLOT], (par >> (k % MNSLOT)) & 1u);
 }
 
-// Step-wide constants of a stage kernel.
-struct StageConsts {
-    float kappa, dtNew, dtSrc, invDtSrc, rainU, drainU, fac0, fac1, fac2;
-    double tNew;
-    uint32_t fl;
-    bool euler;
-    float* Uout;
-    const float* Fin;
-    float* Fout;
-};
-
-template <int STAGE>
-__device__ __forceinline__ StageConsts stageConsts(const Params& P) {
-    const DevState* st = P.st;
-    StageConsts C;
-    C.kappa = P.kappa;
-    C.fl = P.flags;
-    C.euler = (P.flags & F_EULER) != 0;
-    C.dtNew = (float)st->dt;
-    // source clamps use the dt passed to ComputeFluxes: the previous dt in
-    // stage 1 (simulator.cu:786-792), the new one in stage 2
-    C.dtSrc = (STAGE == 1) ? (float)st->dt_old : C.dtNew;
-    C.invDtSrc = 1.f / C.dtSrc;
-    C.tNew = st->t;
-    C.rainU = st->rain_rate;
-    C.drainU = st->drain_rate;
-    C.fac0 = st->factor[0];
-    C.fac1 = st->factor[1];
-    C.fac2 = st->factor[2];
-    C.Uout = (STAGE == 1) ? P.B : P.A;
-    C.Fin = (STAGE == 1) ? P.FA : P.FB;
-    C.Fout = (STAGE == 1) ? P.FB : P.FA;
-    return C;
-}
-
-// Sources, friction, the RK stage, outputs and ghost cells of interior cell
-// (j, i) of `tile`, given its flux divergence (dh, dhu, dhv) and its staged
-// state and face offsets.  Returns the cell's vote for the tile wet flag.
-// pre: centre values loaded one row ahead -- stage 1: Manning n; stage 2:
-// U^n (h, hu, hv) of the cell.
-template <int STAGE>
-__device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
-                                           int i, float dh, float dhu, float dhv, float hC,
-                                           float hu0, float hv0, float eW, float eE, float eS,
-                                           float eN, const float* pre) {
-    const uint32_t fl = C.fl;
-    const size_t c = cidx(P, 0, j, i);
-    // bed-slope source, grid.cu:701,751-752
-    const float S1 = -kG * hC * ((eE - eW) * P.inv_dx);
-    const float S2 = -kG * hC * ((eN - eS) * P.inv_dy);
-    // mass sources, grid.cu:763-807
-    float S0 = 0.f;
-    if (fl & F_RAIN_U) S0 += C.rainU;
-    float rainG = 0.f;
-    if (fl & F_RAIN_G) {
-        rainG = mapValue(P, 0, c, C.fac0);
-        S0 += rainG;
-    }
-    const float cap = hC * C.invDtSrc;
-    if (fl & F_DRAIN_U) S0 -= (C.drainU > cap) ? cap : C.drainU;
-    if (fl & F_DRAIN_G) {
-        float d = mapValue(P, 1, c, C.fac1);
-        S0 -= (d > cap) ? cap : d;
-    }
-    bool srcCell = false;
-    if (P.nsrc > 0) {
-        const int flat = j * P.nx + i;
-        for (int q = P.srcTileStart[tile]; q < P.srcTileStart[tile + 1]; q++) {
-            int sidx = P.srcTileList[q];
-            if (P.srcIdx[sidx] == flat) {
-                S0 += P.srcRate[sidx];
-                srcCell = true;
-            }
-        }
-    }
-    float dF = 0.f, Fc = 0.f;
-    if (fl & F_INFIL) {
-        Fc = C.Fin[c];
-        dF = greenAmpt(P.K[c], Fc, P.psiDtheta, C.dtSrc, hC);
-        S0 -= dF;
-    }
-    dh += S0;
-    dhu += S1;
-    dhv += S2;
-    const float hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
-    const float dtNew = C.dtNew;
-    float hN, huN, hvN;
-    bool wetCell = false;
-    if (STAGE == 1) {
-        // Integrate_1_k (grid.cu:856-922)
-        const float G = manningG(pre[0], hu0, hv0, hC, C.kappa);
-        if (fl & F_SURGE) {
-            float sg = mapValue(P, 2, c, C.fac2);
-            if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
-        }
-        hN = hc + dh * dtNew;
-        const float den = 1.f / (1.f - dtNew * G);
-        huN = (hu0 + dhu * dtNew) * den;
-        hvN = (hv0 + dhv * dtNew) * den;
-        hN = (hN > kEps) ? hN : 0.f;
-        if (fl & F_INFIL) C.Fout[c] = Fc + dF * dtNew;
-        if (C.euler) {
-            // Euler-mode outputs and wet flags (grid.cu:926-1023)
-            const float uC = huN * velFactor(hN, C.kappa), vC = hvN * velFactor(hN, C.kappa);
-            if (fl & F_SAVE_MAX) {
-                float hm = P.hmax[c];
-                if (hN > hm) P.tpeak[c] = (float)C.tNew;
-                if (hN > 0.0762f) P.tdry[c] = (float)C.tNew;
-                P.hmax[c] = fmaxf(hm, hN);
-                P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
-            }
-            if (fl & F_SAVE_ARR) {
-                if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)C.tNew;
-            }
-            wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
-                      ((fl & F_RAIN_G) && rainG > 0.f);
-            if (fl & F_SURGE) {
-                float sg = mapValue(P, 2, c, C.fac2);
-                if (sg != P.nodata && sg > 0.f) wetCell = true;
-            }
-        }
-    } else {
-        // Integrate_2_k (grid.cu:1043-1171)
-        const float hOld = pre[0];
-        const float hOc = (hOld > kEps) ? hOld : 0.f;
-        hN = 0.5f * (hOc + hc + dh * dtNew);
-        huN = 0.5f * (pre[1] + hu0 + dhu * dtNew);
-        hvN = 0.5f * (pre[2] + hv0 + dhv * dtNew);
-        hN = (hN > kEps) ? hN : 0.f;
-        if (fl & F_INFIL) C.Fout[c] = 0.5f * (P.FA[c] + Fc + dF * dtNew);
-        if (fl & F_SAVE_MAX) {
-            const float uC = huN * velFactor(hN, C.kappa);
-            const float vC = hvN * velFactor(hN, C.kappa);
-            P.hmax[c] = fmaxf(P.hmax[c], hN);
-            P.qmax[c] = fmaxf(P.qmax[c], hN * sqrtf(vC * vC + uC * uC));
-        }
-        if (fl & F_SAVE_ARR) {
-            if (P.twet[c] < 0.f && hN > kEps) P.twet[c] = (float)C.tNew;
-        }
-        wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
-                  ((fl & F_RAIN_G) && rainG > 0.f);
-    }
-    C.Uout[cidx(P, 0, j, i)] = hN;
-    C.Uout[cidx(P, 1, j, i)] = huN;
-    C.Uout[cidx(P, 2, j, i)] = hvN;
-    writeGhosts(P, C.Uout, j, i, hN, huN, hvN);
-    return wetCell;
-}
-
 // STAGE 0: reads U^n (A) -> tile speed maxima, dt and t (the speed output of
 //          the first ComputeFluxes and ComputeTimestep), re-sync of U* on
 //          tiles that went inactive.

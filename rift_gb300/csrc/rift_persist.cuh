@@ -9,6 +9,9 @@
 //   grow B   each CTA writes its chunk of the lists (rift_grow.cuh)
 //   speed    tile speeds of U^n, dt and t (last CTA), U* re-sync
 //   stage 1  RK stage 1 (per-tile code of k_stage<1>)
+// With at most one active tile per CTA, the speed and stage-1 phases become
+// one flux phase (its fluxes give the speeds) and an update after the dt
+// barrier, so a step has one tile-flux phase fewer.
 //   stage 2  RK stage 2, or the Euler commit
 // The phases run the same device functions as the per-tile kernels, so the
 // results are identical.  The kernel leaves at a step boundary when
@@ -112,16 +115,60 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
         const int nAct = growWrite(P, G);
         nActPrev = nAct;
         RIFT_SYNC();
-        // speeds of U^n, dt, t, U* re-sync (k_speed_dt)
         float amx = 0.f, amy = 0.f, tmx = 0.f, tmy = 0.f;
-        staleMax(P, amx, amy);
-        if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
-        __syncthreads();
-        finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
-        resyncDeactivated(P);
-        RIFT_SYNC();
-        if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph)) return;
-        RIFT_SYNC();
+        if (nAct <= (int)gridDim.x) {
+            // At most one tile per CTA: stage 1's fluxes of U^n are the first
+            // ComputeFluxes of the step, so they give this step's tile speeds,
+            // and the tile's divergence waits in registers (its staged block
+            // in shared memory) across the dt barrier.
+            const bool mine = (int)blockIdx.x < nAct;
+            int tile = 0, bX, bY, i0 = 0, j0 = 0;
+            float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f;
+            if (mine) {
+                tile = P.act[blockIdx.x];
+                tileOrigin(P, tile, bX, bY, i0, j0);
+                tilePrefetch<1>(P, stageConsts<1>(P), i0, j0, pre);
+            }
+            tileFirst(S, &tmA, &tmE, P, nAct);
+            if (mine) {
+                if (!tileAcquire(S, &tmA, &tmE, P, 0, ph, nAct, nAct)) {
+                    if (tid == 0) atomicOr(&st->error, ERR_TMA_TIMEOUT);
+                    return;
+                }
+                tileFluxDiv<true>(S, S.buf[0], P, i0, j0, dh, dhu, dhv, spx, spy);
+                const float mxv = blockMax(spx, S.red[0]);
+                const float myv = blockMax(spy, S.red[1]);
+                if (tid == 0) {
+                    P.mx[tile] = mxv;
+                    P.my[tile] = myv;
+                    tmx = mxv;
+                    tmy = myv;
+                }
+                __syncthreads();
+            }
+            staleMax(P, amx, amy);
+            finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
+            resyncDeactivated(P);
+            RIFT_SYNC();
+            if (mine) {  // stage-1 update with this step's dt (Integrate_1_k)
+                const StageConsts C1 = stageConsts<1>(P);
+                const bool wetCell =
+                    tileCellUpdate<1>(P, C1, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
+                tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
+                __syncthreads();
+            }
+            RIFT_SYNC();
+        } else {
+            // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1
+            staleMax(P, amx, amy);
+            if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
+            __syncthreads();
+            finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
+            resyncDeactivated(P);
+            RIFT_SYNC();
+            if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph)) return;
+            RIFT_SYNC();
+        }
         if (!(fl & F_EULER)) {
             if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph)) return;
         } else {
