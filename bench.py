@@ -1,6 +1,6 @@
 """Benchmark of the GB300 RIFT step (one JSON line on stdout).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3|5]
                     [--impl ours|reference]
 
 A step is one full RK2 time step (both stages, Grow, dt) of the whole domain
@@ -9,11 +9,15 @@ seeded synthetic configs of rift_gb300.synth (no datasets are involved):
   1: 512^2 bumpy plane, uniform rain           (the reference's small case)
   2: 2048^2 fractal + channel, point-source hydrograph, Green-Ampt (default)
   3: 8192^2 urban fractal with buildings, uniform drain, interpolated rain maps
+  5: a batched ensemble (--members, --side-min/--side-max, --tf) run to tf in
+     one persistent kernel; metric members/hour, per-member p50/p99, and the
+     same members run one after another for comparison
 The state is spun up (untimed) to --spinup seconds of simulated time so the
 timed steps see a developed flood, then W warm-up and K timed steps run.
 
 value  = domain cell-updates/s = interior cells x K / device time (CUDA
-         events on the engine's stream around the K graph launches);
+         events on the engine's stream around the K steps: one persistent
+         launch, or K step-graph launches);
 e2e    = the same metric through the C ABI with host buffers: static fields
          uploaded from host arrays, K rift_step calls (each returns t and dt
          to the host), the depth map read back, all inside the timed region;
@@ -290,10 +294,10 @@ def run_ours(args, device=0, sync=None):
 
 def launches_per_step(flags):
     """Kernels one step's graph launches: k_track (gridded rain or surge),
-    the two grow passes, the speed/dt kernel and the stage kernels of both
-    schedules (the schedule not chosen for the step exits at entry), k_commit
-    in Euler mode."""
-    n = 2 + 2 + 2 + (1 if flags & synth.EULER else 2)
+    k_grow, the speed/dt kernel and the stage kernels of both schedules (the
+    schedule not chosen for the step exits at entry), k_commit in Euler
+    mode."""
+    n = 1 + 2 + 2 + (1 if flags & synth.EULER else 2)
     if flags & (synth.RAIN_GRID | synth.SURGE_GRID):
         n += 1
     return n
@@ -380,12 +384,70 @@ def run_reference(args):
     return line
 
 
+def run_ensemble(args):
+    """Config 5: a batched ensemble run to tf in one persistent kernel
+    (rift_ensemble_run), timed on the host around the synchronous call, then
+    the same members run one after another for comparison."""
+    cases = synth.config5(members=args.members, side=(args.side_min, args.side_max), tf=args.tf)
+
+    def setup():
+        return [capi.Sim(c).setup() for c in cases]
+
+    members = setup()
+    ens = capi.Ensemble(members)
+    ens.run(max_steps=args.warmup)  # warm-up steps (counted in t, not timed)
+    clocks = ClockSampler().start()
+    t0 = time.perf_counter()
+    t_end, k = ens.run(t_stop=args.tf)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    ens.close()
+    cells = np.array([(c.h_nx - 4) * (c.h_ny - 4) for c in cases], dtype=float)
+    iters = int(k.max())
+    # member m finishes at iteration k_m of the shared loop
+    per_member = wall * k / max(iters, 1)
+    for s in members:
+        s.close()
+    seq = 0.0
+    if args.sequential:
+        solo = setup()
+        for s in solo:
+            s.run(args.warmup)
+        for s in solo:
+            ts = time.perf_counter()
+            s.run(2 ** 31 - 1, args.tf)
+            seq += time.perf_counter() - ts
+            s.close()
+    line = {"metric": "members/hour", "value": len(cases) / wall * 3600.0, "unit": "members/hour",
+            "n_gpus": 1, "steps": iters, "warmup": args.warmup, "ms_per_step": wall / iters * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "config5", "members": len(cases),
+                       "side_cells": [args.side_min, args.side_max], "tf_s": args.tf,
+                       "total_cells": int(cells.sum()), "iterations": iters,
+                       "member_steps_min_max": [int(k.min()), int(k.max())]},
+            "per_member_s": {"p50": float(np.percentile(per_member, 50)),
+                             "p99": float(np.percentile(per_member, 99))},
+            "domain_cell_updates_per_s": float((cells * k).sum() / wall),
+            "clocks": clk, "gpu_launches": 2}
+    if args.sequential:
+        line["sequential_s"] = seq
+        line["ensemble_speedup_vs_sequential"] = seq / wall
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3))
+    ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3, 5))
+    ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")
+    ap.add_argument("--side-min", type=int, default=128, help="config 5: smallest side (cells)")
+    ap.add_argument("--side-max", type=int, default=512, help="config 5: largest side (cells)")
+    ap.add_argument("--tf", type=float, default=3600.0, help="config 5: end time (s)")
+    ap.add_argument("--no-sequential", dest="sequential", action="store_false",
+                    help="config 5: skip the one-after-another comparison")
     ap.add_argument("--N", type=int, default=None, help="override the grid size (cells per side)")
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--spinup", type=float, default=None)
@@ -399,6 +461,10 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.config == 5 and args.impl != "reference":
+        if rank == 0:
+            print(json.dumps(run_ensemble(args)))
+        return
     if args.impl == "reference":
         if rank != 0:
             return

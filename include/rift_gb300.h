@@ -127,8 +127,10 @@ int rift_set_map_times(rift_handle* h, int32_t which, double t0, double t1);
  * ApplyBoundaries.  Returns the new t and dt. */
 int rift_step(rift_handle* h, double* t, double* dt);
 
-/* Run nsteps steps on device without a host round trip (CUDA graph replay).
- * Uniform rates / maps stay as last set.  Stops early once t >= t_stop. */
+/* Run nsteps steps on device without a host round trip per step: one
+ * persistent cooperative launch while few tiles are active, else per-step
+ * CUDA graph replays.  Uniform rates / maps stay as last set.  Stops early
+ * once t >= t_stop. */
 int rift_run(rift_handle* h, int32_t nsteps, double t_stop, double* t,
              double* dt, int32_t* steps_done);
 
@@ -203,6 +205,22 @@ int rift_set_schedule(rift_handle* h, int32_t march_min_strips);
  * default (the march threshold in tiles), 0 turns it off.
  * RIFT_ERR_UNSUPPORTED when the device has no cooperative launch. */
 int rift_set_persistent(rift_handle* h, int32_t max_active_tiles);
+
+/* Ensembles (no reference counterpart; the reference runs one scenario per
+ * process): members -- handles created, uploaded and initialised as usual,
+ * on one device, of any sizes and options -- advance together in one
+ * persistent cooperative kernel that walks device queues of (member, tile)
+ * work items; each member keeps its own dt, t, sources and outputs, and its
+ * results are those of a run of its own.  rift_ensemble_run advances each
+ * member until t >= t_stop or max_steps of its steps; t_out and steps_out
+ * (n entries each, may be NULL) receive each member's final t and steps.
+ * The members must not be stepped elsewhere while an ensemble runs them. */
+typedef struct rift_ensemble rift_ensemble;
+int rift_ensemble_create(rift_handle* const* members, int32_t n, rift_ensemble** out);
+int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double* t_out,
+                      int32_t* steps_out);
+const char* rift_ensemble_last_error(rift_ensemble* e);
+void rift_ensemble_destroy(rift_ensemble* e);
 
 /* Steps run so far by the persistent launch and by the per-step graph. */
 int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_steps);

@@ -73,6 +73,13 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                [_P, C.c_int32, C.c_double, C.c_double])
     if hasattr(lib, p + "set_schedule"):
         ns["set_schedule"] = _sig(lib, p + "set_schedule", C.c_int, [_P, C.c_int32])
+    if hasattr(lib, p + "ensemble_create"):
+        ns["ensemble_create"] = _sig(lib, p + "ensemble_create", C.c_int,
+                                     [C.POINTER(_P), C.c_int32, C.POINTER(_P)])
+        ns["ensemble_run"] = _sig(lib, p + "ensemble_run", C.c_int,
+                                  [_P, C.c_double, C.c_int32, _D, C.POINTER(C.c_int32)])
+        ns["ensemble_last_error"] = _sig(lib, p + "ensemble_last_error", C.c_char_p, [_P])
+        ns["ensemble_destroy"] = _sig(lib, p + "ensemble_destroy", None, [_P])
     if hasattr(lib, p + "set_persistent"):
         ns["set_persistent"] = _sig(lib, p + "set_persistent", C.c_int, [_P, C.c_int32])
         ns["get_path_stats"] = _sig(lib, p + "get_path_stats", C.c_int,
@@ -310,3 +317,41 @@ class Sim:
     def load_snapshot(self, s):
         self.set_state(s["t"], s["dt"], s["w"], s["hu"], s["hv"], s.get("F"), s["wet"],
                        s["active"], s["mx"], s["my"])
+
+
+class Ensemble:
+    """Members (Sim objects of one engine library) stepped together by one
+    persistent kernel; each keeps its own dt and results."""
+
+    def __init__(self, sims):
+        self.sims = list(sims)
+        self.f = self.sims[0].f
+        arr = (_P * len(self.sims))(*[s.h for s in self.sims])
+        self.h = _P()
+        rc = self.f["ensemble_create"](arr, len(self.sims), C.byref(self.h))
+        if rc != RIFT_OK:
+            msg = self.f["ensemble_last_error"](self.h) if self.h else b""
+            raise RiftError(f"ensemble_create failed: {ERRORS.get(rc, rc)} "
+                            f"{(msg or b'').decode()}")
+
+    def run(self, t_stop=float("inf"), max_steps=2**31 - 1):
+        n = len(self.sims)
+        t = np.zeros(n)
+        k = np.zeros(n, dtype=np.int32)
+        rc = self.f["ensemble_run"](self.h, t_stop, max_steps, _dp(t),
+                                    k.ctypes.data_as(C.POINTER(C.c_int32)))
+        if rc != RIFT_OK:
+            raise RiftError(f"ensemble_run failed: {ERRORS.get(rc, rc)} "
+                            f"{self.f['ensemble_last_error'](self.h).decode()}")
+        return t, k
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.f["ensemble_destroy"](self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -28,6 +28,7 @@
 #include "rift_kernels.cuh"
 #include "rift_march.cuh"
 #include "rift_persist.cuh"
+#include "rift_ensemble.cuh"
 
 using namespace rift;
 
@@ -59,12 +60,10 @@ struct rift_handle {
     int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0, gridMarch = 0;
     int nSX = 0, nSY = 0;
     int marchMin = 0;  // active strips from which the march kernels run
-    int gridGrow = 0;      // CTAs of the two grow passes of the graph path
+    int gridGrow = 0;      // CTAs of the grow kernel of the graph path
     int gridPersist = 0;   // CTAs of the cooperative step kernel (0: unavailable)
     int persistMax = 0;    // it runs while the active tiles are at most this many
     GridBar* gbar = nullptr;
-    int* growCnt = nullptr;
-    unsigned long long* growCells = nullptr;
     long long persistSteps = 0, graphSteps = 0;  // steps run by each path (diagnostics)
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
@@ -163,8 +162,6 @@ Params makeParams(rift_handle* h) {
     P.marchMin = h->marchMin;
     P.persistMax = h->persistMax;
     P.gbar = h->gbar;
-    P.growCnt = h->growCnt;
-    P.growCells = h->growCells;
     P.mx = h->mx;
     P.my = h->my;
     P.srcIdx = h->srcIdx;
@@ -207,8 +204,7 @@ void enqueueStep(rift_handle* h) {
     cudaStream_t s = h->stream;
     if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
         k_track<<<h->gridTrack, NT, 0, s>>>(P);
-    k_grow_a<<<h->gridGrow, NT, 0, s>>>(P);
-    k_grow_b<<<h->gridGrow, NT, 0, s>>>(P);
+    k_grow<<<h->gridGrow, NT, 0, s>>>(P);
     // per-tile and march variants of each pass; the device keeps one of them
     // (useMarch) and the other returns at once
     k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
@@ -472,9 +468,6 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
         CUDA_TRY(h, cudaMalloc(&h->gbar, sizeof(GridBar)));
     }
     h->gridGrow = std::max(1, std::min(NS, h->numSMs * 4));
-    const int growCTAs = std::max(h->gridGrow, h->gridPersist);
-    CUDA_TRY(h, cudaMalloc(&h->growCnt, (size_t)growCTAs * GROW_LISTS * sizeof(int)));
-    CUDA_TRY(h, cudaMalloc(&h->growCells, (size_t)growCTAs * sizeof(unsigned long long)));
     h->persistMax = h->gridPersist > 0 ? h->marchMin * STRIP_TX * STRIP_TY : 0;
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return RIFT_OK;
@@ -1071,8 +1064,7 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     for (int k = 0; k < M; k++) {
         if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
             k_track<<<h->gridTrack, NT, 0, s>>>(P);
-        k_grow_a<<<h->gridGrow, NT, 0, s>>>(P);
-        k_grow_b<<<h->gridGrow, NT, 0, s>>>(P);
+        k_grow<<<h->gridGrow, NT, 0, s>>>(P);
         k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
         k_march<0><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
         CUDA_TRY(h, cudaEventRecord(e0, s));
@@ -1107,6 +1099,121 @@ int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_s
     return RIFT_OK;
 }
 
+// ---------------------------------------------------------------- ensembles
+struct rift_ensemble {
+    std::vector<rift_handle*> m;
+    cudaStream_t stream = nullptr;
+    Params* dP = nullptr;
+    CUtensorMap* dMaps = nullptr;
+    EnsDev* dE = nullptr;
+    int grid = 0;
+    long long steps = 0;
+    std::string err;
+};
+
+namespace {
+int efail(rift_ensemble* e, int code, const std::string& msg) {
+    if (e) e->err = msg;
+    return code;
+}
+#define ENS_TRY(e, call)                                                                        \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return efail(e, e_ == cudaErrorMemoryAllocation ? RIFT_ERR_NOMEM : RIFT_ERR_CUDA,   \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+    } while (0)
+}  // namespace
+
+int rift_ensemble_create(rift_handle* const* members, int32_t n, rift_ensemble** out) {
+    if (!members || !out || n < 1 || n > ENS_MAX) return RIFT_ERR_ARG;
+    *out = nullptr;
+    for (int k = 0; k < n; k++) {
+        if (!members[k]) return RIFT_ERR_ARG;
+        if (!members[k]->inited) return RIFT_ERR_STATE;
+        if (members[k]->g.device != members[0]->g.device) return RIFT_ERR_ARG;
+        for (int q = 0; q < k; q++)
+            if (members[q] == members[k]) return RIFT_ERR_ARG;
+    }
+    rift_ensemble* e = new rift_ensemble();
+    e->m.assign(members, members + n);
+    *out = e;
+    ENS_TRY(e, cudaSetDevice(members[0]->g.device));
+    int coop = 0, sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, members[0]->g.device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, members[0]->g.device);
+    ENS_TRY(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_ensemble, NT, 0));
+    if (!coop || occ < 1) return efail(e, RIFT_ERR_UNSUPPORTED, "no cooperative launch");
+    e->grid = sms * occ;
+    ENS_TRY(e, cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    ENS_TRY(e, cudaMalloc(&e->dP, sizeof(Params) * n));
+    ENS_TRY(e, cudaMalloc(&e->dMaps, sizeof(CUtensorMap) * 3 * n));
+    ENS_TRY(e, cudaMalloc(&e->dE, sizeof(EnsDev)));
+    return RIFT_OK;
+}
+
+int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double* t_out,
+                      int32_t* steps_out) {
+    if (!e || max_steps < 0) return RIFT_ERR_ARG;
+    const int n = (int)e->m.size();
+    std::vector<Params> P(n);
+    std::vector<CUtensorMap> maps(3 * (size_t)n);
+    std::vector<int> live(n, 0);
+    int nAlive = 0;
+    for (int k = 0; k < n; k++) {
+        rift_handle* h = e->m[k];
+        ENS_TRY(e, cudaStreamSynchronize(h->stream));
+        // every entry point leaves the pinned mirror equal to the device state
+        h->hst->t_stop = t_stop;
+        h->hst->steps_done = 0;
+        ENS_TRY(e, cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, e->stream));
+        P[k] = makeParams(h);
+        maps[3 * k] = h->tmA;
+        maps[3 * k + 1] = h->tmB;
+        maps[3 * k + 2] = h->tmE;
+        live[k] = (h->hst->t < t_stop && max_steps > 0) ? 1 : 0;
+        nAlive += live[k];
+    }
+    ENS_TRY(e, cudaMemcpyAsync(e->dP, P.data(), sizeof(Params) * n, cudaMemcpyHostToDevice, e->stream));
+    ENS_TRY(e, cudaMemcpyAsync(e->dMaps, maps.data(), sizeof(CUtensorMap) * 3 * n,
+                               cudaMemcpyHostToDevice, e->stream));
+    ENS_TRY(e, cudaMemsetAsync(e->dE, 0, sizeof(EnsDev), e->stream));
+    ENS_TRY(e, cudaMemcpyAsync(e->dE->live[0], live.data(), sizeof(int) * n, cudaMemcpyHostToDevice,
+                               e->stream));
+    ENS_TRY(e, cudaMemcpyAsync(&e->dE->nAlive[0], &nAlive, sizeof(int), cudaMemcpyHostToDevice,
+                               e->stream));
+    EnsArgs A{e->dP, e->dMaps, e->dE, n, max_steps};
+    void* args[] = {(void*)&A};
+    ENS_TRY(e, cudaLaunchCooperativeKernel((const void*)k_ensemble, dim3(e->grid), dim3(NT), args, 0,
+                                           e->stream));
+    ENS_TRY(e, cudaStreamSynchronize(e->stream));
+    int rc = RIFT_OK;
+    for (int k = 0; k < n; k++) {
+        rift_handle* h = e->m[k];
+        int r = pullState(h);
+        if (r && !rc) {
+            rc = r;
+            e->err = "member " + std::to_string(k) + ": " + h->err;
+        }
+        if (t_out) t_out[k] = h->hst->t;
+        if (steps_out) steps_out[k] = h->hst->steps_done;
+        e->steps += h->hst->steps_done;
+    }
+    return rc;
+}
+
+const char* rift_ensemble_last_error(rift_ensemble* e) { return e ? e->err.c_str() : "null ensemble"; }
+
+void rift_ensemble_destroy(rift_ensemble* e) {
+    if (!e) return;
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    if (e->dP) cudaFree(e->dP);
+    if (e->dMaps) cudaFree(e->dMaps);
+    if (e->dE) cudaFree(e->dE);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
 const char* rift_last_error(rift_handle* h) { return h ? h->err.c_str() : "null handle"; }
 
 void rift_destroy(rift_handle* h) {
@@ -1119,7 +1226,7 @@ void rift_destroy(rift_handle* h) {
     for (int k = 0; k < 3; k++)
         for (int q = 0; q < 2; q++)
             if (h->maps[k][q]) cudaFree(h->maps[k][q]);
-    for (void* p : {(void*)h->gbar, (void*)h->growCnt, (void*)h->growCells,
+    for (void* p : {(void*)h->gbar,
                     (void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
                     (void*)h->act, (void*)h->deact,
                     (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,

@@ -11,10 +11,10 @@
 // and writes mx = my = 0) get their zero speeds here and are not scheduled.
 //
 // Each CTA owns a contiguous chunk of strips, 16 threads per strip (lanes
-// 0..13 hold its tiles).  Pass A counts the chunk's entries per list; pass B
-// takes its offsets from the counts of the CTAs before it and writes its
-// entries with warp ballots and one block scan per 16 strips.  The lists
-// are not in ascending tile order (consumers only need the sets).
+// 0..13 hold its tiles); entries are appended with one atomic per warp and
+// list, and the last CTA publishes the counts.  The lists are not in
+// ascending tile order: consumers need only the sets, and no result depends
+// on the order (speed maxima are order-free, no float sum crosses tiles).
 #pragma once
 #include "rift_kernels.cuh"
 
@@ -22,14 +22,6 @@ namespace rift {
 
 constexpr int GROW_LISTS = 4;            // scheduled active, deactivated, inactive, strips
 constexpr int STRIPS_PER_ROUND = NT / 16;
-
-struct GrowSmem {
-    int wsum[GROW_LISTS][NT / 32 + 1];
-    int red[GROW_LISTS][NT / 32];
-    unsigned long long cred[NT / 32];
-    int base[GROW_LISTS], total[GROW_LISTS];
-    unsigned long long cells;
-};
 
 // active(t) of tile b: wet itself or a wet 4-neighbour; tile 0 always.
 __device__ __forceinline__ bool tileGrows(const Params& P, int b) {
@@ -91,110 +83,28 @@ __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) 
     return t;
 }
 
-// Block reduction of per-thread list counts (and cells) into thread 0.
-__device__ __forceinline__ void growReduce(GrowSmem& G, int (&c)[GROW_LISTS],
-                                           unsigned long long& cells) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 16; o > 0; o >>= 1) {
-        for (int q = 0; q < GROW_LISTS; q++) c[q] += __shfl_xor_sync(0xffffffffu, c[q], o);
-        cells += __shfl_xor_sync(0xffffffffu, cells, o);
-    }
-    if (lane == 0) {
-        for (int q = 0; q < GROW_LISTS; q++) G.red[q][w] = c[q];
-        G.cred[w] = cells;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < GROW_LISTS; q++) {
-            int x = 0;
-            for (int k = 0; k < NT / 32; k++) x += G.red[q][k];
-            c[q] = x;
-        }
-        unsigned long long cs = 0ull;
-        for (int k = 0; k < NT / 32; k++) cs += G.cred[k];
-        cells = cs;
-    }
-}
-
-// Pass A: the chunk's list counts and cells, published per CTA.
-__device__ void growCount(const Params& P, GrowSmem& G) {
+// One pass: each CTA's chunk of strips appends its entries to the four lists
+// with one atomic per warp and list (the lists are sets: their order changes
+// no result), writes the new active flags, and the last CTA to finish
+// publishes the list sizes and clears the counters for the next step.
+__device__ void growAppend(const Params& P) {
+    DevState* s = P.st;
+    const int tid = threadIdx.x, lane = tid & 31;
     int s0, s1;
     stripChunk(P, s0, s1);
-    int c[GROW_LISTS] = {0, 0, 0, 0};
+    int* const lists[GROW_LISTS] = {P.act, P.deact, P.inact, P.strips};
     unsigned long long cells = 0ull;
-    for (int base = s0; base < s1; base += STRIPS_PER_ROUND) {
-        const GrowItem t = growItem(P, base, s1);
-        for (int q = 0; q < GROW_LISTS; q++) c[q] += t.f[q];
-        if (t.f[0]) cells += (unsigned long long)t.cells;
-    }
-    growReduce(G, c, cells);
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < GROW_LISTS; q++) P.growCnt[blockIdx.x * GROW_LISTS + q] = c[q];
-        P.growCells[blockIdx.x] = cells;
-    }
-}
-
-// Pass B: offsets from the counts of the CTAs before this one, then the
-// chunk's entries and the new active flags.  Returns the number of
-// scheduled active tiles (all threads); CTA 0 publishes the list sizes.
-__device__ int growWrite(const Params& P, GrowSmem& G) {
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    int pre[GROW_LISTS] = {0, 0, 0, 0}, tot[GROW_LISTS] = {0, 0, 0, 0};
-    unsigned long long cells = 0ull, none = 0ull;
-    for (int k = tid; k < (int)gridDim.x; k += NT) {
-        for (int q = 0; q < GROW_LISTS; q++) {
-            const int v = P.growCnt[k * GROW_LISTS + q];
-            tot[q] += v;
-            if (k < (int)blockIdx.x) pre[q] += v;
-        }
-        cells += P.growCells[k];
-    }
-    growReduce(G, pre, none);
-    __syncthreads();
-    growReduce(G, tot, cells);
-    if (tid == 0) {
-        for (int q = 0; q < GROW_LISTS; q++) {
-            G.base[q] = pre[q];
-            G.total[q] = tot[q];
-        }
-        G.cells = cells;
-        if (blockIdx.x == 0) {
-            DevState* s = P.st;
-            s->nActive = tot[0];
-            s->nDeact = tot[1];
-            s->nInact = tot[2];
-            s->nStrips = tot[3];
-            s->activeCells += cells;
-        }
-    }
-    __syncthreads();
-    int base[GROW_LISTS] = {G.base[0], G.base[1], G.base[2], G.base[3]};
-    const int nAct = G.total[0];
-    int s0, s1;
-    stripChunk(P, s0, s1);
     for (int rb = s0; rb < s1; rb += STRIPS_PER_ROUND) {
         const GrowItem t = growItem(P, rb, s1);
-        int inWarp[GROW_LISTS];
         for (int q = 0; q < GROW_LISTS; q++) {
             const unsigned bal = __ballot_sync(0xffffffffu, t.f[q]);
-            inWarp[q] = __popc(bal & ((1u << lane) - 1u));
-            if (lane == 0) G.wsum[q][w] = __popc(bal);
+            if (!bal) continue;  // warp-uniform
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&s->appendCnt[q], __popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (t.f[q]) lists[q][base + __popc(bal & ((1u << lane) - 1u))] = q == 3 ? t.strip : t.b;
         }
-        __syncthreads();
-        if (tid < GROW_LISTS) {  // thread q: exclusive scan of list q's warp totals
-            int x = 0;
-            for (int k = 0; k < NT / 32; k++) {
-                const int y = G.wsum[tid][k];
-                G.wsum[tid][k] = x;
-                x += y;
-            }
-            G.wsum[tid][NT / 32] = x;
-        }
-        __syncthreads();
-        if (t.f[0]) P.act[base[0] + G.wsum[0][w] + inWarp[0]] = t.b;
-        if (t.f[1]) P.deact[base[1] + G.wsum[1][w] + inWarp[1]] = t.b;
-        if (t.f[2]) P.inact[base[2] + G.wsum[2][w] + inWarp[2]] = t.b;
-        if (t.f[3]) P.strips[base[3] + G.wsum[3][w] + inWarp[3]] = t.strip;
+        if (t.f[0]) cells += (unsigned long long)t.cells;
         if (t.b >= 0) {
             if (t.v && t.cells == 0) {
                 P.mx[t.b] = 0.f;
@@ -202,29 +112,34 @@ __device__ int growWrite(const Params& P, GrowSmem& G) {
             }
             P.prevAct[t.b] = (uint8_t)(t.v ? 1 : 0);
         }
-        for (int q = 0; q < GROW_LISTS; q++) base[q] += G.wsum[q][NT / 32];
-        __syncthreads();
     }
-    return nAct;
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
+    if (lane == 0 && cells) atomicAdd(&s->appendCells, cells);
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&s->growTicket, 1u) == gridDim.x - 1) {
+            __threadfence();
+            s->nActive = atomicExch(&s->appendCnt[0], 0);
+            s->nDeact = atomicExch(&s->appendCnt[1], 0);
+            s->nInact = atomicExch(&s->appendCnt[2], 0);
+            s->nStrips = atomicExch(&s->appendCnt[3], 0);
+            s->activeCells += atomicExch(&s->appendCells, 0ull);
+            atomicExch(&s->growTicket, 0u);
+        }
+    }
 }
 
-// Graph path: pass A (with the stop test and the start of the step) and
-// pass B as two launches over the same grid.
-__global__ void __launch_bounds__(NT) k_grow_a(Params P) {
-    __shared__ GrowSmem G;
+// Graph path: the stop test, the start of the step and the grow in one
+// launch.
+__global__ void __launch_bounds__(NT) k_grow(Params P) {
     DevState* s = P.st;
     if (s->t >= s->t_stop) {  // every CTA reads the same t
         if (blockIdx.x == 0 && threadIdx.x == 0) s->stop = 1;
         return;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) beginStep(P, s);
-    growCount(P, G);
-}
-
-__global__ void __launch_bounds__(NT) k_grow_b(Params P) {
-    __shared__ GrowSmem G;
-    if (P.st->stop) return;
-    growWrite(P, G);
+    if (blockIdx.x == 0 && threadIdx.x < 32) beginStep(P, s);
+    growAppend(P);
 }
 
 }  // namespace rift

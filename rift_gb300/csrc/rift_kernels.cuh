@@ -4,7 +4,7 @@
 //   k_track   : re-wet inactive tiles under gridded rain / surge
 //               (TrackRainfall_k / TrackSurge_k, grid.cu:1224-1276); only
 //               when a gridded rain or surge series is on
-//   k_grow_a/b: start of step (stop test, uniform-source interpolation of
+//   k_grow    : start of step (stop test, uniform-source interpolation of
 //               simulator.cu:500-538), then the 4-neighbour dilation of the
 //               wet tiles and the on-device compaction of the active /
 //               inactive / deactivated tile lists and of the march strips
@@ -74,6 +74,10 @@ struct DevState {
     int persistExit;   // the persistent kernel left because the active set grew
     int steps_done;
     unsigned long long activeCells;  // interior cells of active tiles, summed over steps
+    int appendCnt[4];                // grow: list counters (zero between steps)
+    unsigned long long appendCells;
+    unsigned growTicket;
+    unsigned staleBits[2];           // ensemble: stale speed maxima of inactive tiles
     double v_added;    // volume (depth x cells) the sources added since init
     double rain_sum[2];  // interior sums of the two rain maps (volume ledger)
     int error;
@@ -112,8 +116,6 @@ struct Params {
     int marchMin;      // active strips from which the march kernels run
     int persistMax;    // the persistent step kernel runs while active tiles <= this
     struct GridBar* gbar;            // grid barrier of the persistent kernel
-    int* growCnt;                    // [CTA][4] list counts of the chunked grow
-    unsigned long long* growCells;   // [CTA] interior cells of active tiles
     float* mx;
     float* my;
     const int* srcIdx;      // flat h-grid indices j*nx+i
@@ -254,6 +256,31 @@ __device__ __forceinline__ void staleMax(const Params& P, float& amx, float& amy
         }
 }
 
+// ComputeTimestep's arithmetic (simulator.cu:540-566) from the maxima of
+// the tile speeds: dt with the reference's rounding points (fmaxf on the
+// scaled maxima, FP64 division), t += dt, and the step's entry in the
+// volume ledger.
+__device__ __forceinline__ void computeDt(const Params& P, DevState* st, double maxx, double maxy) {
+    double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
+    double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
+    double dt = cx < cy ? cx : cy;
+    if (st->t == 0.0) dt = (double)0.000001f;
+    st->dt_old = st->dt;
+    st->dt = dt;
+    st->t = st->t + dt;
+    // volume ledger: both RK stages (or the Euler stage) apply each
+    // source rate of this step for dt -- uniform rain on every interior
+    // cell, the point sources, the gridded rain map at this step's factor
+    double add = 0.0;
+    if (P.flags & F_RAIN_U) add += (double)st->rain_rate * (double)(P.nx - 4) * (P.ny - 4);
+    for (int k = 0; k < P.nsrc; k++) add += (double)P.srcRate[k];
+    if ((P.flags & F_RAIN_G) && P.mapMode[0] != 0) {
+        add += st->rain_sum[0];
+        if (P.mapMode[0] == 2) add += (double)st->factor[0] * (st->rain_sum[1] - st->rain_sum[0]);
+    }
+    st->v_added += add * dt;
+}
+
 // Simulator::ComputeTimestep (simulator.cu:540-566) on device: block max of
 // stale and new tile speeds, one atomic per CTA; the last CTA to finish turns
 // the maxima into dt with the reference's rounding points (fmaxf on the
@@ -277,62 +304,46 @@ __device__ __forceinline__ void finishDt(const Params& P, float amx, float amy, 
         __threadfence();
         double maxx = (double)__uint_as_float(atomicOr(&st->max_bits[0], 0u));
         double maxy = (double)__uint_as_float(atomicOr(&st->max_bits[1], 0u));
-        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
-        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
-        double dt = cx < cy ? cx : cy;
-        if (st->t == 0.0) dt = (double)0.000001f;
-        st->dt_old = st->dt;
-        st->dt = dt;
-        st->t = st->t + dt;
-        // volume ledger: both RK stages (or the Euler stage) apply each
-        // source rate of this step for dt -- uniform rain on every interior
-        // cell, the point sources, the gridded rain map at this step's factor
-        double add = 0.0;
-        if (P.flags & F_RAIN_U) add += (double)st->rain_rate * (double)(P.nx - 4) * (P.ny - 4);
-        for (int k = 0; k < P.nsrc; k++) add += (double)P.srcRate[k];
-        if ((P.flags & F_RAIN_G) && P.mapMode[0] != 0) {
-            add += st->rain_sum[0];
-            if (P.mapMode[0] == 2) add += (double)st->factor[0] * (st->rain_sum[1] - st->rain_sum[0]);
-        }
-        st->v_added += add * dt;
+        computeDt(P, st, maxx, maxy);
     }
 }
 
 // Re-sync U* with U^n on the tiles that went inactive this step (interior
 // cells and the ghost cells they own): the stage kernels read U* in the halo
 // of active tiles, and for an inactive tile U* = U^n.
-__device__ __forceinline__ void resyncDeactivated(const Params& P) {
-    const int nDe = P.st->nDeact;
+__device__ __forceinline__ void resyncTile(const Params& P, int tile) {
     const int tid = threadIdx.x;
-    for (int k = blockIdx.x; k < nDe; k += gridDim.x) {
-        const int tile = P.deact[k];
-        const int bX = tile % P.nBX, bY = tile / P.nBX;
-        for (int q = tid; q < TW * TH; q += blockDim.x) {
-            const int i = bX * TW + q % TW + 2, j = bY * TH + q / TW + 2;
-            auto cp = [&](int jj, int ii) {
-                for (int f = 0; f < 3; f++) P.B[cidx(P, f, jj, ii)] = P.A[cidx(P, f, jj, ii)];
-            };
-            if (i < P.nx && j < P.ny) cp(j, i);
-            if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
-                if (i == 2) {
-                    cp(j, 0);
-                    cp(j, 1);
-                }
-                if (i == P.nx - 3) {
-                    cp(j, P.nx - 2);
-                    cp(j, P.nx - 1);
-                }
-                if (j == 2) {
-                    cp(0, i);
-                    cp(1, i);
-                }
-                if (j == P.ny - 3) {
-                    cp(P.ny - 2, i);
-                    cp(P.ny - 1, i);
-                }
+    const int bX = tile % P.nBX, bY = tile / P.nBX;
+    for (int q = tid; q < TW * TH; q += blockDim.x) {
+        const int i = bX * TW + q % TW + 2, j = bY * TH + q / TW + 2;
+        auto cp = [&](int jj, int ii) {
+            for (int f = 0; f < 3; f++) P.B[cidx(P, f, jj, ii)] = P.A[cidx(P, f, jj, ii)];
+        };
+        if (i < P.nx && j < P.ny) cp(j, i);
+        if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
+            if (i == 2) {
+                cp(j, 0);
+                cp(j, 1);
+            }
+            if (i == P.nx - 3) {
+                cp(j, P.nx - 2);
+                cp(j, P.nx - 1);
+            }
+            if (j == 2) {
+                cp(0, i);
+                cp(1, i);
+            }
+            if (j == P.ny - 3) {
+                cp(P.ny - 2, i);
+                cp(P.ny - 1, i);
             }
         }
     }
+}
+
+__device__ __forceinline__ void resyncDeactivated(const Params& P) {
+    const int nDe = P.st->nDeact;
+    for (int k = blockIdx.x; k < nDe; k += gridDim.x) resyncTile(P, P.deact[k]);
 }
 
 // Schedule: the march kernels (strips of 7 x 2 tiles) run when at least
@@ -394,85 +405,115 @@ __device__ __forceinline__ bool tileAcquire(StageSmem& S, const CUtensorMap* tmI
 // series is interpolated at float(t) (source.cc:65-73) and its float state
 // divided in place every step.  IEEE float ops (_rn intrinsics) keep the host's
 // arithmetic (no contraction, exact division).
+// Called by one whole warp: the lanes test the intervals [T[i], T[i+1]) in
+// parallel; the last interval holding t wins, as in the sequential loop.
 __device__ __forceinline__ float seriesInterp(const float* T, const float* R, int n, float t,
                                               float cur) {
-    for (int i = 0; i + 1 < n; i++) {
-        if (t >= T[i] && t < T[i + 1]) {
-            float num = __fsub_rn(R[i + 1], R[i]);
-            float den = __fsub_rn(T[i + 1], T[i]);
-            cur = __fadd_rn(R[i], __fmul_rn(__fdiv_rn(num, den), __fsub_rn(t, T[i])));
-        }
+    const int lane = threadIdx.x & 31;
+    int found = -1;
+    for (int base = 0; base + 1 < n; base += 32) {
+        const int i = base + lane;
+        bool m = false;
+        if (i + 1 < n) m = (t >= T[i] && t < T[i + 1]);
+        const unsigned bal = __ballot_sync(0xffffffffu, m);
+        if (bal) found = base + 31 - __clz(bal);
+    }
+    if (found >= 0) {
+        const int i = found;
+        float num = __fsub_rn(R[i + 1], R[i]);
+        float den = __fsub_rn(T[i + 1], T[i]);
+        cur = __fadd_rn(R[i], __fmul_rn(__fdiv_rn(num, den), __fsub_rn(t, T[i])));
     }
     return cur;
 }
 
+// Start of a step, by one whole warp: reset of the step's reductions, the
+// uniform source rates at float(t), the map factors that follow t.
 __device__ void beginStep(const Params& P, DevState* s) {
-    s->stop = 0;
-    s->steps_done += 1;
-    s->max_bits[0] = 0u;
-    s->max_bits[1] = 0u;
-    s->ticket = 0u;
+    const int lane = threadIdx.x & 31;
     const float tf = (float)s->t;
     if (P.serN[2] > 0) {  // hydrograph, cfs -> m^3/s -> m/s per source cell
         float v = seriesInterp(P.serT + 2 * MAX_SERIES, P.serR + 2 * MAX_SERIES, P.serN[2], tf,
                                s->ser_interp[2]);
         v = __fdiv_rn(v, 35.3147f);
-        s->ser_interp[2] = v;
-        double r = (double)v / P.dxd / P.dyd / (double)P.nsrc;
-        for (int k = 0; k < P.nsrc; k++) P.srcRate[k] = (float)r;
+        const double r = (double)v / P.dxd / P.dyd / (double)P.nsrc;
+        for (int k = lane; k < P.nsrc; k += 32) P.srcRate[k] = (float)r;
+        if (lane == 0) s->ser_interp[2] = v;
     }
     if (P.serN[0] > 0) {  // hyetograph, mm/hr -> m/s
         float v = seriesInterp(P.serT, P.serR, P.serN[0], tf, s->ser_interp[0]);
         v = __fdiv_rn(v, 3600.f * 1000.f);
-        s->ser_interp[0] = v;
-        s->rain_rate = v;
+        if (lane == 0) {
+            s->ser_interp[0] = v;
+            s->rain_rate = v;
+        }
     }
     if (P.serN[1] > 0) {  // drain, mm/hr -> m/s
         float v = seriesInterp(P.serT + MAX_SERIES, P.serR + MAX_SERIES, P.serN[1], tf,
                                s->ser_interp[1]);
         v = __fdiv_rn(v, 3600.f * 1000.f);
-        s->ser_interp[1] = v;
-        s->drain_rate = v;
+        if (lane == 0) {
+            s->ser_interp[1] = v;
+            s->drain_rate = v;
+        }
     }
-    // map factor following t (GridSeries::update computes it at the end of
-    // the previous step from the same t, GridSeries.cu:398)
-    for (int w = 0; w < 3; w++)
-        if (s->map_timed[w])
-            s->factor[w] = (float)((s->t - s->map_t0[w]) / (s->map_t1[w] - s->map_t0[w]));
+    if (lane == 0) {
+        s->stop = 0;
+        s->steps_done += 1;
+        s->max_bits[0] = 0u;
+        s->max_bits[1] = 0u;
+        s->ticket = 0u;
+        // map factor following t (GridSeries::update computes it at the end
+        // of the previous step from the same t, GridSeries.cu:398)
+        for (int w = 0; w < 3; w++)
+            if (s->map_timed[w])
+                s->factor[w] = (float)((s->t - s->map_t0[w]) / (s->map_t1[w] - s->map_t0[w]));
+    }
 }
 
 // ---------------------------------------------------------------- k_track
 // TrackRainfall_k / TrackSurge_k over the tiles that were inactive after the
 // previous Grow.  The rows come from blockY * BLOCK_COLS (16), not 14, as in
 // the reference.
-__device__ __forceinline__ void trackTiles(const Params& P) {
+// Factors of the gridded rain and surge maps at the start of the step (the
+// tracking runs before the step's own factor update).
+__device__ __forceinline__ void trackFactors(const Params& P, float& fac0, float& fac2) {
     const DevState* s = P.st;
-    const int n = s->nInact;
-    float fac0 = s->factor[0], fac2 = s->factor[2];
+    fac0 = s->factor[0];
+    fac2 = s->factor[2];
     if (s->map_timed[0]) fac0 = (float)((s->t - s->map_t0[0]) / (s->map_t1[0] - s->map_t0[0]));
     if (s->map_timed[2]) fac2 = (float)((s->t - s->map_t0[2]) / (s->map_t1[2] - s->map_t0[2]));
-    for (int k = blockIdx.x; k < n; k += gridDim.x) {
-        const int tile = P.inact[k];
-        if (P.wet[tile]) continue;  // uniform across the block
-        const int bX = tile % P.nBX, bY = tile / P.nBX;
-        bool hit = false;
-        if (threadIdx.x < TW * TH) {
-            int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
-            int i = bX * TW + tx + 2, j = bY * TW + ty + 2;
-            if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
-                size_t c = cidx(P, 0, j, i);
-                if (P.flags & F_RAIN_G) {
-                    float v = mapValue(P, 0, c, fac0);
-                    if (v > kEps) hit = true;
-                }
-                if (P.flags & F_SURGE) {
-                    float v = mapValue(P, 2, c, fac2);
-                    if (v != P.nodata && v > 0.f) hit = true;
-                }
+}
+
+// One inactive tile: re-wet it when a cell of the rows the reference checks
+// has gridded rain above epsilon or a positive surge depth.
+__device__ __forceinline__ void trackTile(const Params& P, int tile, float fac0, float fac2) {
+    if (P.wet[tile]) return;  // uniform across the block
+    const int bX = tile % P.nBX, bY = tile / P.nBX;
+    bool hit = false;
+    if (threadIdx.x < TW * TH) {
+        int tx = threadIdx.x % TW, ty = threadIdx.x / TW;
+        int i = bX * TW + tx + 2, j = bY * TW + ty + 2;
+        if (i >= 2 && j >= 2 && i <= P.nx - 3 && j <= P.ny - 3) {
+            size_t c = cidx(P, 0, j, i);
+            if (P.flags & F_RAIN_G) {
+                float v = mapValue(P, 0, c, fac0);
+                if (v > kEps) hit = true;
+            }
+            if (P.flags & F_SURGE) {
+                float v = mapValue(P, 2, c, fac2);
+                if (v != P.nodata && v > 0.f) hit = true;
             }
         }
-        if (__syncthreads_or(hit) && threadIdx.x == 0) P.wet[tile] = 1;
     }
+    if (__syncthreads_or(hit) && threadIdx.x == 0) P.wet[tile] = 1;
+}
+
+__device__ __forceinline__ void trackTiles(const Params& P) {
+    const int n = P.st->nInact;
+    float fac0, fac2;
+    trackFactors(P, fac0, fac2);
+    for (int k = blockIdx.x; k < n; k += gridDim.x) trackTile(P, P.inact[k], fac0, fac2);
 }
 
 __global__ void __launch_bounds__(NT) k_track(Params P) {
@@ -487,6 +528,59 @@ __global__ void __launch_bounds__(NT) k_track(Params P) {
 // CTA, dt with the reference's rounding points (fmaxf of the scaled maxima,
 // FP64 division) and t += dt.  Also re-syncs U* with U^n on tiles that went
 // inactive this step (interior cells and the ghost cells they own).
+// Local-speed maxima of one staged tile (the speed output of the first
+// ComputeFluxes, grid.cu:813-838): depth and normal-momentum reconstruction,
+// the east and north face of every interior cell.  Valid in thread 0.
+__device__ __forceinline__ void tileSpeeds(StageSmem& S, const TileBuf& T, const Params& P, int i0,
+                                           int j0, float& mxv, float& myv) {
+    const int tid = threadIdx.x;
+    const float kappa = P.kappa;
+    float spx = 0.f, spy = 0.f;
+    // x: depth + hu reconstruction of cells i0-1..i0+16 on the tile rows
+    if (tid < TH * (TW + 2)) {
+        int r = tid / (TW + 2), c = tid % (TW + 2);
+        int sr = r + 2, sc = c + 1;
+        RecN R = constructN(T.in[0][sr][sc], T.in[1][sr][sc], T.in[0][sr][sc + 1],
+                            T.in[1][sr][sc + 1], T.in[0][sr][sc - 1], T.in[1][sr][sc - 1],
+                            T.e[0][sr][sc], T.e[1][sr][sc], T.e[1][sr][sc] - T.e[0][sr][sc + 1],
+                            T.e[1][sr][sc - 1] - T.e[0][sr][sc]);
+        S.rec.x.P[0][r][c] = R.hP;
+        S.rec.x.P[1][r][c] = R.qP;
+        S.rec.x.M[0][r][c] = R.hM;
+        S.rec.x.M[1][r][c] = R.qM;
+    }
+    __syncthreads();
+    if (tid < TH * TW) {  // east face of tile cell (ty, tx)
+        int ty = tid / TW, tx = tid % TW;
+        if (i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3)
+            spx = faceSpeed(S.rec.x.P[0][ty][tx + 1], S.rec.x.P[1][ty][tx + 1],
+                            S.rec.x.M[0][ty][tx + 2], S.rec.x.M[1][ty][tx + 2], kappa);
+    }
+    __syncthreads();
+    // y: depth + hv reconstruction of rows j0..j0+14
+    if (tid < (TH + 2) * TW) {
+        int r = tid / TW, c = tid % TW;
+        int sr = r + 1, sc = c + 2;
+        RecN R = constructN(T.in[0][sr][sc], T.in[2][sr][sc], T.in[0][sr + 1][sc],
+                            T.in[2][sr + 1][sc], T.in[0][sr - 1][sc], T.in[2][sr - 1][sc],
+                            T.e[2][sr][sc], T.e[3][sr][sc], T.e[3][sr][sc] - T.e[2][sr + 1][sc],
+                            T.e[3][sr - 1][sc] - T.e[2][sr][sc]);
+        S.rec.y.P[0][r][c] = R.hP;
+        S.rec.y.P[1][r][c] = R.qP;
+        S.rec.y.M[0][r][c] = R.hM;
+        S.rec.y.M[1][r][c] = R.qM;
+    }
+    __syncthreads();
+    if (tid < TH * TW) {  // north face of tile cell (ty, tx)
+        int ty = tid / TW, tx = tid % TW;
+        if (i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3)
+            spy = faceSpeed(S.rec.y.P[0][ty + 1][tx], S.rec.y.P[1][ty + 1][tx],
+                            S.rec.y.M[0][ty + 2][tx], S.rec.y.M[1][ty + 2][tx], kappa);
+    }
+    mxv = blockMax(spx, S.red[0]);
+    myv = blockMax(spy, S.red[1]);
+}
+
 // Tile loop of the speed pass over the scheduled active tiles; thread 0
 // keeps the CTA's maximum of the new tile speeds.  False after a TMA
 // timeout (error recorded).
@@ -494,7 +588,6 @@ __device__ bool speedTiles(StageSmem& S, const CUtensorMap* tmA, const CUtensorM
                            const Params& P, int nAct, uint32_t* ph, float& tmx, float& tmy) {
     DevState* st = P.st;
     const int tid = threadIdx.x;
-    const float kappa = P.kappa;
     tileFirst(S, tmA, tmE, P, nAct);
     int bsel = 0;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
@@ -506,50 +599,8 @@ __device__ bool speedTiles(StageSmem& S, const CUtensorMap* tmA, const CUtensorM
             return false;
         }
         const TileBuf& T = S.buf[bsel];
-        float spx = 0.f, spy = 0.f;
-        // x: depth + hu reconstruction of cells i0-1..i0+16 on the tile rows
-        if (tid < TH * (TW + 2)) {
-            int r = tid / (TW + 2), c = tid % (TW + 2);
-            int sr = r + 2, sc = c + 1;
-            RecN R = constructN(T.in[0][sr][sc], T.in[1][sr][sc], T.in[0][sr][sc + 1],
-                                T.in[1][sr][sc + 1], T.in[0][sr][sc - 1], T.in[1][sr][sc - 1],
-                                T.e[0][sr][sc], T.e[1][sr][sc], T.e[1][sr][sc] - T.e[0][sr][sc + 1],
-                                T.e[1][sr][sc - 1] - T.e[0][sr][sc]);
-            S.rec.x.P[0][r][c] = R.hP;
-            S.rec.x.P[1][r][c] = R.qP;
-            S.rec.x.M[0][r][c] = R.hM;
-            S.rec.x.M[1][r][c] = R.qM;
-        }
-        __syncthreads();
-        if (tid < TH * TW) {  // east face of tile cell (ty, tx)
-            int ty = tid / TW, tx = tid % TW;
-            if (i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3)
-                spx = faceSpeed(S.rec.x.P[0][ty][tx + 1], S.rec.x.P[1][ty][tx + 1],
-                                S.rec.x.M[0][ty][tx + 2], S.rec.x.M[1][ty][tx + 2], kappa);
-        }
-        __syncthreads();
-        // y: depth + hv reconstruction of rows j0..j0+14
-        if (tid < (TH + 2) * TW) {
-            int r = tid / TW, c = tid % TW;
-            int sr = r + 1, sc = c + 2;
-            RecN R = constructN(T.in[0][sr][sc], T.in[2][sr][sc], T.in[0][sr + 1][sc],
-                                T.in[2][sr + 1][sc], T.in[0][sr - 1][sc], T.in[2][sr - 1][sc],
-                                T.e[2][sr][sc], T.e[3][sr][sc], T.e[3][sr][sc] - T.e[2][sr + 1][sc],
-                                T.e[3][sr - 1][sc] - T.e[2][sr][sc]);
-            S.rec.y.P[0][r][c] = R.hP;
-            S.rec.y.P[1][r][c] = R.qP;
-            S.rec.y.M[0][r][c] = R.hM;
-            S.rec.y.M[1][r][c] = R.qM;
-        }
-        __syncthreads();
-        if (tid < TH * TW) {  // north face of tile cell (ty, tx)
-            int ty = tid / TW, tx = tid % TW;
-            if (i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3)
-                spy = faceSpeed(S.rec.y.P[0][ty + 1][tx], S.rec.y.P[1][ty + 1][tx],
-                                S.rec.y.M[0][ty + 2][tx], S.rec.y.M[1][ty + 2][tx], kappa);
-        }
-        float mxv = blockMax(spx, S.red[0]);
-        float myv = blockMax(spy, S.red[1]);
+        float mxv, myv;
+        tileSpeeds(S, T, P, i0, j0, mxv, myv);
         if (tid == 0) {
             P.mx[tile] = mxv;
             P.my[tile] = myv;
@@ -955,36 +1006,37 @@ __global__ void __launch_bounds__(NT) k_stage(const __grid_constant__ CUtensorMa
 // result, written to the stage buffer so that no CTA reads a halo cell
 // another CTA is updating, is copied back over U^n for the active tiles
 // (interior cells and the ghost cells they own), together with F.
-__device__ __forceinline__ void commitTiles(const Params& P, int nAct) {
+__device__ __forceinline__ void commitTile(const Params& P, int tile) {
     const int tid = threadIdx.x;
-    for (int k = blockIdx.x; k < nAct; k += gridDim.x) {
-        const int tile = P.act[k];
-        const int bX = tile % P.nBX, bY = tile / P.nBX;
-        if (tid >= TW * TH) continue;
-        const int i = bX * TW + tid % TW + 2, j = bY * TH + tid / TW + 2;
-        if (!(i <= P.nx - 3 && j <= P.ny - 3)) continue;
-        auto cp = [&](int jj, int ii) {
-            for (int f = 0; f < 3; f++) P.A[cidx(P, f, jj, ii)] = P.B[cidx(P, f, jj, ii)];
-        };
-        cp(j, i);
-        if (P.flags & F_INFIL) P.FA[cidx(P, 0, j, i)] = P.FB[cidx(P, 0, j, i)];
-        if (i == 2) {
-            cp(j, 0);
-            cp(j, 1);
-        }
-        if (i == P.nx - 3) {
-            cp(j, P.nx - 2);
-            cp(j, P.nx - 1);
-        }
-        if (j == 2) {
-            cp(0, i);
-            cp(1, i);
-        }
-        if (j == P.ny - 3) {
-            cp(P.ny - 2, i);
-            cp(P.ny - 1, i);
-        }
+    const int bX = tile % P.nBX, bY = tile / P.nBX;
+    if (tid >= TW * TH) return;
+    const int i = bX * TW + tid % TW + 2, j = bY * TH + tid / TW + 2;
+    if (!(i <= P.nx - 3 && j <= P.ny - 3)) return;
+    auto cp = [&](int jj, int ii) {
+        for (int f = 0; f < 3; f++) P.A[cidx(P, f, jj, ii)] = P.B[cidx(P, f, jj, ii)];
+    };
+    cp(j, i);
+    if (P.flags & F_INFIL) P.FA[cidx(P, 0, j, i)] = P.FB[cidx(P, 0, j, i)];
+    if (i == 2) {
+        cp(j, 0);
+        cp(j, 1);
     }
+    if (i == P.nx - 3) {
+        cp(j, P.nx - 2);
+        cp(j, P.nx - 1);
+    }
+    if (j == 2) {
+        cp(0, i);
+        cp(1, i);
+    }
+    if (j == P.ny - 3) {
+        cp(P.ny - 2, i);
+        cp(P.ny - 1, i);
+    }
+}
+
+__device__ __forceinline__ void commitTiles(const Params& P, int nAct) {
+    for (int k = blockIdx.x; k < nAct; k += gridDim.x) commitTile(P, P.act[k]);
 }
 
 __global__ void __launch_bounds__(NT) k_commit(Params P) {

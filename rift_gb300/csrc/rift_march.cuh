@@ -13,7 +13,7 @@
 //   - the cell update (sources, friction, RK stage, outputs, ghost cells) is
 //     the same arithmetic as grid.cu's Integrate kernels.
 // Rows arrive in shared memory through TMA: 4-row chunks of the 120-column
-// block of (h, hu, hv) and of the four face-elevation offsets, a 3-slot ring
+// block of (h, hu, hv) and of the four face-elevation offsets, a 2-slot ring
 // refilled as the march moves up (one barrier per chunk).
 // A cell is updated only when its reference tile is active, so results and
 // tile flags are those of the per-tile schedule of the reference.
@@ -28,7 +28,7 @@ constexpr int MOWN = 28;                           // owned columns per warp
 constexpr int MCOLS = STRIP_TX * TW;               // 112 columns per strip
 constexpr int MBOXW = 120;                         // staged columns [112 sx - 4, 112 sx + 116)
 constexpr int MRC = 4;                             // rows per staged chunk
-constexpr int MNSLOT = 3;                          // chunk ring depth
+constexpr int MNSLOT = 2;                          // chunk ring depth
 constexpr int MHR = STRIP_TY * TH;                 // 28 output rows per strip
 constexpr int MNROWS = MHR + 4;                    // 32 staged rows (2-row halo each side)
 constexpr int MNCHUNK = (MNROWS + MRC - 1) / MRC;  // 8 chunks
@@ -99,7 +99,7 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
 // STAGE 2: reads U* (B) and U^n (A) at the cell -> writes U^{n+1} (A),
 //          F^{n+1} (FA), outputs, tile wet flags and tile speeds.
 template <int STAGE>
-__global__ void __launch_bounds__(MT) k_march(const __grid_constant__ CUtensorMap tmIn,
+__global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtensorMap tmIn,
                                               const __grid_constant__ CUtensorMap tmE, Params P) {
     __shared__ MarchSmem S;
     __shared__ bool last;

@@ -5,8 +5,8 @@
 // working.  k_persist runs many steps in one cooperative launch (all CTAs
 // resident), the phases separated by a grid barrier:
 //   [track]  re-wet inactive tiles under gridded rain / surge
-//   grow A   each CTA counts the list entries of its chunk of strips
-//   grow B   each CTA writes its chunk of the lists (rift_grow.cuh)
+//   grow     each CTA appends the list entries of its chunk of strips; the
+//            last one publishes the counts (rift_grow.cuh)
 //   speed    tile speeds of U^n, dt and t (last CTA), U* re-sync
 //   stage 1  RK stage 1 (per-tile code of k_stage<1>)
 // With at most one active tile per CTA, the speed and stage-1 phases become
@@ -80,7 +80,6 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                                                 const __grid_constant__ CUtensorMap tmE, Params P,
                                                 int maxSteps) {
     __shared__ StageSmem S;
-    __shared__ GrowSmem G;
     __shared__ bool last;
     DevState* st = P.st;
     const int tid = threadIdx.x;
@@ -109,12 +108,11 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             trackTiles(P);
             RIFT_SYNC();
         }
-        if (blockIdx.x == 0 && tid == 0) beginStep(P, st);
-        growCount(P, G);
+        if (blockIdx.x == 0 && tid < 32) beginStep(P, st);
+        growAppend(P);
         RIFT_SYNC();
-        const int nAct = growWrite(P, G);
+        const int nAct = st->nActive;  // published by the grow's last CTA
         nActPrev = nAct;
-        RIFT_SYNC();
         float amx = 0.f, amy = 0.f, tmx = 0.f, tmy = 0.f;
         if (nAct <= (int)gridDim.x) {
             // At most one tile per CTA: stage 1's fluxes of U^n are the first

@@ -261,6 +261,42 @@ def config3(N=8192, seed=2, cell=2.0, tf=10800.0, nblocks=4000) -> Case:
     return case
 
 
+def config5(members=128, side=(256, 2048), seed=0, cell=5.0, tf=14400.0) -> list:
+    """Batched ensemble: members on square domains of uneven size (side
+    uniform in `side` cells at 5 m), each with its own fractal DEM (seed =
+    member id); per member a uniform rain of lognormal scale (median 40
+    mm/hr, sigma_ln 0.5) lasting 1-3 h; every second member also has a
+    point hydrograph of 100-800 cfs (triangular, peak at 1 h, over 3 h) at
+    the domain's lowest interior corner point."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for m in range(members):
+        N = int(rng.integers(side[0], side[1] + 1))
+        mr = np.random.default_rng(m)
+        z = fractal_surface(N, 0.8, 20.0, mr) + 5.0
+        z[:2, :] += 30.0
+        z[-2:, :] += 30.0
+        z[:, :2] += 30.0
+        z[:, -2:] += 30.0
+        n = np.zeros((N + 4, N + 4))
+        n[2:-2, 2:-2] = 0.035
+        rate = float(np.exp(np.log(40.0) + 0.5 * rng.standard_normal()))
+        hours = float(rng.uniform(1.0, 3.0))
+        series = {0: csv_series([0, hours, hours, 4], [rate, rate, 0, 0])}
+        flags = RAIN_UNIFORM | TILE_ACCEL
+        src = None
+        if m % 2 == 1:
+            q = float(rng.uniform(100.0, 800.0))
+            series[2] = csv_series([0, 1, 3], [0, q, 0])
+            inner = z[4:-4, 4:-4]
+            jj, ii = np.unravel_index(np.argmin(inner), inner.shape)
+            src = np.array([(jj + 4 + 2) * (N + 4) + (ii + 4 + 2)], dtype=np.int32)
+            flags |= POINT_SOURCE
+        cases.append(Case(name=f"member{m}_{N}", B=z, cell=cell, n=n, tf=tf, flags=flags,
+                          series=series, src_idx=src))
+    return cases
+
+
 def smooth_field(shape, corr_cells, rng):
     """Gaussian random field with Gaussian correlation (FFT filter), unit variance."""
     ny, nx = shape

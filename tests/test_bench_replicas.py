@@ -60,6 +60,6 @@ def test_combine_replicas_gloo_world2():
 
 def test_launches_per_step():
     from rift_gb300 import synth
-    assert bench.launches_per_step(synth.RAIN_UNIFORM) == 8
-    assert bench.launches_per_step(synth.RAIN_GRID) == 9
-    assert bench.launches_per_step(synth.EULER | synth.SURGE_GRID) == 8
+    assert bench.launches_per_step(synth.RAIN_UNIFORM) == 7
+    assert bench.launches_per_step(synth.RAIN_GRID) == 8
+    assert bench.launches_per_step(synth.EULER | synth.SURGE_GRID) == 7
