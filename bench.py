@@ -218,6 +218,11 @@ def run_ours(args, device=0, sync=None):
 
     # ---- device-timed run (inputs resident) --------------------------------
     sim.load_snapshot(snap)
+    tuned = None
+    if args.autotune > 0:
+        choice, ms = sim.autotune(args.autotune)
+        tuned = {"choice": ["persistent", "graph+tiles", "graph+march"][choice],
+                 "ms_per_step": [None if np.isnan(x) else float(x) for x in ms]}
     for _ in range(args.warmup):
         sim.step()
     clocks = ClockSampler().start()
@@ -284,7 +289,8 @@ def run_ours(args, device=0, sync=None):
                      "kernel": kernel},
         "clocks": clk,
         "gpu_launches": launches,
-        "path": {"persistent_steps": persist_steps, "graph_steps": graph_steps},
+        "path": {"persistent_steps": persist_steps, "graph_steps": graph_steps,
+                 "autotune": tuned},
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, snap, args)
@@ -455,6 +461,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--schedule", type=int, default=-1,
                     help="march kernels from this many active strips up (-1: engine default)")
+    ap.add_argument("--autotune", type=int, default=0,
+                    help="before the timed region, time each schedule for this many steps "
+                         "from the spun-up state and keep the fastest (0: off)")
     ap.add_argument("--persistent", type=int, default=-1,
                     help="persistent step loop while at most this many tiles are active "
                          "(-1: engine default, 0: off)")

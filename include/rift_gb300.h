@@ -206,6 +206,15 @@ int rift_set_schedule(rift_handle* h, int32_t march_min_strips);
  * RIFT_ERR_UNSUPPORTED when the device has no cooperative launch. */
 int rift_set_persistent(rift_handle* h, int32_t max_active_tiles);
 
+/* Schedule autotuner (no reference counterpart): from the current state,
+ * runs probe_steps steps on each schedule -- the persistent loop, the
+ * per-step graph with the per-tile kernels, the graph with the column-march
+ * kernels -- timing each with CUDA events, restores the state exactly, and
+ * keeps the fastest (as rift_set_persistent / rift_set_schedule would set
+ * it).  choice: 0, 1 or 2 in that order; ms_per_step[3] (may be NULL): the
+ * measured times (NaN for a schedule not available). */
+int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* ms_per_step);
+
 /* Ensembles (no reference counterpart; the reference runs one scenario per
  * process): members -- handles created, uploaded and initialised as usual,
  * on one device, of any sizes and options -- advance together in one

@@ -80,6 +80,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                   [_P, C.c_double, C.c_int32, _D, C.POINTER(C.c_int32)])
         ns["ensemble_last_error"] = _sig(lib, p + "ensemble_last_error", C.c_char_p, [_P])
         ns["ensemble_destroy"] = _sig(lib, p + "ensemble_destroy", None, [_P])
+    if hasattr(lib, p + "autotune"):
+        ns["autotune"] = _sig(lib, p + "autotune", C.c_int, [_P, C.c_int32, _I, _D])
     if hasattr(lib, p + "set_persistent"):
         ns["set_persistent"] = _sig(lib, p + "set_persistent", C.c_int, [_P, C.c_int32])
         ns["get_path_stats"] = _sig(lib, p + "get_path_stats", C.c_int,
@@ -237,6 +239,14 @@ class Sim:
         if "set_persistent" in self.f:
             self._check(self.f["set_persistent"](self.h, max_active_tiles), "set_persistent")
         return self
+
+    def autotune(self, probe_steps=10):
+        """Time each kernel schedule from the current state, restore the
+        state, keep the fastest; returns (choice, ms per step of each)."""
+        choice = C.c_int32()
+        ms = np.zeros(3)
+        self._check(self.f["autotune"](self.h, probe_steps, C.byref(choice), _dp(ms)), "autotune")
+        return choice.value, ms
 
     def path_stats(self):
         """(steps run by the persistent launch, steps run by the per-step graph)."""

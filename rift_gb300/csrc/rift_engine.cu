@@ -1099,6 +1099,97 @@ int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_s
     return RIFT_OK;
 }
 
+// ---------------------------------------------------------------- autotuner
+namespace {
+// Device regions that a step writes (state, outputs, tile arrays).
+std::vector<std::pair<void*, size_t>> stepRegions(rift_handle* h) {
+    const size_t pl = h->plane() * 4, G = (size_t)h->gridSize;
+    const size_t NS = (size_t)h->nSX * h->nSY;
+    std::vector<std::pair<void*, size_t>> r = {
+        {h->A, 3 * pl}, {h->B, 3 * pl}, {h->wet, G}, {h->prevAct, G}, {h->act, 4 * G},
+        {h->deact, 4 * G}, {h->inact, 4 * G}, {h->mx, 4 * G}, {h->my, 4 * G},
+        {h->strips, 4 * NS}, {h->stripFlag, NS}, {h->srcRate, 4 * (size_t)h->nsrc}};
+    for (float* p : {h->FA, h->FB, h->hmax, h->qmax, h->twet, h->tpeak, h->tdry})
+        if (p) r.push_back({p, pl});
+    return r;
+}
+}  // namespace
+
+int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* ms_per_step) {
+    if (!h || probe_steps < 1) return RIFT_ERR_ARG;
+    if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
+    int rc;
+    auto regions = stepRegions(h);
+    size_t total = 0;
+    for (auto& r : regions) total += (r.first ? r.second : 0);
+    char* scratch = nullptr;
+    CUDA_TRY(h, cudaMalloc(&scratch, total));
+    const DevState saved = *h->hst;  // the mirror equals the device state
+    auto copyAll = [&](bool save) -> int {
+        size_t off = 0;
+        for (auto& r : regions) {
+            if (!r.first || r.second == 0) continue;
+            void* dst = save ? (void*)(scratch + off) : r.first;
+            const void* src = save ? r.first : (const void*)(scratch + off);
+            CUDA_TRY(h, cudaMemcpyAsync(dst, src, r.second, cudaMemcpyDeviceToDevice, h->stream));
+            off += r.second;
+        }
+        return RIFT_OK;
+    };
+    const int keepPersist = h->persistMax, keepMarch = h->marchMin;
+    // candidates: persistent loop, per-step graph with tile kernels, with march kernels
+    const int persistOf[3] = {h->gridPersist > 0 ? INT32_MAX : -1, 0, 0};
+    const int marchOf[3] = {INT32_MAX, INT32_MAX, 0};
+    double best = INFINITY;
+    int pick = 1;
+    double ms3[3] = {NAN, NAN, NAN};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    rc = copyAll(true);
+    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+        rc = fail(h, RIFT_ERR_CUDA, "cudaEventCreate");
+    for (int c = 0; c < 3 && !rc; c++) {
+        if (persistOf[c] < 0) continue;
+        h->persistMax = persistOf[c];
+        h->marchMin = marchOf[c];
+        destroyGraph(h);
+        *h->hst = saved;
+        h->hst->t_stop = INFINITY;
+        h->hst->steps_done = 0;
+        bool current = false;
+        if ((rc = copyAll(false)) || (rc = pushState(h))) break;
+        if (cudaEventRecord(e0, h->stream) != cudaSuccess) {
+            rc = fail(h, RIFT_ERR_CUDA, "cudaEventRecord");
+            break;
+        }
+        if ((rc = runSteps(h, probe_steps, &current))) break;
+        cudaEventRecord(e1, h->stream);
+        if ((rc = pullState(h))) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms3[c] = ms / probe_steps;
+        if (ms3[c] < best) {
+            best = ms3[c];
+            pick = c;
+        }
+    }
+    // restore the state; keep the chosen schedule
+    if (!rc) {
+        *h->hst = saved;
+        if ((rc = copyAll(false)) == RIFT_OK) rc = pushState(h);
+    }
+    h->persistMax = rc ? keepPersist : (pick == 0 ? INT32_MAX : 0);
+    h->marchMin = rc ? keepMarch : marchOf[pick];
+    destroyGraph(h);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(scratch);
+    if (rc) return rc;
+    if (choice) *choice = pick;
+    if (ms_per_step)
+        for (int c = 0; c < 3; c++) ms_per_step[c] = ms3[c];
+    return RIFT_OK;
+}
+
 // ---------------------------------------------------------------- ensembles
 struct rift_ensemble {
     std::vector<rift_handle*> m;

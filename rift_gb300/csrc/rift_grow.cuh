@@ -85,8 +85,10 @@ __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) 
 
 // One pass: each CTA's chunk of strips appends its entries to the four lists
 // with one atomic per warp and list (the lists are sets: their order changes
-// no result), writes the new active flags, and the last CTA to finish
-// publishes the list sizes and clears the counters for the next step.
+// no result), writes the new active flags, folds the stale speeds of the
+// tiles not active this step into DevState.staleBits (the stale entries
+// ComputeTimestep's max includes, A5), and the last CTA to finish publishes
+// the list sizes and clears the counters for the next step.
 __device__ void growAppend(const Params& P) {
     DevState* s = P.st;
     const int tid = threadIdx.x, lane = tid & 31;
@@ -94,6 +96,7 @@ __device__ void growAppend(const Params& P) {
     stripChunk(P, s0, s1);
     int* const lists[GROW_LISTS] = {P.act, P.deact, P.inact, P.strips};
     unsigned long long cells = 0ull;
+    float smx = 0.f, smy = 0.f;
     for (int rb = s0; rb < s1; rb += STRIPS_PER_ROUND) {
         const GrowItem t = growItem(P, rb, s1);
         for (int q = 0; q < GROW_LISTS; q++) {
@@ -110,11 +113,21 @@ __device__ void growAppend(const Params& P) {
                 P.mx[t.b] = 0.f;
                 P.my[t.b] = 0.f;
             }
+            if (!t.v) {  // a tile not active this step: its stale speeds count for dt (A5)
+                smx = fmaxf(smx, P.mx[t.b]);
+                smy = fmaxf(smy, P.my[t.b]);
+            }
             P.prevAct[t.b] = (uint8_t)(t.v ? 1 : 0);
         }
     }
-    for (int o = 16; o > 0; o >>= 1) cells += __shfl_xor_sync(0xffffffffu, cells, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        cells += __shfl_xor_sync(0xffffffffu, cells, o);
+        smx = fmaxf(smx, __shfl_xor_sync(0xffffffffu, smx, o));
+        smy = fmaxf(smy, __shfl_xor_sync(0xffffffffu, smy, o));
+    }
     if (lane == 0 && cells) atomicAdd(&s->appendCells, cells);
+    if (lane == 0 && smx > 0.f) atomicMax(&s->staleBits[0], __float_as_uint(smx));
+    if (lane == 0 && smy > 0.f) atomicMax(&s->staleBits[1], __float_as_uint(smy));
     __syncthreads();
     if (tid == 0) {
         __threadfence();

@@ -246,31 +246,28 @@ __device__ __forceinline__ float blockMax(float v, float* red) {
     return r;
 }
 
-// Stale speed maxima of the tiles that are not active this step, over this
-// thread's grid-stride slice of the tile grid.
-__device__ __forceinline__ void staleMax(const Params& P, float& amx, float& amy) {
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < P.gridSize; b += gridDim.x * blockDim.x)
-        if (!P.prevAct[b]) {
-            amx = fmaxf(amx, P.mx[b]);
-            amy = fmaxf(amy, P.my[b]);
-        }
-}
 
 // ComputeTimestep's arithmetic (simulator.cu:540-566) from the maxima of
 // the tile speeds: dt with the reference's rounding points (fmaxf on the
 // scaled maxima, FP64 division), t += dt, and the step's entry in the
 // volume ledger.
-__device__ __forceinline__ void computeDt(const Params& P, DevState* st, double maxx, double maxy) {
+__device__ __forceinline__ double stepDt(const Params& P, const DevState* st, double maxx,
+                                         double maxy) {
     double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
     double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
     double dt = cx < cy ? cx : cy;
     if (st->t == 0.0) dt = (double)0.000001f;
+    return dt;
+}
+
+// The step's dt into the device state: dt_old, dt, t += dt, and the step's
+// entry in the volume ledger (both RK stages, or the Euler stage, apply each
+// source rate of this step for dt -- uniform rain on every interior cell,
+// the point sources, the gridded rain map at this step's factor).
+__device__ __forceinline__ void publishDt(const Params& P, DevState* st, double dt) {
     st->dt_old = st->dt;
     st->dt = dt;
     st->t = st->t + dt;
-    // volume ledger: both RK stages (or the Euler stage) apply each
-    // source rate of this step for dt -- uniform rain on every interior
-    // cell, the point sources, the gridded rain map at this step's factor
     double add = 0.0;
     if (P.flags & F_RAIN_U) add += (double)st->rain_rate * (double)(P.nx - 4) * (P.ny - 4);
     for (int k = 0; k < P.nsrc; k++) add += (double)P.srcRate[k];
@@ -281,30 +278,30 @@ __device__ __forceinline__ void computeDt(const Params& P, DevState* st, double 
     st->v_added += add * dt;
 }
 
-// Simulator::ComputeTimestep (simulator.cu:540-566) on device: block max of
-// stale and new tile speeds, one atomic per CTA; the last CTA to finish turns
-// the maxima into dt with the reference's rounding points (fmaxf on the
-// scaled maxima, FP64 division) and advances t.  tmx/tmy are the CTA's new
-// tile maxima, held by thread 0.
-__device__ __forceinline__ void finishDt(const Params& P, float amx, float amy, float tmx,
-                                         float tmy, float* red0, float* red1, bool* last) {
+__device__ __forceinline__ void computeDt(const Params& P, DevState* st, double maxx, double maxy) {
+    publishDt(P, st, stepDt(P, st, maxx, maxy));
+}
+
+// Simulator::ComputeTimestep (simulator.cu:540-566) on device: thread 0 of
+// each CTA adds the CTA's maxima of the new tile speeds (tmx, tmy) with one
+// atomic; the last CTA to finish turns them, with the stale maxima the grow
+// folded in, into dt with the reference's rounding points and advances t.
+__device__ __forceinline__ void finishDt(const Params& P, float tmx, float tmy, bool* last) {
     DevState* st = P.st;
     const int tid = threadIdx.x;
-    float bmx = blockMax(fmaxf(amx, tid == 0 ? tmx : 0.f), red0);
-    float bmy = blockMax(fmaxf(amy, tid == 0 ? tmy : 0.f), red1);
     if (tid == 0) {
-        // speeds are non-negative: their bit patterns order like the values
-        atomicMax(&st->max_bits[0], __float_as_uint(bmx));
-        atomicMax(&st->max_bits[1], __float_as_uint(bmy));
+        atomicMax(&st->max_bits[0], __float_as_uint(tmx));
+        atomicMax(&st->max_bits[1], __float_as_uint(tmy));
         __threadfence();
         *last = (atomicAdd(&st->ticket, 1u) == gridDim.x - 1);
     }
     __syncthreads();
     if (*last && tid == 0) {
         __threadfence();
-        double maxx = (double)__uint_as_float(atomicOr(&st->max_bits[0], 0u));
-        double maxy = (double)__uint_as_float(atomicOr(&st->max_bits[1], 0u));
-        computeDt(P, st, maxx, maxy);
+        // speeds are non-negative: their bit patterns order like the values
+        const unsigned bx = max(atomicOr(&st->max_bits[0], 0u), atomicExch(&st->staleBits[0], 0u));
+        const unsigned by = max(atomicOr(&st->max_bits[1], 0u), atomicExch(&st->staleBits[1], 0u));
+        computeDt(P, st, (double)__uint_as_float(bx), (double)__uint_as_float(by));
     }
 }
 
@@ -618,13 +615,11 @@ __global__ void __launch_bounds__(NT) k_speed_dt(const __grid_constant__ CUtenso
     __shared__ bool last;
     if (P.st->stop || useMarch(P)) return;
     tileInit(S, &tmA, &tmE);
-    float amx = 0.f, amy = 0.f;
-    staleMax(P, amx, amy);
     uint32_t ph[2] = {0u, 0u};
     float tmx = 0.f, tmy = 0.f;
     if (!speedTiles(S, &tmA, &tmE, P, P.st->nActive, ph, tmx, tmy)) return;
     __syncthreads();
-    finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
+    finishDt(P, tmx, tmy, &last);
     resyncDeactivated(P);
 }
 
@@ -697,6 +692,19 @@ __device__ __forceinline__ StageConsts stageConsts(const Params& P) {
     C.Uout = (STAGE == 1) ? P.B : P.A;
     C.Fin = (STAGE == 1) ? P.FA : P.FB;
     C.Fout = (STAGE == 1) ? P.FB : P.FA;
+    return C;
+}
+
+// stageConsts with the step's dt, previous dt and t given by the caller
+// (a caller that computed dt itself before the device state holds it).
+template <int STAGE>
+__device__ __forceinline__ StageConsts stageConstsAt(const Params& P, double dtNew, double dtOld,
+                                                     double tNew) {
+    StageConsts C = stageConsts<STAGE>(P);
+    C.dtNew = (float)dtNew;
+    C.dtSrc = (STAGE == 1) ? (float)dtOld : C.dtNew;
+    C.invDtSrc = 1.f / C.dtSrc;
+    C.tNew = tNew;
     return C;
 }
 
@@ -966,10 +974,11 @@ __device__ __forceinline__ void tileFlags(const Params& P, const StageConsts& C,
 // a TMA timeout (error recorded).
 template <int STAGE>
 __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensorMap* tmE,
-                           const Params& P, int nAct, uint32_t* ph) {
+                           const Params& P, int nAct, uint32_t* ph,
+                           const StageConsts* given = nullptr) {
     const int tid = threadIdx.x;
     tileFirst(S, tmIn, tmE, P, nAct);
-    const StageConsts C = stageConsts<STAGE>(P);
+    const StageConsts C = given ? *given : stageConsts<STAGE>(P);
     int bsel = 0;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];

@@ -107,8 +107,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nItems = P.st->nStrips;
     const StageConsts C = stageConsts<STAGE == 0 ? 1 : STAGE>(P);
-    float amx = 0.f, amy = 0.f, tmxAll = 0.f, tmyAll = 0.f;
-    if (STAGE == 0) staleMax(P, amx, amy);
+    float tmxAll = 0.f, tmyAll = 0.f;
     if (tid == 0) {
         prefetch_tmap(&tmIn);
         prefetch_tmap(&tmE);
@@ -318,8 +317,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
     }
     if (STAGE == 0) {
         __syncthreads();
-        __shared__ float red[2][MT / 32];
-        finishDt(P, amx, amy, tmxAll, tmyAll, red[0], red[1], &last);
+        finishDt(P, tmxAll, tmyAll, &last);
         resyncDeactivated(P);
     }
 }

@@ -113,12 +113,14 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
         RIFT_SYNC();
         const int nAct = st->nActive;  // published by the grow's last CTA
         nActPrev = nAct;
-        float amx = 0.f, amy = 0.f, tmx = 0.f, tmy = 0.f;
+        float tmx = 0.f, tmy = 0.f;
         if (nAct <= (int)gridDim.x) {
             // At most one tile per CTA: stage 1's fluxes of U^n are the first
             // ComputeFluxes of the step, so they give this step's tile speeds,
             // and the tile's divergence waits in registers (its staged block
-            // in shared memory) across the dt barrier.
+            // in shared memory) across the barrier.  After the barrier every
+            // CTA computes the step's dt from the maxima itself; CTA 0
+            // publishes it during stage 2, when no CTA reads the old value.
             const bool mine = (int)blockIdx.x < nAct;
             int tile = 0, bX, bY, i0 = 0, j0 = 0;
             float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f;
@@ -139,29 +141,44 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 if (tid == 0) {
                     P.mx[tile] = mxv;
                     P.my[tile] = myv;
-                    tmx = mxv;
-                    tmy = myv;
+                    atomicMax(&st->max_bits[0], __float_as_uint(mxv));
+                    atomicMax(&st->max_bits[1], __float_as_uint(myv));
                 }
                 __syncthreads();
             }
-            staleMax(P, amx, amy);
-            finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
             resyncDeactivated(P);
             RIFT_SYNC();
+            // dt of this step (Simulator::ComputeTimestep) in every CTA
+            const unsigned bx = max(ld_acquire_gpu(&st->max_bits[0]), ld_acquire_gpu(&st->staleBits[0]));
+            const unsigned by = max(ld_acquire_gpu(&st->max_bits[1]), ld_acquire_gpu(&st->staleBits[1]));
+            const double dtOld = st->dt;
+            const double dtNew = stepDt(P, st, (double)__uint_as_float(bx), (double)__uint_as_float(by));
+            const double tNew = st->t + dtNew;
             if (mine) {  // stage-1 update with this step's dt (Integrate_1_k)
-                const StageConsts C1 = stageConsts<1>(P);
+                const StageConsts C1 = stageConstsAt<1>(P, dtNew, dtOld, tNew);
                 const bool wetCell =
                     tileCellUpdate<1>(P, C1, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
                 tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
                 __syncthreads();
             }
             RIFT_SYNC();
+            if (blockIdx.x == 0 && tid == 0) {
+                publishDt(P, st, dtNew);
+                st->staleBits[0] = st->staleBits[1] = 0u;
+            }
+            const StageConsts C2 = stageConstsAt<2>(P, dtNew, dtOld, tNew);
+            if (!(fl & F_EULER)) {
+                if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph, &C2)) return;
+            } else {
+                commitTiles(P, nAct);
+            }
+            RIFT_SYNC();
+            continue;
         } else {
             // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1
-            staleMax(P, amx, amy);
             if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
             __syncthreads();
-            finishDt(P, amx, amy, tmx, tmy, S.red[0], S.red[1], &last);
+            finishDt(P, tmx, tmy, &last);
             resyncDeactivated(P);
             RIFT_SYNC();
             if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph)) return;

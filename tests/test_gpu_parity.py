@@ -119,3 +119,26 @@ def test_one_step_from_identical_snapshot(engine_api, oracle_api, name, schedule
     assert np.array_equal(ae, ao)
     assert abs(t_e[0] - t_o[0]) <= 1e-6 * max(1.0, t_o[0])
     _close(w_e, w_o, f"{name} snapshot step")
+
+
+def test_autotune_restores_state(engine_api):
+    """The autotuner times the three schedules from the current state, puts
+    the state back exactly and keeps the fastest; the run then goes on as
+    if nothing had happened."""
+    fx, case = FX.load("rain")
+    a = FX.start(capi.Sim(case, api=engine_api), fx)
+    b = FX.start(capi.Sim(case, api=engine_api), fx)
+    a.run(6)
+    b.run(6)
+    choice, ms = b.autotune(8)
+    assert choice in (0, 1, 2)
+    assert np.isfinite(ms[choice]) and ms[choice] == np.nanmin(ms)
+    assert np.array_equal(a.field("W"), b.field("W"))
+    assert a.time() == b.time()
+    (wa, aa), (wb, ab) = a.tiles(), b.tiles()
+    assert np.array_equal(wa, wb) and np.array_equal(aa, ab)
+    a.run(12)
+    b.run(12)
+    (wa, aa), (wb, ab) = a.tiles(), b.tiles()
+    assert np.array_equal(wa, wb) and np.array_equal(aa, ab)
+    _close(b.field("W"), a.field("W"), "after autotune")
