@@ -18,9 +18,11 @@ timed steps see a developed flood, then W warm-up and K timed steps run.
 value  = domain cell-updates/s = interior cells x K / device time (CUDA
          events on the engine's stream around the K steps: one persistent
          launch, or K step-graph launches);
-e2e    = the same metric through the C ABI with host buffers: static fields
-         uploaded from host arrays, K rift_step calls (each returns t and dt
-         to the host), the depth map read back, all inside the timed region;
+e2e    = the same metric through the C ABI with host buffers: the state
+         uploaded from host arrays, one rift_run call over the K steps (as a
+         caller of RunSimulation makes it), the depth map read back, all
+         inside the timed region; e2e.per_step_calls repeats it with one
+         rift_step call per step (t and dt returned to the host each step);
 roofline: HBM bytes per active cell-update (algorithmic, FP32 words of the
          reference data model) x active cell-updates / device time, against
          the measured copy bandwidth.
@@ -202,19 +204,28 @@ def run_ours(args, device=0, sync=None):
     snap = sim.snapshot()
     for _ in range(args.warmup):
         sim.step()
-    e2e_steps = min(args.steps, 200)
-    h2d = 0
-    t0 = time.perf_counter()
-    sim.load_snapshot(snap)  # host arrays -> device (state upload)
-    h2d += sum(snap[k].nbytes for k in ("w", "hu", "hv", "wet", "active", "mx", "my"))
+    e2e_steps = args.steps
+    h2d = sum(snap[k].nbytes for k in ("w", "hu", "hv", "wet", "active", "mx", "my"))
     if "F" in snap:
         h2d += snap["F"].nbytes
-    for _ in range(e2e_steps):
-        sim.step()
+    # one rift_run call over the steps, as a caller of RunSimulation makes it
+    t0 = time.perf_counter()
+    sim.load_snapshot(snap)  # host arrays -> device (state upload)
+    sim.run(e2e_steps)
     depth = sim.field("H")
     t_e2e = time.perf_counter() - t0
     e2e_value = interior * e2e_steps / t_e2e
-    d2h = depth.nbytes + 16 * e2e_steps
+    d2h = depth.nbytes + 24
+    # one rift_step call per step (state mirror synchronised after each)
+    call_steps = min(args.steps, 200)
+    t0 = time.perf_counter()
+    sim.load_snapshot(snap)
+    for _ in range(call_steps):
+        sim.step()
+    sim.field("H")
+    t_calls = time.perf_counter() - t0
+    e2e_calls = {"value": interior * call_steps / t_calls, "steps": call_steps,
+                 "us_per_call": 1e6 * t_calls / call_steps}
 
     # ---- device-timed run (inputs resident) --------------------------------
     sim.load_snapshot(snap)
@@ -282,7 +293,8 @@ def run_ours(args, device=0, sync=None):
                    else "inputs smaller than L2; steps are back to back",
                    "parallelism": "replicas only"},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / e2e_steps,
-                "d2h_bytes_per_step": d2h / e2e_steps, "setup_s": t_setup},
+                "d2h_bytes_per_step": d2h / e2e_steps, "setup_s": t_setup,
+                "per_step_calls": e2e_calls},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "peak_kind": peak_kind, "bytes_per_active_cell_update": bytes_per,

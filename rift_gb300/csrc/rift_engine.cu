@@ -64,6 +64,7 @@ struct rift_handle {
     int gridPersist = 0;   // CTAs of the cooperative step kernel (0: unavailable)
     int persistMax = 0;    // it runs while the active tiles are at most this many
     GridBar* gbar = nullptr;
+    int* owner = nullptr;  // [gridSize] tile table of the persistent loop
     long long persistSteps = 0, graphSteps = 0;  // steps run by each path (diagnostics)
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
@@ -90,6 +91,10 @@ struct rift_handle {
     std::vector<double> Bref, BC, h0_;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
+    // one persistent step with its state copies, for rift_step
+    cudaGraphExec_t stepExec = nullptr;
+    int stepGrid = 0;
+    bool stepGraphBroken = false;
     bool haveStatic = false, inited = false;
     std::string err;
 
@@ -162,6 +167,7 @@ Params makeParams(rift_handle* h) {
     P.marchMin = h->marchMin;
     P.persistMax = h->persistMax;
     P.gbar = h->gbar;
+    P.owner = h->owner;
     P.mx = h->mx;
     P.my = h->my;
     P.srcIdx = h->srcIdx;
@@ -194,8 +200,10 @@ int encodeMap(rift_handle* h, CUtensorMap* tm, float* base, int nfields, int box
 void destroyGraph(rift_handle* h) {
     if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
     if (h->graph) cudaGraphDestroy(h->graph);
+    if (h->stepExec) cudaGraphExecDestroy(h->stepExec);
     h->graphExec = nullptr;
     h->graph = nullptr;
+    h->stepExec = nullptr;
 }
 
 // The launch sequence of one step (captured into the graph).
@@ -466,6 +474,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     if (coop && occ > 0) {
         h->gridPersist = std::min(h->numSMs * occ, PERSIST_MAX_CTAS);
         CUDA_TRY(h, cudaMalloc(&h->gbar, sizeof(GridBar)));
+        CUDA_TRY(h, cudaMalloc(&h->owner, (size_t)G * 4));
     }
     h->gridGrow = std::max(1, std::min(NS, h->numSMs * 4));
     h->persistMax = h->gridPersist > 0 ? h->marchMin * STRIP_TX * STRIP_TY : 0;
@@ -701,6 +710,7 @@ int rift_set_persistent(rift_handle* h, int32_t max_active_tiles) {
     }
     h->persistMax = max_active_tiles >= 0 ? max_active_tiles
                                           : h->marchMin * STRIP_TX * STRIP_TY;
+    destroyGraph(h);  // the step graph holds the bound
     return RIFT_OK;
 }
 
@@ -738,13 +748,17 @@ namespace {
 // grid is a whole number of CTAs per SM, enough for one active tile per CTA
 // at the last known count (up to full occupancy): a smaller grid makes each
 // grid barrier cheaper.
-int launchPersist(rift_handle* h, int nsteps) {
-    CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream));
-    Params P = makeParams(h);
+int persistGrid(const rift_handle* h) {
     // before the first step the count is unknown: full occupancy
     const int perSM = h->hst->nActive > 0 ? (h->hst->nActive + h->numSMs - 1) / h->numSMs
                                           : h->gridPersist / h->numSMs;
-    const int grid = std::max(1, std::min(h->gridPersist, h->numSMs * perSM));
+    return std::max(1, std::min(h->gridPersist, h->numSMs * perSM));
+}
+
+int launchPersist(rift_handle* h, int nsteps) {
+    CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream));
+    Params P = makeParams(h);
+    const int grid = persistGrid(h);
     void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
     CUDA_TRY(h, cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0,
                                             h->stream));
@@ -793,6 +807,60 @@ int runSteps(rift_handle* h, int nsteps, bool* mirrorCurrent) {
 
 }  // namespace
 
+namespace {
+// rift_step on the persistent loop as one graph: state push, barrier reset,
+// the one-step cooperative launch, state pull -- one launch and one wait
+// per step.  Rebuilt when the grid changes; false if the graph cannot be
+// made (the caller launches directly).
+bool stepGraph(rift_handle* h, int& rc) {
+    rc = RIFT_OK;
+    if (h->stepGraphBroken) return false;
+    const int grid = persistGrid(h);
+    if (h->stepExec && h->stepGrid != grid) {
+        cudaGraphExecDestroy(h->stepExec);
+        h->stepExec = nullptr;
+    }
+    if (!h->stepExec) {
+        Params P = makeParams(h);
+        int one = 1;
+        void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&one};
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            h->stepGraphBroken = true;
+            cudaGetLastError();
+            return false;
+        }
+        cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, h->stream);
+        cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream);
+        cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0, h->stream);
+        cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream);
+        cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (e != cudaSuccess || !g || cudaGraphInstantiate(&h->stepExec, g, 0) != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            h->stepExec = nullptr;
+            h->stepGraphBroken = true;
+            cudaGetLastError();
+            return false;
+        }
+        cudaGraphDestroy(g);
+        h->stepGrid = grid;
+    }
+    const int before = h->hst->steps_done;
+    cudaError_t e = cudaGraphLaunch(h->stepExec, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        rc = fail(h, RIFT_ERR_CUDA, std::string("step graph: ") + cudaGetErrorString(e));
+        return true;
+    }
+    if (h->hst->error) {
+        rc = fail(h, RIFT_ERR_CUDA, "device wait timed out");
+        return true;
+    }
+    h->persistSteps += h->hst->steps_done - before;
+    return true;
+}
+}  // namespace
+
 int rift_run(rift_handle* h, int32_t nsteps, double t_stop, double* t, double* dt,
              int32_t* steps_done) {
     if (!h || nsteps < 0) return RIFT_ERR_ARG;
@@ -802,6 +870,14 @@ int rift_run(rift_handle* h, int32_t nsteps, double t_stop, double* t, double* d
     h->hst->steps_done = 0;
     int rc;
     bool current = false;
+    if (nsteps == 1 && h->persistMax > 0 && h->hst->nActive <= h->persistMax &&
+        stepGraph(h, rc)) {
+        if (rc) return rc;
+        if (t) *t = h->hst->t;
+        if (dt) *dt = h->hst->dt;
+        if (steps_done) *steps_done = h->hst->steps_done;
+        return RIFT_OK;
+    }
     if ((rc = pushStateAsync(h)) || (rc = runSteps(h, nsteps, &current))) return rc;
     if (!current && (rc = pullState(h))) return rc;
     if (t) *t = h->hst->t;
@@ -1317,7 +1393,7 @@ void rift_destroy(rift_handle* h) {
     for (int k = 0; k < 3; k++)
         for (int q = 0; q < 2; q++)
             if (h->maps[k][q]) cudaFree(h->maps[k][q]);
-    for (void* p : {(void*)h->gbar,
+    for (void* p : {(void*)h->gbar, (void*)h->owner,
                     (void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
                     (void*)h->act, (void*)h->deact,
                     (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,

@@ -87,8 +87,11 @@ __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) 
 // with one atomic per warp and list (the lists are sets: their order changes
 // no result), writes the new active flags, folds the stale speeds of the
 // tiles not active this step into DevState.staleBits (the stale entries
-// ComputeTimestep's max includes, A5), and the last CTA to finish publishes
-// the list sizes and clears the counters for the next step.
+// ComputeTimestep's max includes, A5).  With PUBLISH the last CTA to finish
+// publishes the list sizes and clears the counters for the next step;
+// without, the caller reads the counters after a grid barrier and publishes
+// them later (publishGrow).
+template <bool PUBLISH = true>
 __device__ void growAppend(const Params& P) {
     DevState* s = P.st;
     const int tid = threadIdx.x, lane = tid & 31;
@@ -99,13 +102,17 @@ __device__ void growAppend(const Params& P) {
     float smx = 0.f, smy = 0.f;
     for (int rb = s0; rb < s1; rb += STRIPS_PER_ROUND) {
         const GrowItem t = growItem(P, rb, s1);
+        unsigned bal[GROW_LISTS];
+        for (int q = 0; q < GROW_LISTS; q++) bal[q] = __ballot_sync(0xffffffffu, t.f[q]);
+        // lane q reserves the warp's entries of list q: the four atomics are
+        // in flight together
+        const unsigned mineBal = lane == 0 ? bal[0] : lane == 1 ? bal[1] : lane == 2 ? bal[2] : bal[3];
+        int base = 0;
+        if (lane < GROW_LISTS && mineBal) base = atomicAdd(&s->appendCnt[lane], __popc(mineBal));
+        const unsigned below = (1u << lane) - 1u;
         for (int q = 0; q < GROW_LISTS; q++) {
-            const unsigned bal = __ballot_sync(0xffffffffu, t.f[q]);
-            if (!bal) continue;  // warp-uniform
-            int base = 0;
-            if (lane == 0) base = atomicAdd(&s->appendCnt[q], __popc(bal));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (t.f[q]) lists[q][base + __popc(bal & ((1u << lane) - 1u))] = q == 3 ? t.strip : t.b;
+            const int bq = __shfl_sync(0xffffffffu, base, q);
+            if (t.f[q]) lists[q][bq + __popc(bal[q] & below)] = q == 3 ? t.strip : t.b;
         }
         if (t.f[0]) cells += (unsigned long long)t.cells;
         if (t.b >= 0) {
@@ -128,6 +135,7 @@ __device__ void growAppend(const Params& P) {
     if (lane == 0 && cells) atomicAdd(&s->appendCells, cells);
     if (lane == 0 && smx > 0.f) atomicMax(&s->staleBits[0], __float_as_uint(smx));
     if (lane == 0 && smy > 0.f) atomicMax(&s->staleBits[1], __float_as_uint(smy));
+    if (!PUBLISH) return;
     __syncthreads();
     if (tid == 0) {
         __threadfence();
@@ -141,6 +149,18 @@ __device__ void growAppend(const Params& P) {
             atomicExch(&s->growTicket, 0u);
         }
     }
+}
+
+// The grow's counters into the published list sizes, cleared for the next
+// step (one thread; no CTA may append or read the counters meanwhile).
+__device__ __forceinline__ void publishGrow(DevState* s) {
+    s->nActive = s->appendCnt[0];
+    s->nDeact = s->appendCnt[1];
+    s->nInact = s->appendCnt[2];
+    s->nStrips = s->appendCnt[3];
+    s->activeCells += s->appendCells;
+    for (int q = 0; q < GROW_LISTS; q++) s->appendCnt[q] = 0;
+    s->appendCells = 0ull;
 }
 
 // Graph path: the stop test, the start of the step and the grow in one

@@ -116,6 +116,7 @@ struct Params {
     int marchMin;      // active strips from which the march kernels run
     int persistMax;    // the persistent step kernel runs while active tiles <= this
     struct GridBar* gbar;            // grid barrier of the persistent kernel
+    int* owner;        // [gridSize] tile -> CTA of the persistent loop's tile table, or -1
     float* mx;
     float* my;
     const int* srcIdx;      // flat h-grid indices j*nx+i
@@ -251,13 +252,17 @@ __device__ __forceinline__ float blockMax(float v, float* red) {
 // the tile speeds: dt with the reference's rounding points (fmaxf on the
 // scaled maxima, FP64 division), t += dt, and the step's entry in the
 // volume ledger.
-__device__ __forceinline__ double stepDt(const Params& P, const DevState* st, double maxx,
-                                         double maxy) {
+__device__ __forceinline__ double stepDtAt(const Params& P, double t, double maxx, double maxy) {
     double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
     double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
     double dt = cx < cy ? cx : cy;
-    if (st->t == 0.0) dt = (double)0.000001f;
+    if (t == 0.0) dt = (double)0.000001f;
     return dt;
+}
+
+__device__ __forceinline__ double stepDt(const Params& P, const DevState* st, double maxx,
+                                         double maxy) {
+    return stepDtAt(P, st->t, maxx, maxy);
 }
 
 // The step's dt into the device state: dt_old, dt, t += dt, and the step's
@@ -270,7 +275,13 @@ __device__ __forceinline__ void publishDt(const Params& P, DevState* st, double 
     st->t = st->t + dt;
     double add = 0.0;
     if (P.flags & F_RAIN_U) add += (double)st->rain_rate * (double)(P.nx - 4) * (P.ny - 4);
-    for (int k = 0; k < P.nsrc; k++) add += (double)P.srcRate[k];
+    if (P.serN[2] > 0) {
+        // every source holds the same float rate: the sequential FP64 sum of
+        // nsrc copies is exact (under 2^29 terms), so it equals the product
+        add += (double)P.nsrc * (double)P.srcRate[0];
+    } else {
+        for (int k = 0; k < P.nsrc; k++) add += (double)P.srcRate[k];
+    }
     if ((P.flags & F_RAIN_G) && P.mapMode[0] != 0) {
         add += st->rain_sum[0];
         if (P.mapMode[0] == 2) add += (double)st->factor[0] * (st->rain_sum[1] - st->rain_sum[0]);
@@ -338,9 +349,12 @@ __device__ __forceinline__ void resyncTile(const Params& P, int tile) {
     }
 }
 
-__device__ __forceinline__ void resyncDeactivated(const Params& P) {
-    const int nDe = P.st->nDeact;
+__device__ __forceinline__ void resyncDeactivated(const Params& P, int nDe) {
     for (int k = blockIdx.x; k < nDe; k += gridDim.x) resyncTile(P, P.deact[k]);
+}
+
+__device__ __forceinline__ void resyncDeactivated(const Params& P) {
+    resyncDeactivated(P, P.st->nDeact);
 }
 
 // Schedule: the march kernels (strips of 7 x 2 tiles) run when at least
@@ -403,38 +417,72 @@ __device__ __forceinline__ bool tileAcquire(StageSmem& S, const CUtensorMap* tmI
 // divided in place every step.  IEEE float ops (_rn intrinsics) keep the host's
 // arithmetic (no contraction, exact division).
 // Called by one whole warp: the lanes test the intervals [T[i], T[i+1]) in
-// parallel; the last interval holding t wins, as in the sequential loop.
+// parallel; the last interval holding t wins, as in the sequential loop.  A
+// lane loads both ends of its interval and both rates at once, so a series of
+// up to 33 points costs one round trip to memory.
 __device__ __forceinline__ float seriesInterp(const float* T, const float* R, int n, float t,
                                               float cur) {
     const int lane = threadIdx.x & 31;
-    int found = -1;
+    bool found = false;
+    float T0f = 0.f, T1f = 0.f, R0f = 0.f, R1f = 0.f;
     for (int base = 0; base + 1 < n; base += 32) {
         const int i = base + lane;
-        bool m = false;
-        if (i + 1 < n) m = (t >= T[i] && t < T[i + 1]);
+        float T0 = 0.f, T1 = 0.f, R0 = 0.f, R1 = 0.f;
+        if (i + 1 < n) {
+            T0 = T[i];
+            T1 = T[i + 1];
+            R0 = R[i];
+            R1 = R[i + 1];
+        }
+        const bool m = (i + 1 < n) && t >= T0 && t < T1;
         const unsigned bal = __ballot_sync(0xffffffffu, m);
-        if (bal) found = base + 31 - __clz(bal);
+        if (bal) {  // warp-uniform
+            const int src = 31 - __clz(bal);
+            found = true;
+            T0f = __shfl_sync(0xffffffffu, T0, src);
+            T1f = __shfl_sync(0xffffffffu, T1, src);
+            R0f = __shfl_sync(0xffffffffu, R0, src);
+            R1f = __shfl_sync(0xffffffffu, R1, src);
+        }
     }
-    if (found >= 0) {
-        const int i = found;
-        float num = __fsub_rn(R[i + 1], R[i]);
-        float den = __fsub_rn(T[i + 1], T[i]);
-        cur = __fadd_rn(R[i], __fmul_rn(__fdiv_rn(num, den), __fsub_rn(t, T[i])));
+    if (found) {
+        float num = __fsub_rn(R1f, R0f);
+        float den = __fsub_rn(T1f, T0f);
+        cur = __fadd_rn(R0f, __fmul_rn(__fdiv_rn(num, den), __fsub_rn(t, T0f)));
     }
     return cur;
 }
 
-// Start of a step, by one whole warp: reset of the step's reductions, the
-// uniform source rates at float(t), the map factors that follow t.
-__device__ void beginStep(const Params& P, DevState* s) {
+// Start of a step, part 1, by one thread: reset of the step's reductions and
+// the map factors that follow t.  Runs before the step's grow.
+__device__ __forceinline__ void beginStepResets(DevState* s) {
+    s->stop = 0;
+    s->steps_done += 1;
+    s->max_bits[0] = 0u;
+    s->max_bits[1] = 0u;
+    s->ticket = 0u;
+    // map factor following t (GridSeries::update computes it at the end
+    // of the previous step from the same t, GridSeries.cu:398)
+    for (int w = 0; w < 3; w++)
+        if (s->map_timed[w])
+            s->factor[w] = (float)((s->t - s->map_t0[w]) / (s->map_t1[w] - s->map_t0[w]));
+}
+
+// Start of a step, part 2, by one whole warp: the uniform source rates at
+// float(t).  Only the cell updates and the volume ledger read them, so it
+// may run any time between the previous step's stage 2 and this step's
+// stage 1.  The FP64 conversion of the hydrograph runs in one lane.
+__device__ void beginStepRates(const Params& P, DevState* s) {
     const int lane = threadIdx.x & 31;
     const float tf = (float)s->t;
     if (P.serN[2] > 0) {  // hydrograph, cfs -> m^3/s -> m/s per source cell
         float v = seriesInterp(P.serT + 2 * MAX_SERIES, P.serR + 2 * MAX_SERIES, P.serN[2], tf,
                                s->ser_interp[2]);
         v = __fdiv_rn(v, 35.3147f);
-        const double r = (double)v / P.dxd / P.dyd / (double)P.nsrc;
-        for (int k = lane; k < P.nsrc; k += 32) P.srcRate[k] = (float)r;
+        float r = 0.f;
+        if (lane == 0) r = (float)((double)v / P.dxd / P.dyd / (double)P.nsrc);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        for (int k = lane; k < P.nsrc; k += 32) P.srcRate[k] = r;
         if (lane == 0) s->ser_interp[2] = v;
     }
     if (P.serN[0] > 0) {  // hyetograph, mm/hr -> m/s
@@ -454,18 +502,12 @@ __device__ void beginStep(const Params& P, DevState* s) {
             s->drain_rate = v;
         }
     }
-    if (lane == 0) {
-        s->stop = 0;
-        s->steps_done += 1;
-        s->max_bits[0] = 0u;
-        s->max_bits[1] = 0u;
-        s->ticket = 0u;
-        // map factor following t (GridSeries::update computes it at the end
-        // of the previous step from the same t, GridSeries.cu:398)
-        for (int w = 0; w < 3; w++)
-            if (s->map_timed[w])
-                s->factor[w] = (float)((s->t - s->map_t0[w]) / (s->map_t1[w] - s->map_t0[w]));
-    }
+}
+
+// Start of a step, by one whole warp: both parts.
+__device__ void beginStep(const Params& P, DevState* s) {
+    beginStepRates(P, s);
+    if ((threadIdx.x & 31) == 0) beginStepResets(s);
 }
 
 // ---------------------------------------------------------------- k_track
@@ -951,11 +993,13 @@ __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConst
 
 // Tile flags (stage 2, or stage 1 in Euler mode) and stage-2 tile speeds.
 template <int STAGE>
-__device__ __forceinline__ void tileFlags(const Params& P, const StageConsts& C, StageSmem& S,
+__device__ __forceinline__ bool tileFlags(const Params& P, const StageConsts& C, StageSmem& S,
                                           int tile, bool wetCell, float spx, float spy) {
+    bool wetTile = false;
     if (STAGE == 2 || C.euler) {
         bool any = __syncthreads_or(wetCell);
-        if (threadIdx.x == 0) P.wet[tile] = (uint8_t)((!(C.fl & F_TILE_ACC)) || any);
+        wetTile = (!(C.fl & F_TILE_ACC)) || any;
+        if (threadIdx.x == 0) P.wet[tile] = (uint8_t)wetTile;
     }
     if (STAGE == 2) {
         float mxv = blockMax(spx, S.red[0]);
@@ -965,6 +1009,7 @@ __device__ __forceinline__ void tileFlags(const Params& P, const StageConsts& C,
             P.my[tile] = myv;
         }
     }
+    return wetTile;  // the tile's new wet flag (stage 2 or Euler), else false
 }
 
 // STAGE 1: reads U^n (A) -> writes U* (B), F* (FB).

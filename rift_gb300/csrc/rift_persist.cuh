@@ -30,10 +30,24 @@ namespace rift {
 
 constexpr int PERSIST_MAX_CTAS = 4096;
 
-// Grid barrier state: one arrival counter on its own 128-byte line.
+// Grid barrier state: one arrival counter on its own 128-byte line; then
+// the tile table of the persistent loop (cleared with the counter before
+// every launch).
 struct GridBar {
     unsigned count[32];
+    int freeTop;    // entries of freeStack
+    int overflow;   // a claim found no free CTA: the table is void
+    int ownedCnt;   // owned tiles found active this step
+    int schedCnt;   // scheduled tiles found by the scan this step
+    int slotTile[PERSIST_MAX_CTAS];   // CTA -> its tile, or -1
+    int freeStack[PERSIST_MAX_CTAS];  // CTAs without a tile
 };
+
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     unsigned v;
@@ -74,17 +88,155 @@ __device__ bool gridSync(GridBar* gb, unsigned& target, DevState* st) {
     return __syncthreads_and(ok) != 0;
 }
 
+// ------------------------------------------------------------ tile table
+// With one scheduled tile per CTA and no tracking (no gridded rain or surge)
+// and RK2, the loop keeps the tile -> CTA assignment from step to step
+// instead of compacting the active set behind a grid barrier:
+//   - at the start of a step each CTA tests its own tile (active iff it or a
+//     4-neighbour is wet, tile 0 always) and gives the tile up if inactive;
+//   - in the same phase a scan over all tiles writes the active flags, folds
+//     the stale speeds of inactive tiles, re-syncs U* on deactivated tiles
+//     and counts the scheduled tiles;
+//   - a tile that turns wet in stage 2 gives a CTA to each neighbour with
+//     interior cells that holds none.  A tile becomes active only next to a
+//     tile that just turned wet (the others were active already), so the
+//     table holds the next step's scheduled set.
+// The owned active tiles are counted against the scan every step (a
+// mismatch is an error, never a silent result).  A claim that finds no free
+// CTA voids the table: the loop returns to the grow, and rebuilds the table
+// from the grow's list once the active set fits the grid again.
+
+// Rebuild, grow phase: no tile holds a CTA.
+__device__ __forceinline__ void tableClear(const Params& P) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < P.gridSize; b += gridDim.x * blockDim.x)
+        P.owner[b] = -1;
+}
+
+// Rebuild, after the grow's barrier (thread 0): CTA c takes act[c] or joins
+// the free stack.
+__device__ __forceinline__ void tableBuild(const Params& P, int nAct, int tile) {
+    GridBar* T = P.gbar;
+    const int c = blockIdx.x;
+    T->slotTile[c] = tile;
+    if (tile >= 0)
+        P.owner[tile] = c;
+    else
+        T->freeStack[c - nAct] = c;
+    if (c == 0) {
+        T->freeTop = (int)gridDim.x - nAct;
+        T->overflow = 0;
+        T->ownedCnt = 0;
+        T->schedCnt = 0;
+    }
+}
+
+// Table step, flux phase: active flags, stale speeds, zero speeds of active
+// tiles without interior cells, U* re-sync of deactivated tiles and the
+// scheduled count over this CTA's chunk of tiles (what the grow does, less
+// the lists).  deList/deCount: shared scratch (NT entries, count 0).
+__device__ void scanTiles(const Params& P, int* deList, int* deCount) {
+    DevState* s = P.st;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int per = (P.gridSize + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int b0 = min(P.gridSize, (int)blockIdx.x * per), b1 = min(P.gridSize, b0 + per);
+    int sched = 0;
+    unsigned long long cells = 0ull;
+    float smx = 0.f, smy = 0.f;
+    for (int base = b0; base < b1; base += blockDim.x) {
+        const int b = base + tid;
+        bool de = false;
+        if (b < b1) {
+            const bool v = tileGrows(P, b);
+            const int nc = tileCells(P, b);
+            de = P.prevAct[b] && !v;
+            if (v && nc > 0) {
+                sched++;
+                cells += (unsigned long long)nc;
+            }
+            if (v && nc == 0) {
+                P.mx[b] = 0.f;
+                P.my[b] = 0.f;
+            }
+            if (!v) {  // stale speeds count for dt (A5)
+                smx = fmaxf(smx, P.mx[b]);
+                smy = fmaxf(smy, P.my[b]);
+            }
+            P.prevAct[b] = (uint8_t)(v ? 1 : 0);
+        }
+        const int nde = __syncthreads_count(de);
+        if (nde) {  // rare: re-sync U* on this round's deactivated tiles
+            if (de) deList[atomicAdd(deCount, 1)] = b;
+            __syncthreads();
+            for (int k = 0; k < nde; k++) resyncTile(P, deList[k]);
+            __syncthreads();
+            if (tid == 0) *deCount = 0;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sched += __shfl_xor_sync(0xffffffffu, sched, o);
+        cells += __shfl_xor_sync(0xffffffffu, cells, o);
+        smx = fmaxf(smx, __shfl_xor_sync(0xffffffffu, smx, o));
+        smy = fmaxf(smy, __shfl_xor_sync(0xffffffffu, smy, o));
+    }
+    if (lane == 0) {
+        if (sched) atomicAdd(&P.gbar->schedCnt, sched);
+        if (cells) atomicAdd(&s->appendCells, cells);
+        if (smx > 0.f) atomicMax(&s->staleBits[0], __float_as_uint(smx));
+        if (smy > 0.f) atomicMax(&s->staleBits[1], __float_as_uint(smy));
+    }
+}
+
+// Table step, flux phase (thread 0): this CTA gives up its inactive tile.
+__device__ __forceinline__ void tableRelease(const Params& P, int tile) {
+    GridBar* T = P.gbar;
+    P.owner[tile] = -1;
+    T->slotTile[blockIdx.x] = -1;
+    T->freeStack[atomicAdd(&T->freeTop, 1)] = blockIdx.x;
+}
+
+// Stage 2 (threads 0..3, one neighbour each): `tile` turned wet; each
+// neighbour with interior cells and no CTA gets one from the free stack.
+__device__ __forceinline__ void tableClaim(const Params& P, int tile) {
+    const int q = threadIdx.x;
+    const int bX = tile % P.nBX, bY = tile / P.nBX;
+    int nb = -1;
+    if (q == 0 && bX > 0) nb = tile - 1;
+    if (q == 1 && bX < P.nBX - 1) nb = tile + 1;
+    if (q == 2 && bY > 0) nb = tile - P.nBX;
+    if (q == 3 && bY < P.nBY - 1) nb = tile + P.nBX;
+    if (nb < 0 || tileCells(P, nb) == 0) return;
+    if (atomicCAS(&P.owner[nb], -1, -2) != -1) return;  // held, or claimed by another tile
+    GridBar* T = P.gbar;
+    const int k = atomicSub(&T->freeTop, 1) - 1;
+    if (k < 0) {
+        atomicExch(&T->overflow, 1);
+        return;
+    }
+    const int c = T->freeStack[k];
+    P.owner[nb] = c;
+    T->slotTile[c] = nb;
+}
+
 // The step loop.  maxSteps: steps to attempt in this launch.
+//
+// Work off the critical path goes to the spare CTA (the last one; it holds
+// no tile when the grid is larger than the active set): the step's source
+// rates during the flux phase, the dt bookkeeping and the grow's counts
+// during stage 2.  Every CTA reads the grow's counters itself after the
+// grow's barrier, so the grow needs no last-CTA hand-off.
 __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUtensorMap tmA,
                                                 const __grid_constant__ CUtensorMap tmB,
                                                 const __grid_constant__ CUtensorMap tmE, Params P,
                                                 int maxSteps) {
     __shared__ StageSmem S;
     __shared__ bool last;
+    __shared__ StageConsts sC[2];
+    __shared__ double sDt;
     DevState* st = P.st;
     const int tid = threadIdx.x;
     const uint32_t fl = P.flags;
     const bool track = (fl & (F_RAIN_G | F_SURGE)) != 0;
+    const bool spare = blockIdx.x == gridDim.x - 1;
     tileInit(S, &tmA, &tmE);
     if (tid == 0) prefetch_tmap(&tmB);
     uint32_t ph[2] = {0u, 0u};
@@ -108,29 +260,33 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             trackTiles(P);
             RIFT_SYNC();
         }
-        if (blockIdx.x == 0 && tid < 32) beginStep(P, st);
-        growAppend(P);
+        if (blockIdx.x == 0 && tid == 0) beginStepResets(st);
+        growAppend<false>(P);
         RIFT_SYNC();
-        const int nAct = st->nActive;  // published by the grow's last CTA
+        const int nAct = (int)ld_relaxed_gpu((const unsigned*)&st->appendCnt[0]);
+        const int nDe = (int)ld_relaxed_gpu((const unsigned*)&st->appendCnt[1]);
         nActPrev = nAct;
-        float tmx = 0.f, tmy = 0.f;
         if (nAct <= (int)gridDim.x) {
             // At most one tile per CTA: stage 1's fluxes of U^n are the first
             // ComputeFluxes of the step, so they give this step's tile speeds,
             // and the tile's divergence waits in registers (its staged block
             // in shared memory) across the barrier.  After the barrier every
-            // CTA computes the step's dt from the maxima itself; CTA 0
+            // CTA computes the step's dt from the maxima itself; the spare CTA
             // publishes it during stage 2, when no CTA reads the old value.
             const bool mine = (int)blockIdx.x < nAct;
             int tile = 0, bX, bY, i0 = 0, j0 = 0;
             float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f;
+            // t and dt of the previous step: published before the last barrier
+            double tCur = 0.0, dtOld = 0.0;
+            if (tid == 0) {
+                tCur = st->t;
+                dtOld = st->dt;
+            }
+            tileFirst(S, &tmA, &tmE, P, nAct);
             if (mine) {
                 tile = P.act[blockIdx.x];
                 tileOrigin(P, tile, bX, bY, i0, j0);
                 tilePrefetch<1>(P, stageConsts<1>(P), i0, j0, pre);
-            }
-            tileFirst(S, &tmA, &tmE, P, nAct);
-            if (mine) {
                 if (!tileAcquire(S, &tmA, &tmE, P, 0, ph, nAct, nAct)) {
                     if (tid == 0) atomicOr(&st->error, ERR_TMA_TIMEOUT);
                     return;
@@ -146,49 +302,84 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 }
                 __syncthreads();
             }
-            resyncDeactivated(P);
+            if (spare && tid < 32) beginStepRates(P, st);
+            resyncDeactivated(P, nDe);
             RIFT_SYNC();
-            // dt of this step (Simulator::ComputeTimestep) in every CTA
-            const unsigned bx = max(ld_acquire_gpu(&st->max_bits[0]), ld_acquire_gpu(&st->staleBits[0]));
-            const unsigned by = max(ld_acquire_gpu(&st->max_bits[1]), ld_acquire_gpu(&st->staleBits[1]));
-            const double dtOld = st->dt;
-            const double dtNew = stepDt(P, st, (double)__uint_as_float(bx), (double)__uint_as_float(by));
-            const double tNew = st->t + dtNew;
+            // dt of this step (Simulator::ComputeTimestep), by thread 0 of
+            // every CTA; the FP64 arithmetic stays in one thread
+            if (tid == 0) {
+                const unsigned mx0 = ld_relaxed_gpu(&st->max_bits[0]);
+                const unsigned my0 = ld_relaxed_gpu(&st->max_bits[1]);
+                const unsigned mx1 = ld_relaxed_gpu(&st->staleBits[0]);
+                const unsigned my1 = ld_relaxed_gpu(&st->staleBits[1]);
+                const double dtNew = stepDtAt(P, tCur, (double)__uint_as_float(max(mx0, mx1)),
+                                              (double)__uint_as_float(max(my0, my1)));
+                const double tNew = tCur + dtNew;
+                sC[0] = stageConstsAt<1>(P, dtNew, dtOld, tNew);
+                sC[1] = stageConstsAt<2>(P, dtNew, dtOld, tNew);
+                sDt = dtNew;
+            }
+            __syncthreads();
             if (mine) {  // stage-1 update with this step's dt (Integrate_1_k)
-                const StageConsts C1 = stageConstsAt<1>(P, dtNew, dtOld, tNew);
+                const StageConsts C1 = sC[0];
                 const bool wetCell =
                     tileCellUpdate<1>(P, C1, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
                 tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
                 __syncthreads();
             }
             RIFT_SYNC();
-            if (blockIdx.x == 0 && tid == 0) {
-                publishDt(P, st, dtNew);
-                st->staleBits[0] = st->staleBits[1] = 0u;
-            }
-            const StageConsts C2 = stageConstsAt<2>(P, dtNew, dtOld, tNew);
             if (!(fl & F_EULER)) {
-                if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph, &C2)) return;
+                // stage 2 of the same tile: its U* block into the second buffer
+                if (mine) {
+                    if (tid == 0) issueTile(S.buf[1], &S.bar[1], &tmB, &tmE, P, tile);
+                    const StageConsts C2 = sC[1];
+                    tilePrefetch<2>(P, C2, i0, j0, pre);
+                    const bool ok = mbar_wait_bounded(&S.bar[1], ph[1]);
+                    if (!__syncthreads_and(ok)) {
+                        mbar_wait_bounded(&S.bar[1], ph[1]);
+                        if (tid == 0) atomicOr(&st->error, ERR_TMA_TIMEOUT);
+                        return;
+                    }
+                    ph[1] ^= 1u;
+                    float sx2, sy2;
+                    tileFluxDiv<true>(S, S.buf[1], P, i0, j0, dh, dhu, dhv, sx2, sy2);
+                    const bool wetCell =
+                        tileCellUpdate<2>(P, C2, S.buf[1], tile, i0, j0, dh, dhu, dhv, pre);
+                    tileFlags<2>(P, C2, S, tile, wetCell, sx2, sy2);
+                    __syncthreads();
+                }
             } else {
                 commitTiles(P, nAct);
             }
+            if (spare && tid == 0) {
+                publishDt(P, st, sDt);
+                st->staleBits[0] = st->staleBits[1] = 0u;
+                publishGrow(st);
+            }
             RIFT_SYNC();
             continue;
-        } else {
-            // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1
-            if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
-            __syncthreads();
-            finishDt(P, tmx, tmy, &last);
-            resyncDeactivated(P);
-            RIFT_SYNC();
-            if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph)) return;
-            RIFT_SYNC();
         }
+        // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1
+        if (blockIdx.x == 0 && tid < 32) beginStepRates(P, st);
+        float tmx = 0.f, tmy = 0.f;
+        if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
+        __syncthreads();
+        finishDt(P, tmx, tmy, &last);
+        resyncDeactivated(P, nDe);
+        RIFT_SYNC();
+        if (tid == 0) {  // the stage constants, FP64 conversions in one thread
+            sC[0] = stageConsts<1>(P);
+            sC[1] = stageConsts<2>(P);
+        }
+        __syncthreads();
+        if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph, &sC[0])) return;
+        RIFT_SYNC();
         if (!(fl & F_EULER)) {
-            if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph)) return;
+            if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph, &sC[1])) return;
         } else {
             commitTiles(P, nAct);
         }
+        if (spare && tid == 0) publishGrow(st);
         RIFT_SYNC();
     }
 #undef RIFT_SYNC

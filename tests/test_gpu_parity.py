@@ -95,6 +95,29 @@ def test_persistent_hands_over_to_graph(engine_api):
     _close(W1, W0, "persistent then graph vs graph")
 
 
+def test_single_steps_switching_paths(engine_api):
+    """rift_step calls (the one-step persistent graph) interleaved with
+    changes of the persistent bound and runs match one run of the same
+    length."""
+    fx, case = FX.load("gridrain_surge")
+    a = FX.start(_scheduled(capi.Sim(case, api=engine_api), "persist"), fx)
+    for k in range(12):
+        if k % 4 == 2:
+            a.set_persistent(0)
+        elif k % 4 == 3:
+            a.set_persistent(1 << 30)
+        if k % 5 == 4:
+            a.run(1)
+        else:
+            a.step()
+    b = FX.start(_scheduled(capi.Sim(case, api=engine_api), "tiles"), fx)
+    b.run(12)
+    assert a.path_stats()[0] > 0 and a.path_stats()[1] > 0
+    assert np.array_equal(a.tiles()[0], b.tiles()[0]) and np.array_equal(a.tiles()[1], b.tiles()[1])
+    assert abs(a.time()[0] - b.time()[0]) <= 1e-6 * max(1.0, b.time()[0])
+    _close(a.field("W"), b.field("W"), "single steps vs run")
+
+
 @pytest.mark.parametrize("schedule", ["tiles", "march", "persist"])
 @pytest.mark.parametrize("name", ["rain", "front", "gridrain_surge", "h0_infil_src", "euler"])
 def test_one_step_from_identical_snapshot(engine_api, oracle_api, name, schedule):
