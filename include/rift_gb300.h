@@ -234,6 +234,11 @@ void rift_ensemble_destroy(rift_ensemble* e);
 /* Steps run so far by the persistent launch and by the per-step graph. */
 int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_steps);
 
+/* Of the persistent steps, those run from the loop's tile table: one
+   scheduled tile per CTA kept from step to step, no grow phase (no gridded
+   rain or surge, RK2).  No reference counterpart. */
+int rift_get_table_steps(rift_handle* h, int64_t* table_steps);
+
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
 

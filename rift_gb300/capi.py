@@ -86,6 +86,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
         ns["set_persistent"] = _sig(lib, p + "set_persistent", C.c_int, [_P, C.c_int32])
         ns["get_path_stats"] = _sig(lib, p + "get_path_stats", C.c_int,
                                     [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)])
+        ns["get_table_steps"] = _sig(lib, p + "get_table_steps", C.c_int,
+                                     [_P, C.POINTER(C.c_int64)])
     ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
     ns["step"] = _sig(lib, p + "step", C.c_int, [_P, _D, _D])
     ns["run"] = _sig(lib, p + "run", C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _I])
@@ -253,6 +255,12 @@ class Sim:
         a, b = C.c_int64(), C.c_int64()
         self._check(self.f["get_path_stats"](self.h, C.byref(a), C.byref(b)), "get_path_stats")
         return a.value, b.value
+
+    def table_steps(self):
+        """Persistent steps run from the loop's tile table (no grow phase)."""
+        a = C.c_int64()
+        self._check(self.f["get_table_steps"](self.h, C.byref(a)), "get_table_steps")
+        return a.value
 
     # -- stepping ---------------------------------------------------------
     def step(self):

@@ -21,6 +21,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/rift_gb300.h"
@@ -65,6 +66,7 @@ struct rift_handle {
     int persistMax = 0;    // it runs while the active tiles are at most this many
     GridBar* gbar = nullptr;
     int* owner = nullptr;  // [gridSize] tile table of the persistent loop
+    int* tileFlag = nullptr;  // [gridSize] stage-1 completion of the persistent loop
     long long persistSteps = 0, graphSteps = 0;  // steps run by each path (diagnostics)
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
@@ -86,14 +88,19 @@ struct rift_handle {
     int serN[3] = {0, 0, 0};
     DevState* st = nullptr;
     DevState* hst = nullptr;  // pinned mirror
+    float* stage = nullptr;   // pinned host planes for field uploads / readbacks
+    size_t stageFloats = 0;
     double* volPartial = nullptr;
     CUtensorMap tmA{}, tmB{}, tmE{};
     std::vector<double> Bref, BC, h0_;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
-    // one persistent step with its state copies, for rift_step
-    cudaGraphExec_t stepExec = nullptr;
-    int stepGrid = 0;
+    // one persistent step with its state copies, for rift_step: one graph
+    // per grid size seen (the grid follows the active count)
+    static constexpr int STEP_CACHE = 4;
+    cudaGraphExec_t stepExec[STEP_CACHE] = {};
+    int stepGrid[STEP_CACHE] = {};
+    int stepNext = 0;
     bool stepGraphBroken = false;
     bool haveStatic = false, inited = false;
     std::string err;
@@ -137,6 +144,11 @@ Params makeParams(rift_handle* h) {
     P.dyd = h->g.dy;
     P.kappad = h->g.kappa;
     P.courant = h->g.courant;
+    {
+        int e = 0;
+        const double m = std::frexp(h->g.courant, &e);
+        P.courantScale = (m == 0.5 && h->g.courant > 0.0) ? (float)(1.0 / h->g.courant) : 0.f;
+    }
     P.flags = h->g.flags;
     P.A = h->A;
     P.B = h->B;
@@ -168,6 +180,7 @@ Params makeParams(rift_handle* h) {
     P.persistMax = h->persistMax;
     P.gbar = h->gbar;
     P.owner = h->owner;
+    P.tileFlag = h->tileFlag;
     P.mx = h->mx;
     P.my = h->my;
     P.srcIdx = h->srcIdx;
@@ -200,10 +213,13 @@ int encodeMap(rift_handle* h, CUtensorMap* tm, float* base, int nfields, int box
 void destroyGraph(rift_handle* h) {
     if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
     if (h->graph) cudaGraphDestroy(h->graph);
-    if (h->stepExec) cudaGraphExecDestroy(h->stepExec);
+    for (int k = 0; k < rift_handle::STEP_CACHE; k++) {
+        if (h->stepExec[k]) cudaGraphExecDestroy(h->stepExec[k]);
+        h->stepExec[k] = nullptr;
+        h->stepGrid[k] = 0;
+    }
     h->graphExec = nullptr;
     h->graph = nullptr;
-    h->stepExec = nullptr;
 }
 
 // The launch sequence of one step (captured into the graph).
@@ -237,13 +253,16 @@ int buildGraph(rift_handle* h) {
     return RIFT_OK;
 }
 
+const char* deviceErrorText(int err) {
+    if (err & ERR_TILE_TABLE) return "persistent loop: tile table and active set disagree";
+    if (err & ERR_BARRIER_TIMEOUT) return "device wait timed out (grid barrier)";
+    return "device wait timed out (TMA barrier)";
+}
+
 int pullState(rift_handle* h) {
     CUDA_TRY(h, cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    if (h->hst->error)
-        return fail(h, RIFT_ERR_CUDA,
-                    (h->hst->error & ERR_BARRIER_TIMEOUT) ? "device wait timed out (grid barrier)"
-                                                          : "device wait timed out (TMA barrier)");
+    if (h->hst->error) return fail(h, RIFT_ERR_CUDA, deviceErrorText(h->hst->error));
     return RIFT_OK;
 }
 
@@ -297,8 +316,7 @@ float depthFromW(const rift_handle* h, double w, int j, int i) {
 
 // Critical-depth ghosts on the host (init / state upload), same rule as the
 // device writeGhosts.
-void hostGhosts(rift_handle* h, std::vector<float>& H, std::vector<float>& U,
-                std::vector<float>& V) {
+void hostGhosts(rift_handle* h, float* H, float* U, float* V) {
     const int nx = h->nx, ny = h->ny;
     auto crit = [](float q, float d) { return std::fmin(std::cbrt(q * q / kG), d); };
     for (int j = 2; j <= ny - 3; j++) {
@@ -332,18 +350,59 @@ void hostGhosts(rift_handle* h, std::vector<float>& H, std::vector<float>& U,
     }
 }
 
-int upField(rift_handle* h, float* dev, const std::vector<float>& host) {
-    CUDA_TRY(h, cudaMemcpy2DAsync(dev, (size_t)h->pitch * 4, host.data(), (size_t)h->nx * 4,
+int upField(rift_handle* h, float* dev, const float* host) {
+    CUDA_TRY(h, cudaMemcpy2DAsync(dev, (size_t)h->pitch * 4, host, (size_t)h->nx * 4,
                                   (size_t)h->nx * 4, h->ny, cudaMemcpyHostToDevice, h->stream));
     return RIFT_OK;
 }
 
-int downField(rift_handle* h, const float* dev, std::vector<float>& host) {
-    host.resize((size_t)h->nx * h->ny);
-    CUDA_TRY(h, cudaMemcpy2DAsync(host.data(), (size_t)h->nx * 4, dev, (size_t)h->pitch * 4,
+int upField(rift_handle* h, float* dev, const std::vector<float>& host) {
+    return upField(h, dev, host.data());
+}
+
+// Device plane -> host (nx x ny), synchronous.
+int downField(rift_handle* h, const float* dev, float* host) {
+    CUDA_TRY(h, cudaMemcpy2DAsync(host, (size_t)h->nx * 4, dev, (size_t)h->pitch * 4,
                                   (size_t)h->nx * 4, h->ny, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return RIFT_OK;
+}
+
+// `planes` host planes of nx x ny floats in pinned memory (kept by the
+// handle; the caller finishes its copies before the next use).
+float* stagePlanes(rift_handle* h, int planes) {
+    const size_t need = (size_t)planes * h->nx * h->ny;
+    if (h->stageFloats < need) {
+        if (h->stage) cudaFreeHost(h->stage);
+        h->stage = nullptr;
+        h->stageFloats = 0;
+        if (cudaMallocHost(&h->stage, need * 4) != cudaSuccess) {
+            cudaGetLastError();
+            h->stage = nullptr;
+            return nullptr;
+        }
+        h->stageFloats = need;
+    }
+    return h->stage;
+}
+
+// fn(j0, j1) over row bands of [0, ny) on up to 16 host threads (inline for
+// small grids).
+template <class F>
+void parallelRows(int ny, size_t cells, F fn) {
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::max(1u, std::min(16u, nt));
+    if (cells < (size_t)1 << 18 || nt == 1) {
+        fn(0, ny);
+        return;
+    }
+    std::vector<std::thread> th;
+    const int per = (ny + (int)nt - 1) / (int)nt;
+    for (unsigned t = 0; t < nt; t++) {
+        const int j0 = (int)t * per, j1 = std::min(ny, j0 + per);
+        if (j0 < j1) th.emplace_back(fn, j0, j1);
+    }
+    for (auto& x : th) x.join();
 }
 
 bool tileInGrid(const rift_handle* h, int b) {
@@ -352,8 +411,8 @@ bool tileInGrid(const rift_handle* h, int b) {
 }
 
 // Upload U (A and B), tile flags and lists.
-int uploadState(rift_handle* h, const std::vector<float>& H, const std::vector<float>& U,
-                const std::vector<float>& V, const std::vector<uint8_t>& wet,
+int uploadState(rift_handle* h, const float* H, const float* U, const float* V,
+                const std::vector<uint8_t>& wet,
                 const std::vector<uint8_t>& activeFlags, const std::vector<int>& inactList) {
     const size_t pl = h->plane();
     int r;
@@ -368,6 +427,13 @@ int uploadState(rift_handle* h, const std::vector<float>& H, const std::vector<f
         CUDA_TRY(h, cudaMemcpyAsync(h->inact, inactList.data(), inactList.size() * 4,
                                     cudaMemcpyHostToDevice, h->stream));
     h->hst->nInact = (int)inactList.size();
+    // the scheduled count of the uploaded active set: the persistent
+    // launch sizes its grid by it until the next grow publishes its own
+    int nAct = 0;
+    for (int b = 0; b < h->gridSize; b++)
+        if (activeFlags[b] && (b % h->nBX) * TW + 2 <= h->nx - 3 && (b / h->nBX) * TH + 2 <= h->ny - 3)
+            nAct++;
+    h->hst->nActive = nAct;
     return RIFT_OK;
 }
 
@@ -475,6 +541,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
         h->gridPersist = std::min(h->numSMs * occ, PERSIST_MAX_CTAS);
         CUDA_TRY(h, cudaMalloc(&h->gbar, sizeof(GridBar)));
         CUDA_TRY(h, cudaMalloc(&h->owner, (size_t)G * 4));
+        CUDA_TRY(h, cudaMalloc(&h->tileFlag, (size_t)G * 4));
     }
     h->gridGrow = std::max(1, std::min(NS, h->numSMs * 4));
     h->persistMax = h->gridPersist > 0 ? h->marchMin * STRIP_TX * STRIP_TY : 0;
@@ -529,7 +596,7 @@ int rift_init(rift_handle* h, double t0) {
     if (h->has(RIFT_F_H_INIT) && !h->h0_.empty())
         for (int j = 2; j < ny; j++)
             for (int i = 2; i < nx; i++) H[hidx(h, j, i)] = (float)h->h0_[hidx(h, j, i)];
-    hostGhosts(h, H, U, V);
+    hostGhosts(h, H.data(), U.data(), V.data());
     std::vector<uint8_t> wet(h->gridSize), actf(h->gridSize);
     bool anyOut = false;
     for (int b = 0; b < h->gridSize; b++) {
@@ -557,7 +624,7 @@ int rift_init(rift_handle* h, double t0) {
     h->hst->drain_rate = keepDrain;
     h->hst->rain_sum[0] = keep.rain_sum[0];
     h->hst->rain_sum[1] = keep.rain_sum[1];
-    int rc = uploadState(h, H, U, V, wet, actf, inact);
+    int rc = uploadState(h, H.data(), U.data(), V.data(), wet, actf, inact);
     if (rc) return rc;
     const size_t pl = h->plane() * 4;
     if (h->FA) {
@@ -816,11 +883,14 @@ bool stepGraph(rift_handle* h, int& rc) {
     rc = RIFT_OK;
     if (h->stepGraphBroken) return false;
     const int grid = persistGrid(h);
-    if (h->stepExec && h->stepGrid != grid) {
-        cudaGraphExecDestroy(h->stepExec);
-        h->stepExec = nullptr;
-    }
-    if (!h->stepExec) {
+    int slot = -1;
+    for (int k = 0; k < rift_handle::STEP_CACHE; k++)
+        if (h->stepExec[k] && h->stepGrid[k] == grid) slot = k;
+    if (slot < 0) {
+        slot = h->stepNext;
+        h->stepNext = (h->stepNext + 1) % rift_handle::STEP_CACHE;
+        if (h->stepExec[slot]) cudaGraphExecDestroy(h->stepExec[slot]);
+        h->stepExec[slot] = nullptr;
         Params P = makeParams(h);
         int one = 1;
         void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&one};
@@ -835,25 +905,26 @@ bool stepGraph(rift_handle* h, int& rc) {
         cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0, h->stream);
         cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream);
         cudaError_t e = cudaStreamEndCapture(h->stream, &g);
-        if (e != cudaSuccess || !g || cudaGraphInstantiate(&h->stepExec, g, 0) != cudaSuccess) {
+        if (e != cudaSuccess || !g ||
+            cudaGraphInstantiate(&h->stepExec[slot], g, 0) != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
-            h->stepExec = nullptr;
+            h->stepExec[slot] = nullptr;
             h->stepGraphBroken = true;
             cudaGetLastError();
             return false;
         }
         cudaGraphDestroy(g);
-        h->stepGrid = grid;
+        h->stepGrid[slot] = grid;
     }
     const int before = h->hst->steps_done;
-    cudaError_t e = cudaGraphLaunch(h->stepExec, h->stream);
+    cudaError_t e = cudaGraphLaunch(h->stepExec[slot], h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
         rc = fail(h, RIFT_ERR_CUDA, std::string("step graph: ") + cudaGetErrorString(e));
         return true;
     }
     if (h->hst->error) {
-        rc = fail(h, RIFT_ERR_CUDA, "device wait timed out");
+        rc = fail(h, RIFT_ERR_CUDA, deviceErrorText(h->hst->error));
         return true;
     }
     h->persistSteps += h->hst->steps_done - before;
@@ -912,11 +983,17 @@ int rift_get_field(rift_handle* h, int32_t which, double* host, size_t ld) {
     if (!h || !host || ld < (size_t)h->nx) return RIFT_ERR_ARG;
     const int nx = h->nx, ny = h->ny;
     const size_t pl = h->plane();
-    std::vector<float> a, b, c;
+    const size_t N = (size_t)nx * ny;
+    float* const a = stagePlanes(h, 4);
+    if (!a) return fail(h, RIFT_ERR_NOMEM, "pinned staging planes");
+    float* const b = a + N;
+    float* const c = a + 2 * N;
     int rc = 0;
     auto put = [&](auto fn) {
-        for (int j = 0; j < ny; j++)
-            for (int i = 0; i < nx; i++) host[(size_t)j * ld + i] = fn(j, i);
+        parallelRows(ny, N, [&](int j0, int j1) {
+            for (int j = j0; j < j1; j++)
+                for (int i = 0; i < nx; i++) host[(size_t)j * ld + i] = fn(j, i);
+        });
     };
     auto zero = [&](int, int) { return 0.0; };
     switch (which) {
@@ -1022,17 +1099,22 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
     if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
     const int nx = h->nx, ny = h->ny;
     const size_t N = (size_t)nx * ny;
-    std::vector<float> H(N), U(N), V(N);
-    for (int j = 0; j < ny; j++)
-        for (int i = 0; i < nx; i++) {
-            size_t c = hidx(h, j, i);
-            H[c] = depthFromW(h, w[c], j, i);
-            U[c] = (float)hu[c];
-            V[c] = (float)hv[c];
-        }
-    hostGhosts(h, H, U, V);
-    int rc = pullState(h);
+    int rc = pullState(h);  // also: no earlier copy still reads the staging planes
     if (rc) return rc;
+    float* const H = stagePlanes(h, 4);
+    if (!H) return fail(h, RIFT_ERR_NOMEM, "pinned staging planes");
+    float* const U = H + N;
+    float* const V = H + 2 * N;
+    parallelRows(ny, N, [&](int j0, int j1) {
+        for (int j = j0; j < j1; j++)
+            for (int i = 0; i < nx; i++) {
+                size_t c = hidx(h, j, i);
+                H[c] = depthFromW(h, w[c], j, i);
+                U[c] = (float)hu[c];
+                V[c] = (float)hv[c];
+            }
+    });
+    hostGhosts(h, H, U, V);
     std::vector<uint8_t> wetv(h->gridSize), actf(h->gridSize);
     CUDA_TRY(h, cudaMemcpyAsync(wetv.data(), h->wet, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(actf.data(), h->prevAct, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
@@ -1048,8 +1130,10 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
         if (!actf[b]) inact.push_back(b);
     if ((rc = uploadState(h, H, U, V, wetv, actf, inact))) return rc;
     if (F && h->FA) {
-        std::vector<float> f(N);
-        for (size_t c = 0; c < N; c++) f[c] = (float)F[c];
+        float* const f = H + 3 * N;
+        parallelRows(ny, N, [&](int j0, int j1) {
+            for (size_t c = (size_t)j0 * nx; c < (size_t)j1 * nx; c++) f[c] = (float)F[c];
+        });
         if ((rc = upField(h, h->FA, f)) || (rc = upField(h, h->FB, f))) return rc;
     }
     if (mx || my) {
@@ -1172,6 +1256,12 @@ int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_s
     if (!h) return RIFT_ERR_ARG;
     if (persist_steps) *persist_steps = h->persistSteps;
     if (graph_steps) *graph_steps = h->graphSteps;
+    return RIFT_OK;
+}
+
+int rift_get_table_steps(rift_handle* h, int64_t* table_steps) {
+    if (!h || !table_steps) return RIFT_ERR_ARG;
+    *table_steps = h->hst ? h->hst->tableSteps : 0;
     return RIFT_OK;
 }
 
@@ -1393,13 +1483,14 @@ void rift_destroy(rift_handle* h) {
     for (int k = 0; k < 3; k++)
         for (int q = 0; q < 2; q++)
             if (h->maps[k][q]) cudaFree(h->maps[k][q]);
-    for (void* p : {(void*)h->gbar, (void*)h->owner,
+    for (void* p : {(void*)h->gbar, (void*)h->owner, (void*)h->tileFlag,
                     (void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
                     (void*)h->act, (void*)h->deact,
                     (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,
                     (void*)h->srcTileList, (void*)h->st, (void*)h->volPartial})
         if (p) cudaFree(p);
     if (h->hst) cudaFreeHost(h->hst);
+    if (h->stage) cudaFreeHost(h->stage);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -248,8 +248,12 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
         if (D->nAlive[cur] == 0) return;  // every CTA reads the same count
         const int* live = D->live[cur];
         // ---- T: re-wet tracking of the members with gridded rain or surge
+        // (a member without an inactive list -- last stepped by the
+        // persistent loop's tile table -- scans its tiles instead)
         ensPrefix(n, [&](int m) {
-            return live[m] && (E.Ps[m].flags & (F_RAIN_G | F_SURGE)) ? E.Ps[m].st->nInact : 0;
+            if (!live[m] || !(E.Ps[m].flags & (F_RAIN_G | F_SURGE))) return 0;
+            const int k = E.Ps[m].st->nInact;
+            return k >= 0 ? k : E.Ps[m].gridSize - 1;
         }, Q.offs);
         if (Q.offs[n] > 0) {  // the same total in every CTA
             for (int g = blockIdx.x; g < Q.offs[n]; g += gridDim.x) {
@@ -257,7 +261,9 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
                 const Params& P = E.Ps[m];
                 float fac0, fac2;
                 trackFactors(P, fac0, fac2);
-                trackTile(P, P.inact[g - Q.offs[m]], fac0, fac2);
+                const bool listed = P.st->nInact >= 0;
+                const int b = listed ? P.inact[g - Q.offs[m]] : g - Q.offs[m] + 1;
+                if (listed || !P.prevAct[b]) trackTile(P, b, fac0, fac2);
             }
             ENS_SYNC();
         }

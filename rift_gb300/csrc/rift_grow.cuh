@@ -24,10 +24,16 @@ constexpr int GROW_LISTS = 4;            // scheduled active, deactivated, inact
 constexpr int STRIPS_PER_ROUND = NT / 16;
 
 // active(t) of tile b: wet itself or a wet 4-neighbour; tile 0 always.
+// The five flags are loaded together (no short-circuit: a dry tile would
+// otherwise wait for five loads in a row).
 __device__ __forceinline__ bool tileGrows(const Params& P, int b) {
     const int bX = b % P.nBX, bY = b / P.nBX;
-    return P.wet[b] || (bX > 0 && P.wet[b - 1]) || (bX < P.nBX - 1 && P.wet[b + 1]) ||
-           (bY > 0 && P.wet[b - P.nBX]) || (bY < P.nBY - 1 && P.wet[b + P.nBX]) || b == 0;
+    const unsigned w = P.wet[b];
+    const unsigned wW = bX > 0 ? P.wet[b - 1] : 0u;
+    const unsigned wE = bX < P.nBX - 1 ? P.wet[b + 1] : 0u;
+    const unsigned wS = bY > 0 ? P.wet[b - P.nBX] : 0u;
+    const unsigned wN = bY < P.nBY - 1 ? P.wet[b + P.nBX] : 0u;
+    return ((w | wW | wE | wS | wN) != 0u) || b == 0;
 }
 
 // Interior cells of tile b (0 for a tile wholly in the ghost band).
@@ -53,6 +59,7 @@ struct GrowItem {
     int b, strip, cells;
     bool v;
     int f[GROW_LISTS];
+    float mxb, myb;  // the tile's speeds entering the step
 };
 
 __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) {
@@ -60,6 +67,7 @@ __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) 
     t.b = -1;
     t.v = false;
     t.cells = 0;
+    t.mxb = t.myb = 0.f;
     for (int q = 0; q < GROW_LISTS; q++) t.f[q] = 0;
     const int lane = threadIdx.x & 31, r = threadIdx.x & 15;
     t.strip = base + (int)threadIdx.x / 16;
@@ -70,10 +78,13 @@ __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) 
         if (bx < P.nBX && by < P.nBY) {
             const int b = by * P.nBX + bx;
             t.b = b;
+            const bool was = P.prevAct[b] != 0;
+            t.mxb = P.mx[b];
+            t.myb = P.my[b];
             t.v = tileGrows(P, b);
             t.cells = tileCells(P, b);
             t.f[0] = (t.v && t.cells > 0) ? 1 : 0;
-            t.f[1] = (P.prevAct[b] && !t.v) ? 1 : 0;
+            t.f[1] = (was && !t.v) ? 1 : 0;
             t.f[2] = (!t.v && b != 0) ? 1 : 0;
         }
     }
@@ -92,7 +103,7 @@ __device__ __forceinline__ GrowItem growItem(const Params& P, int base, int s1) 
 // without, the caller reads the counters after a grid barrier and publishes
 // them later (publishGrow).
 template <bool PUBLISH = true>
-__device__ void growAppend(const Params& P) {
+__device__ void growAppend(const Params& P, unsigned* staleDst = nullptr) {
     DevState* s = P.st;
     const int tid = threadIdx.x, lane = tid & 31;
     int s0, s1;
@@ -121,8 +132,8 @@ __device__ void growAppend(const Params& P) {
                 P.my[t.b] = 0.f;
             }
             if (!t.v) {  // a tile not active this step: its stale speeds count for dt (A5)
-                smx = fmaxf(smx, P.mx[t.b]);
-                smy = fmaxf(smy, P.my[t.b]);
+                smx = fmaxf(smx, t.mxb);
+                smy = fmaxf(smy, t.myb);
             }
             P.prevAct[t.b] = (uint8_t)(t.v ? 1 : 0);
         }
@@ -133,8 +144,9 @@ __device__ void growAppend(const Params& P) {
         smy = fmaxf(smy, __shfl_xor_sync(0xffffffffu, smy, o));
     }
     if (lane == 0 && cells) atomicAdd(&s->appendCells, cells);
-    if (lane == 0 && smx > 0.f) atomicMax(&s->staleBits[0], __float_as_uint(smx));
-    if (lane == 0 && smy > 0.f) atomicMax(&s->staleBits[1], __float_as_uint(smy));
+    unsigned* const stale = staleDst ? staleDst : s->staleBits;
+    if (lane == 0 && smx > 0.f) atomicMax(&stale[0], __float_as_uint(smx));
+    if (lane == 0 && smy > 0.f) atomicMax(&stale[1], __float_as_uint(smy));
     if (!PUBLISH) return;
     __syncthreads();
     if (tid == 0) {

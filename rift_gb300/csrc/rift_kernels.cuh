@@ -52,6 +52,7 @@ constexpr uint32_t F_RAIN_U = 1u << 0, F_RAIN_G = 1u << 1, F_DRAIN_U = 1u << 2,
 
 constexpr int ERR_TMA_TIMEOUT = 1;
 constexpr int ERR_BARRIER_TIMEOUT = 2;
+constexpr int ERR_TILE_TABLE = 4;  // persistent loop: tile table and scan disagree
 
 // Device-resident scalars of the run (one per handle).
 struct DevState {
@@ -72,6 +73,7 @@ struct DevState {
     int nStrips;       // strips of the march kernels holding an active tile
     int stop;
     int persistExit;   // the persistent kernel left because the active set grew
+    int tableSteps;    // steps the persistent loop ran from its tile table (no grow)
     int steps_done;
     unsigned long long activeCells;  // interior cells of active tiles, summed over steps
     int appendCnt[4];                // grow: list counters (zero between steps)
@@ -89,6 +91,7 @@ struct Params {
     int pitch, rows;   // floats per row, rows per field plane
     float dx, dy, inv_dx, inv_dy, kappa, psiDtheta, nodata;
     double dxd, dyd, kappad, courant;
+    float courantScale;  // 1/courant when courant is a power of two, else 0
     uint32_t flags;
     float* A;          // [3][rows][pitch]  U^n / U^{n+1}: h, hu, hv
     float* B;          // [3][rows][pitch]  U*
@@ -117,6 +120,7 @@ struct Params {
     int persistMax;    // the persistent step kernel runs while active tiles <= this
     struct GridBar* gbar;            // grid barrier of the persistent kernel
     int* owner;        // [gridSize] tile -> CTA of the persistent loop's tile table, or -1
+    int* tileFlag;     // [gridSize] persistent loop: last step whose stage 1 the tile finished
     float* mx;
     float* my;
     const int* srcIdx;      // flat h-grid indices j*nx+i
@@ -252,10 +256,28 @@ __device__ __forceinline__ float blockMax(float v, float* red) {
 // the tile speeds: dt with the reference's rounding points (fmaxf on the
 // scaled maxima, FP64 division), t += dt, and the step's entry in the
 // volume ledger.
+// maxx, maxy: float speed maxima.  When the Courant number is a power of
+// two, float(max / courant) is the exact float product with 1/courant, and
+// with square cells min(dx / fx, dx / fy) = dx / max(fx, fy) (rounded
+// division is monotone in the divisor): one FP64 division instead of four,
+// with the same result.
 __device__ __forceinline__ double stepDtAt(const Params& P, double t, double maxx, double maxy) {
-    double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
-    double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
-    double dt = cx < cy ? cx : cy;
+    double dt;
+    if (P.courantScale > 0.f) {
+        const float kap = (float)P.kappad;
+        const float fx = fmaxf((float)maxx * P.courantScale, kap);
+        const float fy = fmaxf((float)maxy * P.courantScale, kap);
+        if (P.dxd == P.dyd) {
+            dt = P.dxd / (double)fmaxf(fx, fy);
+        } else {
+            const double cx = P.dxd / (double)fx, cy = P.dyd / (double)fy;
+            dt = cx < cy ? cx : cy;
+        }
+    } else {
+        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
+        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
+        dt = cx < cy ? cx : cy;
+    }
     if (t == 0.0) dt = (double)0.000001f;
     return dt;
 }
@@ -552,6 +574,11 @@ __device__ __forceinline__ void trackTiles(const Params& P) {
     const int n = P.st->nInact;
     float fac0, fac2;
     trackFactors(P, fac0, fac2);
+    if (n < 0) {  // no list (a step of the persistent loop's tile table): scan
+        for (int b = blockIdx.x + 1; b < P.gridSize; b += gridDim.x)
+            if (!P.prevAct[b]) trackTile(P, b, fac0, fac2);
+        return;
+    }
     for (int k = blockIdx.x; k < n; k += gridDim.x) trackTile(P, P.inact[k], fac0, fac2);
 }
 

@@ -35,10 +35,13 @@ constexpr int PERSIST_MAX_CTAS = 4096;
 // every launch).
 struct GridBar {
     unsigned count[32];
-    int freeTop;    // entries of freeStack
-    int overflow;   // a claim found no free CTA: the table is void
-    int ownedCnt;   // owned tiles found active this step
-    int schedCnt;   // scheduled tiles found by the scan this step
+    // step reductions of the fused steps, by step parity: a step's values
+    // are cleared during the next step, when no CTA can still read them
+    unsigned maxb[2][2];   // speed maxima of the scheduled tiles (bits)
+    unsigned staleb[2][2]; // stale speed maxima of the inactive tiles (bits)
+    int ownedCnt[2];       // owned tiles found active
+    int schedCnt[2];       // scheduled tiles found by the scan
+    int freeTop;           // entries of freeStack
     int slotTile[PERSIST_MAX_CTAS];   // CTA -> its tile, or -1
     int freeStack[PERSIST_MAX_CTAS];  // CTAs without a tile
 };
@@ -68,15 +71,30 @@ __device__ __forceinline__ void fence_proxy_async_global() {
 // After the barrier, TMA loads (async proxy) see the generic-proxy writes made
 // before it.  Measured on GB300: 1.2 us for 152 CTAs, 2.1 us for 608.  False
 // after the poll limit (error recorded).
-__device__ bool gridSync(GridBar* gb, unsigned& target, DevState* st) {
+//
+// A CTA may raise an event at a barrier (`raise`): its arrival adds
+// BAR_EVENT + 1.  Every CTA leaves with the number of events raised there
+// (*events): no barrier passes before every arrival is counted, and the
+// arrivals at the next barrier that a slow poller may also see add less
+// than BAR_EVENT in all (they raise nothing: the caller raises events at
+// one barrier only, never at the one after it).  The event count then moves
+// into `target`, so later barriers see none.
+constexpr unsigned BAR_EVENT = 1u << 16;  // > any grid (PERSIST_MAX_CTAS)
+static_assert(BAR_EVENT > (unsigned)PERSIST_MAX_CTAS, "event unit above the arrivals");
+
+__device__ bool gridSync(GridBar* gb, unsigned& target, DevState* st, bool raise = false,
+                         int* events = nullptr) {
+    __shared__ int sEvents;
     __syncthreads();
     int ok = 1;
     if (threadIdx.x == 0) {
         target += gridDim.x;
-        red_add_release_gpu(&gb->count[0], 1u);
+        red_add_release_gpu(&gb->count[0], raise ? BAR_EVENT + 1u : 1u);
         ok = 0;
+        unsigned v = 0u;
         for (int it = 0; it < (1 << 22); ++it) {
-            if ((int)(ld_acquire_gpu(&gb->count[0]) - target) >= 0) {
+            v = ld_acquire_gpu(&gb->count[0]);
+            if ((int)(v - target) >= 0) {
                 ok = 1;
                 break;
             }
@@ -84,8 +102,13 @@ __device__ bool gridSync(GridBar* gb, unsigned& target, DevState* st) {
         }
         fence_proxy_async_global();
         if (!ok) atomicOr(&st->error, ERR_BARRIER_TIMEOUT);
+        const unsigned k = ok ? (v - target) / BAR_EVENT : 0u;
+        target += k * BAR_EVENT;
+        sEvents = (int)k;
     }
-    return __syncthreads_and(ok) != 0;
+    ok = __syncthreads_and(ok);
+    if (events) *events = sEvents;
+    return ok != 0;
 }
 
 // ------------------------------------------------------------ tile table
@@ -103,14 +126,9 @@ __device__ bool gridSync(GridBar* gb, unsigned& target, DevState* st) {
 //     table holds the next step's scheduled set.
 // The owned active tiles are counted against the scan every step (a
 // mismatch is an error, never a silent result).  A claim that finds no free
-// CTA voids the table: the loop returns to the grow, and rebuilds the table
-// from the grow's list once the active set fits the grid again.
-
-// Rebuild, grow phase: no tile holds a CTA.
-__device__ __forceinline__ void tableClear(const Params& P) {
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < P.gridSize; b += gridDim.x * blockDim.x)
-        P.owner[b] = -1;
-}
+// CTA voids the table (an event at the barrier after stage 2): the loop
+// returns to the grow, and rebuilds the table from the grow's list once the
+// active set fits the grid again.
 
 // Rebuild, after the grow's barrier (thread 0): CTA c takes act[c] or joins
 // the free stack.
@@ -122,19 +140,16 @@ __device__ __forceinline__ void tableBuild(const Params& P, int nAct, int tile) 
         P.owner[tile] = c;
     else
         T->freeStack[c - nAct] = c;
-    if (c == 0) {
-        T->freeTop = (int)gridDim.x - nAct;
-        T->overflow = 0;
-        T->ownedCnt = 0;
-        T->schedCnt = 0;
-    }
+    if (c == 0) T->freeTop = (int)gridDim.x - nAct;
 }
 
 // Table step, flux phase: active flags, stale speeds, zero speeds of active
 // tiles without interior cells, U* re-sync of deactivated tiles and the
 // scheduled count over this CTA's chunk of tiles (what the grow does, less
-// the lists).  deList/deCount: shared scratch (NT entries, count 0).
-__device__ void scanTiles(const Params& P, int* deList, int* deCount) {
+// the lists), into staleDst[2] and *schedDst.  deList/deCount: shared
+// scratch (NT entries, count 0).
+__device__ void scanTiles(const Params& P, unsigned* staleDst, int* schedDst, int* deList,
+                          int* deCount) {
     DevState* s = P.st;
     const int tid = threadIdx.x, lane = tid & 31;
     const int per = (P.gridSize + (int)gridDim.x - 1) / (int)gridDim.x;
@@ -146,9 +161,12 @@ __device__ void scanTiles(const Params& P, int* deList, int* deCount) {
         const int b = base + tid;
         bool de = false;
         if (b < b1) {
+            // every load of the tile issued before any is used
+            const bool was = P.prevAct[b] != 0;
+            const float mxb = P.mx[b], myb = P.my[b];
             const bool v = tileGrows(P, b);
             const int nc = tileCells(P, b);
-            de = P.prevAct[b] && !v;
+            de = was && !v;
             if (v && nc > 0) {
                 sched++;
                 cells += (unsigned long long)nc;
@@ -158,8 +176,8 @@ __device__ void scanTiles(const Params& P, int* deList, int* deCount) {
                 P.my[b] = 0.f;
             }
             if (!v) {  // stale speeds count for dt (A5)
-                smx = fmaxf(smx, P.mx[b]);
-                smy = fmaxf(smy, P.my[b]);
+                smx = fmaxf(smx, mxb);
+                smy = fmaxf(smy, myb);
             }
             P.prevAct[b] = (uint8_t)(v ? 1 : 0);
         }
@@ -179,10 +197,10 @@ __device__ void scanTiles(const Params& P, int* deList, int* deCount) {
         smy = fmaxf(smy, __shfl_xor_sync(0xffffffffu, smy, o));
     }
     if (lane == 0) {
-        if (sched) atomicAdd(&P.gbar->schedCnt, sched);
+        if (sched) atomicAdd(schedDst, sched);
         if (cells) atomicAdd(&s->appendCells, cells);
-        if (smx > 0.f) atomicMax(&s->staleBits[0], __float_as_uint(smx));
-        if (smy > 0.f) atomicMax(&s->staleBits[1], __float_as_uint(smy));
+        if (smx > 0.f) atomicMax(&staleDst[0], __float_as_uint(smx));
+        if (smy > 0.f) atomicMax(&staleDst[1], __float_as_uint(smy));
     }
 }
 
@@ -196,7 +214,7 @@ __device__ __forceinline__ void tableRelease(const Params& P, int tile) {
 
 // Stage 2 (threads 0..3, one neighbour each): `tile` turned wet; each
 // neighbour with interior cells and no CTA gets one from the free stack.
-__device__ __forceinline__ void tableClaim(const Params& P, int tile) {
+__device__ __forceinline__ void tableClaim(const Params& P, int tile, int* overflow) {
     const int q = threadIdx.x;
     const int bX = tile % P.nBX, bY = tile / P.nBX;
     int nb = -1;
@@ -209,7 +227,7 @@ __device__ __forceinline__ void tableClaim(const Params& P, int tile) {
     GridBar* T = P.gbar;
     const int k = atomicSub(&T->freeTop, 1) - 1;
     if (k < 0) {
-        atomicExch(&T->overflow, 1);
+        *overflow = 1;  // raised as an event at the barrier after stage 2
         return;
     }
     const int c = T->freeStack[k];
@@ -224,6 +242,31 @@ __device__ __forceinline__ void tableClaim(const Params& P, int tile) {
 // rates during the flux phase, the dt bookkeeping and the grow's counts
 // during stage 2.  Every CTA reads the grow's counters itself after the
 // grow's barrier, so the grow needs no last-CTA hand-off.
+// Stage 1 -> stage 2 of the fused steps (RK2): a tile's stage 2 reads U*
+// of its 4 edge neighbours only (2 cells deep; the ghost cells in that band
+// are written by the tile itself or by those neighbours), so instead of a
+// grid barrier each CTA publishes its tile's stage-1 completion and waits
+// for the neighbours scheduled this step.  Thread q < 4 waits for
+// neighbour q; bounded like every wait.
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool waitNeighbour(const Params& P, int tile, int q, int epoch) {
+    const int bX = tile % P.nBX, bY = tile / P.nBX;
+    int nb = -1;
+    if (q == 0 && bX > 0) nb = tile - 1;
+    if (q == 1 && bX < P.nBX - 1) nb = tile + 1;
+    if (q == 2 && bY > 0) nb = tile - P.nBX;
+    if (q == 3 && bY < P.nBY - 1) nb = tile + P.nBX;
+    if (nb < 0 || !P.prevAct[nb] || tileCells(P, nb) == 0) return true;  // not scheduled
+    for (int it = 0; it < (1 << 22); ++it) {
+        if ((int)ld_acquire_gpu((const unsigned*)&P.tileFlag[nb]) >= epoch) return true;
+        __nanosleep(20);
+    }
+    return false;
+}
+
 __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUtensorMap tmA,
                                                 const __grid_constant__ CUtensorMap tmB,
                                                 const __grid_constant__ CUtensorMap tmE, Params P,
@@ -232,23 +275,41 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
     __shared__ bool last;
     __shared__ StageConsts sC[2];
     __shared__ double sDt;
+    __shared__ int deList[NT];
+    __shared__ int deCount;
+    __shared__ int sFail;
+    __shared__ int sSched;
+    __shared__ int sOverflow;  // a claim of this CTA found no free CTA
     DevState* st = P.st;
+    GridBar* const T = P.gbar;
     const int tid = threadIdx.x;
     const uint32_t fl = P.flags;
     const bool track = (fl & (F_RAIN_G | F_SURGE)) != 0;
+    const bool euler = (fl & F_EULER) != 0;
+    const bool tableOk = !track && !euler && P.owner != nullptr;
     const bool spare = blockIdx.x == gridDim.x - 1;
     tileInit(S, &tmA, &tmE);
-    if (tid == 0) prefetch_tmap(&tmB);
+    if (tid == 0) {
+        prefetch_tmap(&tmB);
+        deCount = 0;
+        sOverflow = 0;
+    }
     uint32_t ph[2] = {0u, 0u};
     unsigned barTarget = 0u;
     int nActPrev = 0;
+    bool table = false;  // the tile table is valid (same in every CTA)
+    int myTile = -1;     // table steps: the tile this CTA held through the last step
+    // t as every CTA computes it (st->t gets the same FP64 sum); t_stop is
+    // fixed for the launch
+    double tNow = st->t;
+    const double tStop = st->t_stop;
+    int stepsDone = st->steps_done, tableSteps = st->tableSteps;  // used by CTA 0
     if (blockIdx.x == 0 && tid == 0) st->persistExit = 0;
 #define RIFT_SYNC()                          \
     if (!gridSync(P.gbar, barTarget, st)) return; \
     (void)0
     for (int step = 0; step < maxSteps; step++) {
-        // every CTA reads the same t (written before the last barrier)
-        if (st->t >= st->t_stop) {
+        if (tNow >= tStop) {
             if (blockIdx.x == 0 && tid == 0) st->stop = 1;
             return;
         }
@@ -256,70 +317,127 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             if (blockIdx.x == 0 && tid == 0) st->persistExit = 1;
             return;
         }
+        const int par = step & 1;  // parity of this step's reductions
         if (track) {
             trackTiles(P);
             RIFT_SYNC();
         }
-        if (blockIdx.x == 0 && tid == 0) beginStepResets(st);
-        growAppend<false>(P);
-        RIFT_SYNC();
-        const int nAct = (int)ld_relaxed_gpu((const unsigned*)&st->appendCnt[0]);
-        const int nDe = (int)ld_relaxed_gpu((const unsigned*)&st->appendCnt[1]);
-        nActPrev = nAct;
-        if (nAct <= (int)gridDim.x) {
+        int nAct, nDe = 0, tile = -1;
+        bool built = false;
+        if (table) {
+            if (blockIdx.x == 0 && tid == 0) {  // counters kept in registers: no load
+                st->stop = 0;
+                st->steps_done = ++stepsDone;
+                st->ticket = 0u;
+                st->tableSteps = ++tableSteps;
+            }
+            // a CTA that kept its tile still holds it (claims take free CTAs
+            // only); a free CTA looks whether a claim gave it one
+            tile = myTile >= 0 ? myTile : T->slotTile[blockIdx.x];
+            nAct = 0;  // not needed: every scheduled tile holds a CTA
+        } else {
+            if (blockIdx.x == 0 && tid == 0) {
+                beginStepResets(st);
+                stepsDone++;
+            }
+            growAppend<false>(P, T->staleb[par]);
+            for (int b = blockIdx.x * NT + tid; b < P.gridSize; b += gridDim.x * NT) {
+                P.tileFlag[b] = 0;
+                if (tableOk) P.owner[b] = -1;
+            }
+            RIFT_SYNC();
+            nAct = (int)ld_relaxed_gpu((const unsigned*)&st->appendCnt[0]);
+            nDe = (int)ld_relaxed_gpu((const unsigned*)&st->appendCnt[1]);
+            if (nAct <= (int)gridDim.x) {
+                tile = (int)blockIdx.x < nAct ? P.act[blockIdx.x] : -1;
+                if (tableOk) {
+                    if (tid == 0) tableBuild(P, nAct, tile);
+                    built = true;
+                }
+                myTile = tile;
+            }
+        }
+        if (table || nAct <= (int)gridDim.x) {
             // At most one tile per CTA: stage 1's fluxes of U^n are the first
             // ComputeFluxes of the step, so they give this step's tile speeds,
             // and the tile's divergence waits in registers (its staged block
             // in shared memory) across the barrier.  After the barrier every
             // CTA computes the step's dt from the maxima itself; the spare CTA
             // publishes it during stage 2, when no CTA reads the old value.
-            const bool mine = (int)blockIdx.x < nAct;
-            int tile = 0, bX, bY, i0 = 0, j0 = 0;
+            bool mine = tile >= 0;
+            int bX, bY, i0 = 0, j0 = 0;
             float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f;
             // t and dt of the previous step: published before the last barrier
             double tCur = 0.0, dtOld = 0.0;
             if (tid == 0) {
                 tCur = st->t;
                 dtOld = st->dt;
+                if (mine) issueTile(S.buf[0], &S.bar[0], &tmA, &tmE, P, tile);
             }
-            tileFirst(S, &tmA, &tmE, P, nAct);
+            bool wetOld = false, live = true;
             if (mine) {
-                tile = P.act[blockIdx.x];
                 tileOrigin(P, tile, bX, bY, i0, j0);
                 tilePrefetch<1>(P, stageConsts<1>(P), i0, j0, pre);
-                if (!tileAcquire(S, &tmA, &tmE, P, 0, ph, nAct, nAct)) {
+                wetOld = P.wet[tile] != 0;
+                if (table) live = tileGrows(P, tile);
+            }
+            if (table) scanTiles(P, T->staleb[par], &T->schedCnt[par], deList, &deCount);
+            if (mine) {
+                const bool ok = mbar_wait_bounded(&S.bar[0], ph[0]);
+                if (!__syncthreads_and(ok)) {
+                    mbar_wait_bounded(&S.bar[0], ph[0]);
                     if (tid == 0) atomicOr(&st->error, ERR_TMA_TIMEOUT);
                     return;
                 }
-                tileFluxDiv<true>(S, S.buf[0], P, i0, j0, dh, dhu, dhv, spx, spy);
-                const float mxv = blockMax(spx, S.red[0]);
-                const float myv = blockMax(spy, S.red[1]);
-                if (tid == 0) {
-                    P.mx[tile] = mxv;
-                    P.my[tile] = myv;
-                    atomicMax(&st->max_bits[0], __float_as_uint(mxv));
-                    atomicMax(&st->max_bits[1], __float_as_uint(myv));
+                ph[0] ^= 1u;
+                if (live) {
+                    tileFluxDiv<true>(S, S.buf[0], P, i0, j0, dh, dhu, dhv, spx, spy);
+                    const float mxv = blockMax(spx, S.red[0]);
+                    const float myv = blockMax(spy, S.red[1]);
+                    if (tid == 0) {
+                        P.mx[tile] = mxv;
+                        P.my[tile] = myv;
+                        atomicMax(&T->maxb[par][0], __float_as_uint(mxv));
+                        atomicMax(&T->maxb[par][1], __float_as_uint(myv));
+                        if (table) atomicAdd(&T->ownedCnt[par], 1);
+                    }
+                    __syncthreads();
+                } else {
+                    if (tid == 0) tableRelease(P, tile);
+                    mine = false;
                 }
-                __syncthreads();
+                myTile = mine ? tile : -1;
             }
             if (spare && tid < 32) beginStepRates(P, st);
-            resyncDeactivated(P, nDe);
+            if (!table) resyncDeactivated(P, nDe);
             RIFT_SYNC();
             // dt of this step (Simulator::ComputeTimestep), by thread 0 of
             // every CTA; the FP64 arithmetic stays in one thread
             if (tid == 0) {
-                const unsigned mx0 = ld_relaxed_gpu(&st->max_bits[0]);
-                const unsigned my0 = ld_relaxed_gpu(&st->max_bits[1]);
-                const unsigned mx1 = ld_relaxed_gpu(&st->staleBits[0]);
-                const unsigned my1 = ld_relaxed_gpu(&st->staleBits[1]);
+                const unsigned mx0 = ld_relaxed_gpu(&T->maxb[par][0]);
+                const unsigned my0 = ld_relaxed_gpu(&T->maxb[par][1]);
+                const unsigned mx1 = ld_relaxed_gpu(&T->staleb[par][0]);
+                const unsigned my1 = ld_relaxed_gpu(&T->staleb[par][1]);
+                int fail = 0, sched = nAct;
+                if (table) {
+                    const int owned = (int)ld_relaxed_gpu((const unsigned*)&T->ownedCnt[par]);
+                    sched = (int)ld_relaxed_gpu((const unsigned*)&T->schedCnt[par]);
+                    fail = owned != sched;
+                }
                 const double dtNew = stepDtAt(P, tCur, (double)__uint_as_float(max(mx0, mx1)),
                                               (double)__uint_as_float(max(my0, my1)));
                 const double tNew = tCur + dtNew;
                 sC[0] = stageConstsAt<1>(P, dtNew, dtOld, tNew);
                 sC[1] = stageConstsAt<2>(P, dtNew, dtOld, tNew);
                 sDt = dtNew;
+                sFail = fail;
+                sSched = sched;
+                if (fail && blockIdx.x == 0) atomicOr(&st->error, ERR_TILE_TABLE);
             }
             __syncthreads();
+            if (sFail) return;  // every CTA read the same counts
+            tNow = sC[1].tNew;
+            nActPrev = sSched;
             if (mine) {  // stage-1 update with this step's dt (Integrate_1_k)
                 const StageConsts C1 = sC[0];
                 const bool wetCell =
@@ -327,11 +445,20 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
                 __syncthreads();
             }
-            RIFT_SYNC();
-            if (!(fl & F_EULER)) {
-                // stage 2 of the same tile: its U* block into the second buffer
+            if (!euler) {
                 if (mine) {
-                    if (tid == 0) issueTile(S.buf[1], &S.bar[1], &tmB, &tmE, P, tile);
+                    // publish this tile's U*, wait for the scheduled neighbours'
+                    if (tid == 0) st_release_gpu(&P.tileFlag[tile], step + 1);
+                    const bool okN = tid < 4 ? waitNeighbour(P, tile, tid, step + 1) : true;
+                    if (!__syncthreads_and(okN)) {
+                        if (tid == 0) atomicOr(&st->error, ERR_BARRIER_TIMEOUT);
+                        return;
+                    }
+                    // stage 2 of the same tile: its U* block into the second buffer
+                    if (tid == 0) {
+                        fence_proxy_async_global();
+                        issueTile(S.buf[1], &S.bar[1], &tmB, &tmE, P, tile);
+                    }
                     const StageConsts C2 = sC[1];
                     tilePrefetch<2>(P, C2, i0, j0, pre);
                     const bool ok = mbar_wait_bounded(&S.bar[1], ph[1]);
@@ -345,24 +472,47 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                     tileFluxDiv<true>(S, S.buf[1], P, i0, j0, dh, dhu, dhv, sx2, sy2);
                     const bool wetCell =
                         tileCellUpdate<2>(P, C2, S.buf[1], tile, i0, j0, dh, dhu, dhv, pre);
-                    tileFlags<2>(P, C2, S, tile, wetCell, sx2, sy2);
+                    const bool wetNew = tileFlags<2>(P, C2, S, tile, wetCell, sx2, sy2);
+                    if ((table || built) && wetNew && !wetOld && tid < 4)
+                        tableClaim(P, tile, &sOverflow);
                     __syncthreads();
                 }
             } else {
+                RIFT_SYNC();
                 commitTiles(P, nAct);
             }
             if (spare && tid == 0) {
                 publishDt(P, st, sDt);
-                st->staleBits[0] = st->staleBits[1] = 0u;
-                publishGrow(st);
+                // the other parity: last read in the previous step
+                T->maxb[par ^ 1][0] = T->maxb[par ^ 1][1] = 0u;
+                T->staleb[par ^ 1][0] = T->staleb[par ^ 1][1] = 0u;
+                T->ownedCnt[par ^ 1] = T->schedCnt[par ^ 1] = 0;
+                if (table) {  // the scan's counts; the lists were not built
+                    st->nActive = sSched;
+                    st->nDeact = 0;
+                    st->nInact = -1;
+                    st->activeCells += st->appendCells;
+                    st->appendCells = 0ull;
+                } else {
+                    publishGrow(st);
+                }
             }
-            RIFT_SYNC();
+            int voided = 0;
+            if (!gridSync(P.gbar, barTarget, st, sOverflow != 0, &voided)) return;
+            if (tid == 0) sOverflow = 0;
+            table = (table || built) && voided == 0;
             continue;
         }
-        // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1
+        nActPrev = nAct;
+        // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1; the
+        // stale maxima of this step went to staleb[par]
         if (blockIdx.x == 0 && tid < 32) beginStepRates(P, st);
         float tmx = 0.f, tmy = 0.f;
         if (!speedTiles(S, &tmA, &tmE, P, nAct, ph, tmx, tmy)) return;
+        if (tid == 0) {
+            tmx = fmaxf(tmx, __uint_as_float(ld_relaxed_gpu(&T->staleb[par][0])));
+            tmy = fmaxf(tmy, __uint_as_float(ld_relaxed_gpu(&T->staleb[par][1])));
+        }
         __syncthreads();
         finishDt(P, tmx, tmy, &last);
         resyncDeactivated(P, nDe);
@@ -372,14 +522,20 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             sC[1] = stageConsts<2>(P);
         }
         __syncthreads();
+        tNow = sC[1].tNew;  // published by finishDt before the barrier
         if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph, &sC[0])) return;
         RIFT_SYNC();
-        if (!(fl & F_EULER)) {
+        if (!euler) {
             if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph, &sC[1])) return;
         } else {
             commitTiles(P, nAct);
         }
-        if (spare && tid == 0) publishGrow(st);
+        if (spare && tid == 0) {
+            T->maxb[par ^ 1][0] = T->maxb[par ^ 1][1] = 0u;
+            T->staleb[par ^ 1][0] = T->staleb[par ^ 1][1] = 0u;
+            T->ownedCnt[par ^ 1] = T->schedCnt[par ^ 1] = 0;
+            publishGrow(st);
+        }
         RIFT_SYNC();
     }
 #undef RIFT_SYNC

@@ -76,20 +76,30 @@ def test_engine_matches_reference_kernels(engine_api, name, schedule):
         assert persist_steps == 0 and graph_steps > 0
 
 
+def _scheduled_count(sim):
+    """Active tiles that hold interior cells (the persistent loop's count)."""
+    _, act = sim.tiles()
+    bx, by = act % sim.nBX, act // sim.nBX
+    return int(np.sum((bx * 16 + 2 <= sim.nx - 3) & (by * 14 + 2 <= sim.ny - 3)))
+
+
 def test_persistent_hands_over_to_graph(engine_api):
-    """A persistent threshold below the active-tile count makes the loop
-    leave after its first step and the per-step graph finish the run with
-    the same results as the graph alone."""
-    fx, case = FX.load("rain")
+    """A persistent threshold at the active count of step 2 (21 tiles) runs
+    the loop until the wet front grows the set past it (24 tiles at step 5);
+    the per-step graph then finishes the run, with the results of the graph
+    alone."""
+    fx, case = FX.load("front")
     runs = []
-    for persist in (1, 0):
-        eng = FX.start(_scheduled(capi.Sim(case, api=engine_api), "tiles").set_persistent(persist),
-                       fx)
+    for persist in (True, False):
+        eng = FX.start(_scheduled(capi.Sim(case, api=engine_api), "tiles").set_persistent(0), fx)
+        eng.run(2)
+        if persist:
+            eng.set_persistent(_scheduled_count(eng))
         eng.run(12)
         runs.append((eng.tiles(), eng.field("W"), eng.time(), eng.path_stats()))
     (w1, a1), W1, t1, st1 = runs[0]
     (w0, a0), W0, t0, st0 = runs[1]
-    assert st1[0] >= 1 and st1[1] >= 1 and st1[0] + st1[1] == 12
+    assert st1[0] >= 1 and st1[1] >= 3 and st1[0] + st1[1] == 14, st1
     assert np.array_equal(w1, w0) and np.array_equal(a1, a0)
     assert abs(t1[0] - t0[0]) <= 1e-6 * max(1.0, t0[0])
     _close(W1, W0, "persistent then graph vs graph")
