@@ -459,6 +459,10 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     h->pitch = ((h->nBX * TW + 8) + 31) / 32 * 32;
     h->rows = h->nBY * TH + 4;
     *out = h;
+    // cell offsets are 32-bit on the device: the largest field (4 planes)
+    // must stay below 2^32 elements
+    if (4.0 * (double)h->rows * (double)h->pitch >= 4294967296.0)
+        return fail(h, RIFT_ERR_TOO_LARGE, "grid above 2^32 cells per 4-plane field");
     cudaError_t e = cudaSetDevice(g->device);
     if (e != cudaSuccess) return fail(h, RIFT_ERR_CUDA, cudaGetErrorString(e));
     int dev = g->device;

@@ -134,8 +134,11 @@ struct Params {
     DevState* st;
 };
 
+// Offset of cell (j, i) of plane f: 32-bit arithmetic (the host keeps every
+// field below 2^32 elements), zero-extended.
 __device__ __forceinline__ size_t cidx(const Params& P, int f, int j, int i) {
-    return ((size_t)f * P.rows + j) * P.pitch + i;
+    return (size_t)(((unsigned)f * (unsigned)P.rows + (unsigned)j) * (unsigned)P.pitch +
+                    (unsigned)i);
 }
 
 // ---------------------------------------------------------------- PTX glue
@@ -783,11 +786,13 @@ __device__ __forceinline__ StageConsts stageConstsAt(const Params& P, double dtN
 // pre: the cell's own inputs loaded ahead of use -- stage 1: Manning n;
 // stage 2: U^n (h, hu, hv); with PREF also pre[3] = F entering the stage,
 // pre[4] = K, pre[5] = F^n (stage 2), else those are read here.
+// edge: the work item holds a cell next to the ghost band (i or j at 2 or
+// at n - 3); false skips the ghost tests for the items inside.
 template <int STAGE, bool PREF = false>
 __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
                                            int i, float dh, float dhu, float dhv, float hC,
                                            float hu0, float hv0, float eW, float eE, float eS,
-                                           float eN, const float* pre) {
+                                           float eN, const float* pre, bool edge = true) {
     const uint32_t fl = C.fl;
     const size_t c = cidx(P, 0, j, i);
     // bed-slope source, grid.cu:701,751-752
@@ -888,7 +893,7 @@ __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C
     C.Uout[cidx(P, 0, j, i)] = hN;
     C.Uout[cidx(P, 1, j, i)] = huN;
     C.Uout[cidx(P, 2, j, i)] = hvN;
-    writeGhosts(P, C.Uout, j, i, hN, huN, hvN);
+    if (edge) writeGhosts(P, C.Uout, j, i, hN, huN, hvN);
     return wetCell;
 }
 
@@ -1013,9 +1018,11 @@ __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConst
     const int i = i0 + tx, j = j0 + ty;
     if (tid >= TH * TW || i > P.nx - 3 || j > P.ny - 3) return false;
     const int r = ty + 2, c = tx + 2;
+    // tile-uniform: does the tile reach the first or last interior row/column?
+    const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
     return cellUpdate<STAGE, true>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][r][c], T.in[1][r][c],
                                    T.in[2][r][c], T.e[0][r][c], T.e[1][r][c], T.e[2][r][c],
-                                   T.e[3][r][c], pre);
+                                   T.e[3][r][c], pre, edge);
 }
 
 // Tile flags (stage 2, or stage 1 in Euler mode) and stage-2 tile speeds.

@@ -126,6 +126,9 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
         const int strip = P.strips[item];
         const int sx = strip % P.nSX, sy = strip / P.nSX;
         const int X0 = MCOLS * sx + 2, Y0 = MHR * sy + 2;
+        // strip-uniform: does the strip reach the first or last interior row/column?
+        const bool edgeStrip =
+            X0 == 2 || Y0 == 2 || X0 + MCOLS - 1 >= P.nx - 3 || Y0 + MHR - 1 >= P.ny - 3;
         const int xs = MCOLS * sx - 4, ys = Y0 - 2;
         const int i = X0 + lc;
         __syncthreads();  // the previous item no longer reads the ring or the tile tables
@@ -263,7 +266,8 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                     const float dhv = -(fE[2] - fW2) * P.inv_dx - (fN[2] - fS2) * P.inv_dy;
                     const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
                     accWet |= cellUpdate<STAGE>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
-                                                cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre);
+                                                cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre,
+                                                edgeStrip);
                 }
                 fS0 = fN[0];
                 fS1 = fN[1];

@@ -139,7 +139,7 @@ __device__ __forceinline__ void tableBuild(const Params& P, int nAct, int tile) 
     if (tile >= 0)
         P.owner[tile] = c;
     else
-        T->freeStack[c - nAct] = c;
+        T->freeStack[gridDim.x - 1 - c] = c;  // claims pop the lowest free CTA first
     if (c == 0) T->freeTop = (int)gridDim.x - nAct;
 }
 
@@ -148,12 +148,13 @@ __device__ __forceinline__ void tableBuild(const Params& P, int nAct, int tile) 
 // scheduled count over this CTA's chunk of tiles (what the grow does, less
 // the lists), into staleDst[2] and *schedDst.  deList/deCount: shared
 // scratch (NT entries, count 0).
+// The scan runs on CTAs rank 0 .. nRank-1 of the scanners.
 __device__ void scanTiles(const Params& P, unsigned* staleDst, int* schedDst, int* deList,
-                          int* deCount) {
+                          int* deCount, int rank, int nRank) {
     DevState* s = P.st;
     const int tid = threadIdx.x, lane = tid & 31;
-    const int per = (P.gridSize + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int b0 = min(P.gridSize, (int)blockIdx.x * per), b1 = min(P.gridSize, b0 + per);
+    const int per = (P.gridSize + nRank - 1) / nRank;
+    const int b0 = min(P.gridSize, rank * per), b1 = min(P.gridSize, b0 + per);
     int sched = 0;
     unsigned long long cells = 0ull;
     float smx = 0.f, smy = 0.f;
@@ -299,6 +300,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
     int nActPrev = 0;
     bool table = false;  // the tile table is valid (same in every CTA)
     int myTile = -1;     // table steps: the tile this CTA held through the last step
+    int nScan = 1;       // table steps: CTAs of the scan (the last nScan)
     // t as every CTA computes it (st->t gets the same FP64 sum); t_stop is
     // fixed for the launch
     double tNow = st->t;
@@ -353,6 +355,8 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 if (tableOk) {
                     if (tid == 0) tableBuild(P, nAct, tile);
                     built = true;
+                    const int freeCtas = (int)gridDim.x - nAct;
+                    nScan = freeCtas >= 32 ? freeCtas : (int)gridDim.x;
                 }
                 myTile = tile;
             }
@@ -381,7 +385,12 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 wetOld = P.wet[tile] != 0;
                 if (table) live = tileGrows(P, tile);
             }
-            if (table) scanTiles(P, T->staleb[par], &T->schedCnt[par], deList, &deCount);
+            // the scan runs on the CTAs that were free at the rebuild (the
+            // highest ones; claims take the lowest free CTA first), so the
+            // tile CTAs' flux phase does not wait for it
+            if (table && (int)blockIdx.x >= (int)gridDim.x - nScan)
+                scanTiles(P, T->staleb[par], &T->schedCnt[par], deList, &deCount,
+                          (int)blockIdx.x - ((int)gridDim.x - nScan), nScan);
             if (mine) {
                 const bool ok = mbar_wait_bounded(&S.bar[0], ph[0]);
                 if (!__syncthreads_and(ok)) {
@@ -418,6 +427,10 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 const unsigned my0 = ld_relaxed_gpu(&T->maxb[par][1]);
                 const unsigned mx1 = ld_relaxed_gpu(&T->staleb[par][0]);
                 const unsigned my1 = ld_relaxed_gpu(&T->staleb[par][1]);
+                // the step's rates (the spare CTA wrote them before the barrier),
+                // loaded with the maxima in one round trip
+                const float rainU = __uint_as_float(ld_relaxed_gpu((const unsigned*)&st->rain_rate));
+                const float drainU = __uint_as_float(ld_relaxed_gpu((const unsigned*)&st->drain_rate));
                 int fail = 0, sched = nAct;
                 if (table) {
                     const int owned = (int)ld_relaxed_gpu((const unsigned*)&T->ownedCnt[par]);
@@ -427,8 +440,12 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 const double dtNew = stepDtAt(P, tCur, (double)__uint_as_float(max(mx0, mx1)),
                                               (double)__uint_as_float(max(my0, my1)));
                 const double tNew = tCur + dtNew;
-                sC[0] = stageConstsAt<1>(P, dtNew, dtOld, tNew);
-                sC[1] = stageConstsAt<2>(P, dtNew, dtOld, tNew);
+                StageConsts c1 = stageConstsAt<1>(P, dtNew, dtOld, tNew);
+                StageConsts c2 = stageConstsAt<2>(P, dtNew, dtOld, tNew);
+                c1.rainU = c2.rainU = rainU;
+                c1.drainU = c2.drainU = drainU;
+                sC[0] = c1;
+                sC[1] = c2;
                 sDt = dtNew;
                 sFail = fail;
                 sSched = sched;
