@@ -59,6 +59,7 @@ struct rift_handle {
     rift_grid_desc g{};
     int nx = 0, ny = 0, nBX = 0, nBY = 0, gridSize = 0, pitch = 0, rows = 0;
     int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0, gridMarch = 0;
+    int gridUpdate = 0;  // k_update1: resident CTAs over half-strip items
     int nSX = 0, nSY = 0;
     int marchMin = 0;  // active strips from which the march kernels run
     int gridGrow = 0;      // CTAs of the grow kernel of the graph path
@@ -73,6 +74,7 @@ struct rift_handle {
     CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
     cudaStream_t stream = nullptr;
     float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
+    float* D = nullptr;  // [3] planes: the march's stage-1 divergence
     float *FA = nullptr, *FB = nullptr, *hmax = nullptr, *qmax = nullptr, *twet = nullptr;
     float *tpeak = nullptr, *tdry = nullptr;
     float* maps[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
@@ -152,6 +154,8 @@ Params makeParams(rift_handle* h) {
     P.flags = h->g.flags;
     P.A = h->A;
     P.B = h->B;
+    P.D = h->D;
+    P.planeSize = (int)h->plane();
     P.E = h->E;
     P.nman = h->nman;
     P.K = h->K;
@@ -232,9 +236,9 @@ void enqueueStep(rift_handle* h) {
     // per-tile and march variants of each pass; the device keeps one of them
     // (useMarch) and the other returns at once
     k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
-    k_march<0><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+    k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);  // fluxes, speeds, dt
     k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
-    k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+    k_update1<<<h->gridUpdate, MT, 0, s>>>(P);
     if (!h->has(RIFT_F_EULER)) {
         k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
         k_march<2><<<h->gridMarch, MT, 0, s>>>(h->tmBm, h->tmEm, P);
@@ -471,6 +475,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     const size_t pl = h->plane() * 4;
     CUDA_TRY(h, cudaMalloc(&h->A, 3 * pl));
     CUDA_TRY(h, cudaMalloc(&h->B, 3 * pl));
+    CUDA_TRY(h, cudaMalloc(&h->D, 3 * pl));
     CUDA_TRY(h, cudaMalloc(&h->E, 4 * pl));
     CUDA_TRY(h, cudaMalloc(&h->nman, pl));
     CUDA_TRY(h, cudaMemset(h->A, 0, 3 * pl));
@@ -529,6 +534,9 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_march<2>, MT, 0);
     if (occ < 1) occ = 1;
     h->gridMarch = std::max(1, std::min(NS, h->numSMs * occ));
+    int occU = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1, MT, 0);
+    h->gridUpdate = std::max(1, std::min(2 * NS, h->numSMs * std::max(occU, 1)));
     // the march pays off once every resident march CTA has a strip of its own
     h->marchMin = h->numSMs * occ;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_speed_dt, NT, 0);
@@ -1230,10 +1238,10 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
             k_track<<<h->gridTrack, NT, 0, s>>>(P);
         k_grow<<<h->gridGrow, NT, 0, s>>>(P);
         k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
-        k_march<0><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
         CUDA_TRY(h, cudaEventRecord(e0, s));
-        k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
         k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+        k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
+        k_update1<<<h->gridUpdate, MT, 0, s>>>(P);
         if (!h->has(RIFT_F_EULER)) {
             k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
             k_march<2><<<h->gridMarch, MT, 0, s>>>(h->tmBm, h->tmEm, P);
@@ -1481,7 +1489,7 @@ void rift_destroy(rift_handle* h) {
     if (!h) return;
     destroyGraph(h);
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (float* p : {h->A, h->B, h->E, h->nman, h->K, h->FA, h->FB, h->hmax, h->qmax, h->twet,
+    for (float* p : {h->A, h->B, h->D, h->E, h->nman, h->K, h->FA, h->FB, h->hmax, h->qmax, h->twet,
                      h->tpeak, h->tdry, h->mx, h->my, h->srcRate, h->serT, h->serR})
         if (p) cudaFree(p);
     for (int k = 0; k < 3; k++)

@@ -95,6 +95,8 @@ struct Params {
     uint32_t flags;
     float* A;          // [3][rows][pitch]  U^n / U^{n+1}: h, hu, hv
     float* B;          // [3][rows][pitch]  U*
+    float* D;          // [3][rows][pitch]  stage-1 flux divergence + bed source (march)
+    int planeSize;     // rows * pitch
     const float* E;    // [4][rows][pitch]  eW, eE, eS, eN
     const float* nman; // [rows][pitch]
     const float* K;
@@ -240,6 +242,21 @@ __device__ __forceinline__ float mapValue(const Params& P, int which, size_t c, 
     if (x1 == nd) return x0;
     if (x0 == nd) return x1;
     return factor * (x1 - x0) + x0;
+}
+
+// L1 prefetch of the gridded maps a cell update will read (rain, drain,
+// surge), issued a row or a group of rows ahead.
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+__device__ __forceinline__ void prefetchMaps(const Params& P, uint32_t fl, size_t c) {
+    const uint32_t use[3] = {F_RAIN_G, F_DRAIN_G, F_SURGE};
+#pragma unroll
+    for (int w = 0; w < 3; w++) {
+        if (!(fl & use[w]) || P.mapMode[w] == 0) continue;
+        prefetch_l1(P.map0[w] + c);
+        if (P.mapMode[w] == 2) prefetch_l1(P.map1[w] + c);
+    }
 }
 
 // Block-wide max (non-negative values); result valid in thread 0.
@@ -786,18 +803,26 @@ __device__ __forceinline__ StageConsts stageConstsAt(const Params& P, double dtN
 // pre: the cell's own inputs loaded ahead of use -- stage 1: Manning n;
 // stage 2: U^n (h, hu, hv); with PREF also pre[3] = F entering the stage,
 // pre[4] = K, pre[5] = F^n (stage 2), else those are read here.
+// Bed-slope source of the momentum equations (grid.cu:701,751-752).
+__device__ __forceinline__ float bedSourceX(const Params& P, float hC, float eW, float eE) {
+    return -kG * hC * ((eE - eW) * P.inv_dx);
+}
+__device__ __forceinline__ float bedSourceY(const Params& P, float hC, float eS, float eN) {
+    return -kG * hC * ((eN - eS) * P.inv_dy);
+}
+
 // edge: the work item holds a cell next to the ghost band (i or j at 2 or
 // at n - 3); false skips the ghost tests for the items inside.
-template <int STAGE, bool PREF = false>
+// BED: add the bed-slope source here (false: the caller's dhu, dhv hold it).
+template <int STAGE, bool PREF = false, bool BED = true>
 __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
                                            int i, float dh, float dhu, float dhv, float hC,
                                            float hu0, float hv0, float eW, float eE, float eS,
                                            float eN, const float* pre, bool edge = true) {
     const uint32_t fl = C.fl;
     const size_t c = cidx(P, 0, j, i);
-    // bed-slope source, grid.cu:701,751-752
-    const float S1 = -kG * hC * ((eE - eW) * P.inv_dx);
-    const float S2 = -kG * hC * ((eN - eS) * P.inv_dy);
+    const float S1 = BED ? bedSourceX(P, hC, eW, eE) : 0.f;
+    const float S2 = BED ? bedSourceY(P, hC, eS, eN) : 0.f;
     // mass sources, grid.cu:763-807
     float S0 = 0.f;
     if (fl & F_RAIN_U) S0 += C.rainU;
@@ -830,8 +855,10 @@ __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C
         S0 -= dF;
     }
     dh += S0;
-    dhu += S1;
-    dhv += S2;
+    if (BED) {
+        dhu += S1;
+        dhv += S2;
+    }
     const float hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
     const float dtNew = C.dtNew;
     float hN, huN, hvN;

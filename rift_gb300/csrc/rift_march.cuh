@@ -17,6 +17,13 @@
 // refilled as the march moves up (one barrier per chunk).
 // A cell is updated only when its reference tile is active, so results and
 // tile flags are those of the per-tile schedule of the reference.
+//
+// Stage 1 needs dt, and dt needs the speeds of stage 1's own fluxes (the
+// first ComputeFluxes of the step).  So the stage-1 march computes the
+// fluxes, the tile speeds and dt (last CTA), and stores each cell's flux
+// divergence with the bed-slope source folded in (3 words); k_update1 then
+// applies the rest of Integrate_1_k.  The step does one flux pass per stage
+// and no separate speed pass.
 #pragma once
 #include "rift_kernels.cuh"
 
@@ -92,10 +99,9 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
         mbar_wait_bounded(&S.bar[k % MNSLOT], (par >> (k % MNSLOT)) & 1u);
 }
 
-// STAGE 0: reads U^n (A) -> tile speed maxima, dt and t (the speed output of
-//          the first ComputeFluxes and ComputeTimestep), re-sync of U* on
-//          tiles that went inactive.
-// STAGE 1: reads U^n (A) -> writes U* (B), F* (FB).
+// STAGE 1: reads U^n (A) -> flux divergence + bed source (D), tile speed
+//          maxima, dt and t (ComputeFluxes' speed output and
+//          ComputeTimestep), re-sync of U* on tiles that went inactive.
 // STAGE 2: reads U* (B) and U^n (A) at the cell -> writes U^{n+1} (A),
 //          F^{n+1} (FA), outputs, tile wet flags and tile speeds.
 template <int STAGE>
@@ -106,7 +112,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
     if (P.st->stop || !useMarch(P)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nItems = P.st->nStrips;
-    const StageConsts C = stageConsts<STAGE == 0 ? 1 : STAGE>(P);
+    const StageConsts C = stageConsts<STAGE>(P);
     float tmxAll = 0.f, tmyAll = 0.f;
     if (tid == 0) {
         prefetch_tmap(&tmIn);
@@ -158,14 +164,8 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
         const Row r1 = loadRow(S.slot[0], 1, col);
         Row cur = loadRow(S.slot[0], 2, col);
         Row nxt = loadRow(S.slot[0], 3, col);
-        float fS0 = 0.f, fS1 = 0.f, fS2 = 0.f, yPh, yPu, yPv;
-        if (STAGE == 0) {
-            const RecN y2 = constructN(cur.h, cur.v, nxt.h, nxt.v, r1.h, r1.v, cur.eS, cur.eN,
-                                       cur.eN - nxt.eS, r1.eN - cur.eS);
-            yPh = y2.hP;
-            yPv = y2.qP;
-            yPu = 0.f;
-        } else {
+        float fS0, fS1, fS2, yPh, yPu, yPv;
+        {
             const Rec y1 = constructY(r0, r1, cur);
             const Rec y2 = constructY(r1, cur, nxt);
             float f[3];
@@ -177,17 +177,13 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
             yPu = y2.uP;
             yPv = y2.vP;
         }
-        // centre values of the first output row, loaded ahead of use
+        // centre values of the first output row (stage 2: U^n), loaded ahead of use
         const bool colIn = owned && i <= P.nx - 3;
         float pre[3] = {0.f, 0.f, 0.f}, nextPre[3] = {0.f, 0.f, 0.f};
-        if (STAGE != 0 && colIn && Y0 <= P.ny - 3) {
-            if (STAGE == 1) {
-                pre[0] = P.nman[cidx(P, 0, Y0, i)];
-            } else {
-                pre[0] = P.A[cidx(P, 0, Y0, i)];
-                pre[1] = P.A[cidx(P, 1, Y0, i)];
-                pre[2] = P.A[cidx(P, 2, Y0, i)];
-            }
+        if (STAGE == 2 && colIn && Y0 <= P.ny - 3) {
+            pre[0] = P.A[cidx(P, 0, Y0, i)];
+            pre[1] = P.A[cidx(P, 1, Y0, i)];
+            pre[2] = P.A[cidx(P, 2, Y0, i)];
         }
         float accMx = 0.f, accMy = 0.f;
         bool accWet = false;
@@ -211,35 +207,17 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
             const Row ld = loadRow(S.slot[(lead / MRC) % MNSLOT], lead % MRC, col);
             const int j = Y0 + R - 2;
             // centre values of the next output row, in flight during this one
-            if (STAGE != 0 && colIn && j + 1 <= P.ny - 3) {
-                if (STAGE == 1) {
-                    nextPre[0] = P.nman[cidx(P, 0, j + 1, i)];
-                } else {
-                    nextPre[0] = P.A[cidx(P, 0, j + 1, i)];
-                    nextPre[1] = P.A[cidx(P, 1, j + 1, i)];
-                    nextPre[2] = P.A[cidx(P, 2, j + 1, i)];
-                }
+            if (STAGE == 2 && colIn && j + 1 <= P.ny - 3) {
+                const size_t cn = cidx(P, 0, j + 1, i);
+                nextPre[0] = P.A[cn];
+                nextPre[1] = P.A[cn + P.planeSize];
+                nextPre[2] = P.A[cn + 2 * (size_t)P.planeSize];
+                prefetchMaps(P, C.fl, cn);
             }
             const int tslot = ((R - 2) / TH) * STRIP_TX + tcol;
             const bool cellOn = colIn && S.tact[tslot] && j <= P.ny - 3;
             float spx, spy;
-            if (STAGE == 0) {
-                // speeds only: depth + normal momentum reconstructions
-                const RecN yn = constructN(nxt.h, nxt.v, ld.h, ld.v, cur.h, cur.v, nxt.eS, nxt.eN,
-                                           nxt.eN - ld.eS, cur.eN - nxt.eS);
-                spy = faceSpeed(yPh, yPv, yn.hM, yn.qM, kappa);
-                const float hm = __shfl_up_sync(FULL, cur.h, 1), hp = __shfl_down_sync(FULL, cur.h, 1);
-                const float um = __shfl_up_sync(FULL, cur.u, 1), up = __shfl_down_sync(FULL, cur.u, 1);
-                const float eEm = __shfl_up_sync(FULL, cur.eE, 1);
-                const float eWp = __shfl_down_sync(FULL, cur.eW, 1);
-                const RecN xr = constructN(cur.h, cur.u, hp, up, hm, um, cur.eW, cur.eE,
-                                           cur.eE - eWp, eEm - cur.eW);
-                const float rh = __shfl_down_sync(FULL, xr.hM, 1);
-                const float rq = __shfl_down_sync(FULL, xr.qM, 1);
-                spx = faceSpeed(xr.hP, xr.qP, rh, rq, kappa);
-                yPh = yn.hP;
-                yPv = yn.qP;
-            } else {
+            {
                 // y: reconstruction of row R+1, flux through the north face of row R
                 const Rec yn = constructY(cur, nxt, ld);
                 float fN[3];
@@ -264,10 +242,18 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                     const float dh = -(fE[0] - fW0) * P.inv_dx - (fN[0] - fS0) * P.inv_dy;
                     const float dhu = -(fE[1] - fW1) * P.inv_dx - (fN[1] - fS1) * P.inv_dy;
                     const float dhv = -(fE[2] - fW2) * P.inv_dx - (fN[2] - fS2) * P.inv_dy;
-                    const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
-                    accWet |= cellUpdate<STAGE>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
-                                                cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre,
-                                                edgeStrip);
+                    if (STAGE == 1) {
+                        // divergence + bed-slope source (dt-free) for k_update1
+                        const size_t c = cidx(P, 0, j, i);
+                        P.D[c] = dh;
+                        P.D[c + P.planeSize] = dhu + bedSourceX(P, cur.h, cur.eW, cur.eE);
+                        P.D[c + 2 * (size_t)P.planeSize] = dhv + bedSourceY(P, cur.h, cur.eS, cur.eN);
+                    } else {
+                        const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
+                        accWet |= cellUpdate<STAGE>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
+                                                    cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre,
+                                                    edgeStrip);
+                    }
                 }
                 fS0 = fN[0];
                 fS1 = fN[1];
@@ -282,11 +268,9 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
             }
             if ((R - 2) % TH == TH - 1) {  // last row of a tile row: fold into the tile
                 if (owned) {
-                    if (STAGE != 1) {
-                        atomicMax(&S.tmx[tslot], __float_as_uint(accMx));
-                        atomicMax(&S.tmy[tslot], __float_as_uint(accMy));
-                    }
-                    if ((STAGE == 2 || C.euler) && accWet) atomicOr(&S.twet[tslot], 1);
+                    atomicMax(&S.tmx[tslot], __float_as_uint(accMx));
+                    atomicMax(&S.tmy[tslot], __float_as_uint(accMy));
+                    if (STAGE == 2 && accWet) atomicOr(&S.twet[tslot], 1);
                 }
                 accMx = 0.f;
                 accMy = 0.f;
@@ -302,14 +286,11 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
         if (tid < STRIP_TX * STRIP_TY && S.tact[tid]) {
             const int bx = STRIP_TX * sx + tid % STRIP_TX, by = STRIP_TY * sy + tid / STRIP_TX;
             const int b = by * P.nBX + bx;
-            if (STAGE != 0 && (STAGE == 2 || C.euler))
-                P.wet[b] = (uint8_t)((!(C.fl & F_TILE_ACC)) || S.twet[tid]);
-            if (STAGE != 1) {
-                P.mx[b] = __uint_as_float(S.tmx[tid]);
-                P.my[b] = __uint_as_float(S.tmy[tid]);
-            }
+            if (STAGE == 2) P.wet[b] = (uint8_t)((!(C.fl & F_TILE_ACC)) || S.twet[tid]);
+            P.mx[b] = __uint_as_float(S.tmx[tid]);
+            P.my[b] = __uint_as_float(S.tmy[tid]);
         }
-        if (STAGE == 0) {  // thread 0 keeps this CTA's maximum of new tile speeds
+        if (STAGE == 1) {  // thread 0 keeps this CTA's maximum of new tile speeds
             __syncthreads();
             if (tid == 0)
                 for (int k = 0; k < STRIP_TX * STRIP_TY; k++)
@@ -319,10 +300,86 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                     }
         }
     }
-    if (STAGE == 0) {
+    if (STAGE == 1) {
         __syncthreads();
         finishDt(P, tmxAll, tmyAll, &last);
         resyncDeactivated(P);
+    }
+}
+
+// The rest of Integrate_1_k (grid.cu:856-1023) on the march's strips, once
+// dt is known: sources, friction, the RK stage, outputs and ghost cells, from
+// U^n and the stored divergence; in Euler mode also the tile wet flags.  No
+// halo, so the work item is half a strip (one tile row of 7 tiles): finer
+// items balance the grid.  One thread per column, rows in groups of four
+// whose loads are in flight together.
+__global__ void __launch_bounds__(MT) k_update1(Params P) {
+    __shared__ int tact[STRIP_TX];
+    __shared__ int twet[STRIP_TX];
+    if (P.st->stop || !useMarch(P)) return;
+    const int tid = threadIdx.x;
+    const int nItems = 2 * P.st->nStrips;
+    const StageConsts C = stageConsts<1>(P);
+    const size_t pl = (size_t)P.planeSize;
+    for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
+        const int strip = P.strips[item >> 1];
+        const int half = item & 1;
+        const int sx = strip % P.nSX, sy = strip / P.nSX;
+        const int by = STRIP_TY * sy + half;  // the tile row of this item
+        const int X0 = MCOLS * sx + 2, Y0 = by * TH + 2;
+        const bool edgeStrip =
+            X0 == 2 || Y0 == 2 || X0 + MCOLS - 1 >= P.nx - 3 || Y0 + TH - 1 >= P.ny - 3;
+        __syncthreads();  // the previous item no longer reads the tile tables
+        if (tid < STRIP_TX) {
+            const int bx = STRIP_TX * sx + tid;
+            int a = 0;
+            if (bx < P.nBX && by < P.nBY)
+                a = P.prevAct[by * P.nBX + bx] && (bx * TW + 2 <= P.nx - 3) && (Y0 <= P.ny - 3);
+            tact[tid] = a;
+            twet[tid] = 0;
+        }
+        __syncthreads();
+        const int i = X0 + tid, slot = tid / TW;
+        if (tid < MCOLS && i <= P.nx - 3 && tact[slot]) {
+            const int tile = by * P.nBX + STRIP_TX * sx + slot;
+            constexpr int G = 4;
+            bool wetAny = false;
+            for (int r0 = 0; r0 < TH; r0 += G) {
+                float v[G][7];
+                bool on[G];
+#pragma unroll
+                for (int q = 0; q < G; q++) {
+                    const int j = Y0 + r0 + q;
+                    on[q] = r0 + q < TH && j <= P.ny - 3;
+                    if (on[q]) {
+                        const size_t c = cidx(P, 0, j, i);
+                        v[q][0] = P.D[c];
+                        v[q][1] = P.D[c + pl];
+                        v[q][2] = P.D[c + 2 * pl];
+                        v[q][3] = P.A[c];
+                        v[q][4] = P.A[c + pl];
+                        v[q][5] = P.A[c + 2 * pl];
+                        v[q][6] = P.nman[c];
+                        prefetchMaps(P, C.fl, c);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < G; q++) {
+                    if (!on[q]) continue;
+                    const float pre[1] = {v[q][6]};
+                    wetAny |= cellUpdate<1, false, false>(P, C, tile, Y0 + r0 + q, i, v[q][0],
+                                                          v[q][1], v[q][2], v[q][3], v[q][4],
+                                                          v[q][5], 0.f, 0.f, 0.f, 0.f, pre,
+                                                          edgeStrip);
+                }
+            }
+            if (C.euler && wetAny) atomicOr(&twet[slot], 1);
+        }
+        if (C.euler) {
+            __syncthreads();
+            if (tid < STRIP_TX && tact[tid])
+                P.wet[by * P.nBX + STRIP_TX * sx + tid] = (uint8_t)((!(C.fl & F_TILE_ACC)) || twet[tid]);
+        }
     }
 }
 
