@@ -510,40 +510,76 @@ __device__ __forceinline__ void beginStepResets(DevState* s) {
             s->factor[w] = (float)((s->t - s->map_t0[w]) / (s->map_t1[w] - s->map_t0[w]));
 }
 
-// Start of a step, part 2, by one whole warp: the uniform source rates at
-// float(t).  Only the cell updates and the volume ledger read them, so it
-// may run any time between the previous step's stage 2 and this step's
-// stage 1.  The FP64 conversion of the hydrograph runs in one lane.
-__device__ void beginStepRates(const Params& P, DevState* s) {
+// The step's uniform source rates at float(t) from the series state (one
+// whole warp; writes nothing).  interp[w] gets the new series state.  The
+// FP64 conversion of the hydrograph runs in one lane.
+struct StepRates {
+    float rainU, drainU, srcR;
+    float interp[3];
+};
+
+// From the previous step's rates and series state `prev` (the rates of a
+// series that is not set stay as they are).
+__device__ StepRates stepRatesFrom(const Params& P, const StepRates& prev, double t) {
     const int lane = threadIdx.x & 31;
-    const float tf = (float)s->t;
+    const float tf = (float)t;
+    StepRates q = prev;
+    q.srcR = 0.f;
     if (P.serN[2] > 0) {  // hydrograph, cfs -> m^3/s -> m/s per source cell
         float v = seriesInterp(P.serT + 2 * MAX_SERIES, P.serR + 2 * MAX_SERIES, P.serN[2], tf,
-                               s->ser_interp[2]);
+                               q.interp[2]);
         v = __fdiv_rn(v, 35.3147f);
         float r = 0.f;
         if (lane == 0) r = (float)((double)v / P.dxd / P.dyd / (double)P.nsrc);
-        r = __shfl_sync(0xffffffffu, r, 0);
-        for (int k = lane; k < P.nsrc; k += 32) P.srcRate[k] = r;
-        if (lane == 0) s->ser_interp[2] = v;
+        q.srcR = __shfl_sync(0xffffffffu, r, 0);
+        q.interp[2] = v;
     }
     if (P.serN[0] > 0) {  // hyetograph, mm/hr -> m/s
-        float v = seriesInterp(P.serT, P.serR, P.serN[0], tf, s->ser_interp[0]);
+        float v = seriesInterp(P.serT, P.serR, P.serN[0], tf, q.interp[0]);
         v = __fdiv_rn(v, 3600.f * 1000.f);
-        if (lane == 0) {
-            s->ser_interp[0] = v;
-            s->rain_rate = v;
-        }
+        q.interp[0] = v;
+        q.rainU = v;
     }
     if (P.serN[1] > 0) {  // drain, mm/hr -> m/s
         float v = seriesInterp(P.serT + MAX_SERIES, P.serR + MAX_SERIES, P.serN[1], tf,
-                               s->ser_interp[1]);
+                               q.interp[1]);
         v = __fdiv_rn(v, 3600.f * 1000.f);
-        if (lane == 0) {
-            s->ser_interp[1] = v;
-            s->drain_rate = v;
-        }
+        q.interp[1] = v;
+        q.drainU = v;
     }
+    return q;
+}
+
+// From the device state.
+__device__ StepRates stepRates(const Params& P, const DevState* s, double t) {
+    StepRates prev;
+    prev.rainU = s->rain_rate;
+    prev.drainU = s->drain_rate;
+    prev.srcR = 0.f;
+    for (int w = 0; w < 3; w++) prev.interp[w] = s->ser_interp[w];
+    return stepRatesFrom(P, prev, t);
+}
+
+// The rates and the series state into the device state (one whole warp).
+__device__ void writeRates(const Params& P, DevState* s, const StepRates& q) {
+    const int lane = threadIdx.x & 31;
+    if (P.serN[2] > 0)
+        for (int k = lane; k < P.nsrc; k += 32) P.srcRate[k] = q.srcR;
+    if (lane == 0) {
+        for (int w = 0; w < 3; w++)
+            if (P.serN[w] > 0) s->ser_interp[w] = q.interp[w];
+        if (P.serN[0] > 0) s->rain_rate = q.rainU;
+        if (P.serN[1] > 0) s->drain_rate = q.drainU;
+    }
+    __syncwarp();
+}
+
+// Start of a step, part 2, by one whole warp: the uniform source rates into
+// the device state.  Only the cell updates and the volume ledger read them,
+// so it may run any time between the previous step's stage 2 and this
+// step's stage 1.
+__device__ void beginStepRates(const Params& P, DevState* s) {
+    writeRates(P, s, stepRates(P, s, s->t));
 }
 
 // Start of a step, by one whole warp: both parts.
@@ -752,6 +788,7 @@ __device__ __forceinline__ void writeGhosts(const Params& P, float* U, int j, in
 // Step-wide constants of a stage kernel.
 struct StageConsts {
     float kappa, dtNew, dtSrc, invDtSrc, rainU, drainU, fac0, fac1, fac2;
+    float srcR;  // the hydrograph's rate per source cell (every source holds it)
     double tNew;
     uint32_t fl;
     bool euler;
@@ -778,10 +815,21 @@ __device__ __forceinline__ StageConsts stageConsts(const Params& P) {
     C.fac0 = st->factor[0];
     C.fac1 = st->factor[1];
     C.fac2 = st->factor[2];
+    C.srcR = (P.serN[2] > 0 && P.nsrc > 0) ? P.srcRate[0] : 0.f;
     C.Uout = (STAGE == 1) ? P.B : P.A;
     C.Fin = (STAGE == 1) ? P.FA : P.FB;
     C.Fout = (STAGE == 1) ? P.FB : P.FA;
     return C;
+}
+
+// stageConsts by thread 0, shared with the CTA (the FP64 loads and
+// conversions once per CTA, not per thread).  Every thread of the CTA calls it.
+template <int STAGE>
+__device__ __forceinline__ StageConsts blockConsts(const Params& P) {
+    __shared__ StageConsts sc;
+    if (threadIdx.x == 0) sc = stageConsts<STAGE>(P);
+    __syncthreads();
+    return sc;
 }
 
 // stageConsts with the step's dt, previous dt and t given by the caller
@@ -811,14 +859,26 @@ __device__ __forceinline__ float bedSourceY(const Params& P, float hC, float eS,
     return -kG * hC * ((eN - eS) * P.inv_dy);
 }
 
-// edge: the work item holds a cell next to the ghost band (i or j at 2 or
-// at n - 3); false skips the ghost tests for the items inside.
+// The per-cell update is split at dt: cellSources is everything that does
+// not need the step's dt (for stage 1: the bed slope, the mass sources with
+// their clamps at the previous dt, infiltration, Manning's G), cellFinish the
+// rest.  cellUpdate runs both; the persistent loop runs cellSources before
+// its dt barrier.
+struct CellSrc {
+    float dh, dhu, dhv;  // divergence + sources
+    float hc;            // depth clamped at epsilon (grid.cu:748-749)
+    float Fc, dF;        // infiltration: F entering the stage, rate
+    float rainG;         // gridded rain at the cell
+    float G;             // stage 1: semi-implicit Manning coefficient
+    bool srcCell;        // the cell holds a point source
+};
+
 // BED: add the bed-slope source here (false: the caller's dhu, dhv hold it).
 template <int STAGE, bool PREF = false, bool BED = true>
-__device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
-                                           int i, float dh, float dhu, float dhv, float hC,
-                                           float hu0, float hv0, float eW, float eE, float eS,
-                                           float eN, const float* pre, bool edge = true) {
+__device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConsts& C, int tile,
+                                               int j, int i, float dh, float dhu, float dhv,
+                                               float hC, float hu0, float hv0, float eW, float eE,
+                                               float eS, float eN, const float* pre) {
     const uint32_t fl = C.fl;
     const size_t c = cidx(P, 0, j, i);
     const float S1 = BED ? bedSourceX(P, hC, eW, eE) : 0.f;
@@ -843,7 +903,7 @@ __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C
         for (int q = P.srcTileStart[tile]; q < P.srcTileStart[tile + 1]; q++) {
             int sidx = P.srcTileList[q];
             if (P.srcIdx[sidx] == flat) {
-                S0 += P.srcRate[sidx];
+                S0 += P.serN[2] > 0 ? C.srcR : P.srcRate[sidx];
                 srcCell = true;
             }
         }
@@ -859,13 +919,37 @@ __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C
         dhu += S1;
         dhv += S2;
     }
-    const float hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
+    CellSrc r;
+    r.dh = dh;
+    r.dhu = dhu;
+    r.dhv = dhv;
+    r.hc = (hC > kEps) ? hC : 0.f;  // grid.cu:748-749
+    r.Fc = Fc;
+    r.dF = dF;
+    r.rainG = rainG;
+    r.srcCell = srcCell;
+    r.G = STAGE == 1 ? manningG(pre[0], hu0, hv0, hC, C.kappa) : 0.f;
+    return r;
+}
+
+// edge: the work item holds a cell next to the ghost band (i or j at 2 or
+// at n - 3); false skips the ghost tests for the items inside.
+template <int STAGE, bool PREF = false>
+__device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C, int j, int i,
+                                           const CellSrc& src, float hC, float hu0, float hv0,
+                                           const float* pre, bool edge) {
+    const uint32_t fl = C.fl;
+    const size_t c = cidx(P, 0, j, i);
+    float dh = src.dh;
+    const float dhu = src.dhu, dhv = src.dhv, hc = src.hc, Fc = src.Fc, dF = src.dF;
+    const float rainG = src.rainG;
+    const bool srcCell = src.srcCell;
     const float dtNew = C.dtNew;
     float hN, huN, hvN;
     bool wetCell = false;
     if (STAGE == 1) {
         // Integrate_1_k (grid.cu:856-922)
-        const float G = manningG(pre[0], hu0, hv0, hC, C.kappa);
+        const float G = src.G;
         if (fl & F_SURGE) {
             float sg = mapValue(P, 2, c, C.fac2);
             if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
@@ -923,6 +1007,17 @@ __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C
     if (edge) writeGhosts(P, C.Uout, j, i, hN, huN, hvN);
     return wetCell;
 }
+
+template <int STAGE, bool PREF = false, bool BED = true>
+__device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
+                                           int i, float dh, float dhu, float dhv, float hC,
+                                           float hu0, float hv0, float eW, float eE, float eS,
+                                           float eN, const float* pre, bool edge = true) {
+    const CellSrc src = cellSources<STAGE, PREF, BED>(P, C, tile, j, i, dh, dhu, dhv, hC, hu0, hv0,
+                                                      eW, eE, eS, eN, pre);
+    return cellFinish<STAGE, PREF>(P, C, j, i, src, hC, hu0, hv0, pre, edge);
+}
+
 
 // Flux divergence of every interior cell of a staged tile (the ComputeFluxes_k
 // sweeps, grid.cu:659-746): x reconstruction of cells i0-1 .. i0+16 on the
@@ -1052,6 +1147,37 @@ __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConst
                                    T.e[3][r][c], pre, edge);
 }
 
+// tileCellUpdate in its two halves (see cellSources / cellFinish).
+template <int STAGE>
+__device__ __forceinline__ CellSrc tileCellSources(const Params& P, const StageConsts& C,
+                                                   const TileBuf& T, int tile, int i0, int j0,
+                                                   float dh, float dhu, float dhv,
+                                                   const float (&pre)[6]) {
+    const int tid = threadIdx.x;
+    const int tx = tid % TW, ty = tid / TW;
+    const int i = i0 + tx, j = j0 + ty;
+    CellSrc r{};
+    if (tid >= TH * TW || i > P.nx - 3 || j > P.ny - 3) return r;
+    const int rr = ty + 2, cc = tx + 2;
+    return cellSources<STAGE, true>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][rr][cc],
+                                    T.in[1][rr][cc], T.in[2][rr][cc], T.e[0][rr][cc],
+                                    T.e[1][rr][cc], T.e[2][rr][cc], T.e[3][rr][cc], pre);
+}
+
+template <int STAGE>
+__device__ __forceinline__ bool tileCellFinish(const Params& P, const StageConsts& C,
+                                               const TileBuf& T, int i0, int j0,
+                                               const CellSrc& src, const float (&pre)[6]) {
+    const int tid = threadIdx.x;
+    const int tx = tid % TW, ty = tid / TW;
+    const int i = i0 + tx, j = j0 + ty;
+    if (tid >= TH * TW || i > P.nx - 3 || j > P.ny - 3) return false;
+    const int rr = ty + 2, cc = tx + 2;
+    const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
+    return cellFinish<STAGE, true>(P, C, j, i, src, T.in[0][rr][cc], T.in[1][rr][cc],
+                                   T.in[2][rr][cc], pre, edge);
+}
+
 // Tile flags (stage 2, or stage 1 in Euler mode) and stage-2 tile speeds.
 template <int STAGE>
 __device__ __forceinline__ bool tileFlags(const Params& P, const StageConsts& C, StageSmem& S,
@@ -1084,7 +1210,7 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
                            const StageConsts* given = nullptr) {
     const int tid = threadIdx.x;
     tileFirst(S, tmIn, tmE, P, nAct);
-    const StageConsts C = given ? *given : stageConsts<STAGE>(P);
+    const StageConsts C = given ? *given : blockConsts<STAGE>(P);
     int bsel = 0;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];

@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
     if (P.st->stop || !useMarch(P)) return;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nItems = P.st->nStrips;
-    const StageConsts C = stageConsts<STAGE>(P);
+    const StageConsts C = blockConsts<STAGE>(P);
     float tmxAll = 0.f, tmyAll = 0.f;
     if (tid == 0) {
         prefetch_tmap(&tmIn);
@@ -311,15 +311,15 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
 // dt is known: sources, friction, the RK stage, outputs and ghost cells, from
 // U^n and the stored divergence; in Euler mode also the tile wet flags.  No
 // halo, so the work item is half a strip (one tile row of 7 tiles): finer
-// items balance the grid.  One thread per column, rows in groups of four
-// whose loads are in flight together.
-__global__ void __launch_bounds__(MT) k_update1(Params P) {
+// items balance the grid.  One thread per column, rows in pairs whose loads
+// are in flight together (64 registers: 8 CTAs per SM).
+__global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
     __shared__ int tact[STRIP_TX];
     __shared__ int twet[STRIP_TX];
     if (P.st->stop || !useMarch(P)) return;
     const int tid = threadIdx.x;
     const int nItems = 2 * P.st->nStrips;
-    const StageConsts C = stageConsts<1>(P);
+    const StageConsts C = blockConsts<1>(P);
     const size_t pl = (size_t)P.planeSize;
     for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
         const int strip = P.strips[item >> 1];
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(MT) k_update1(Params P) {
         const int i = X0 + tid, slot = tid / TW;
         if (tid < MCOLS && i <= P.nx - 3 && tact[slot]) {
             const int tile = by * P.nBX + STRIP_TX * sx + slot;
-            constexpr int G = 4;
+            constexpr int G = 2;
             bool wetAny = false;
             for (int r0 = 0; r0 < TH; r0 += G) {
                 float v[G][7];

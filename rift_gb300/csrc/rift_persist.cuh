@@ -42,6 +42,7 @@ struct GridBar {
     int ownedCnt[2];       // owned tiles found active
     int schedCnt[2];       // scheduled tiles found by the scan
     int freeTop;           // entries of freeStack
+    float nextRates[6];    // the next step's source rates and series state (spare CTA)
     int slotTile[PERSIST_MAX_CTAS];   // CTA -> its tile, or -1
     int freeStack[PERSIST_MAX_CTAS];  // CTAs without a tile
 };
@@ -109,6 +110,39 @@ __device__ bool gridSync(GridBar* gb, unsigned& target, DevState* st, bool raise
     ok = __syncthreads_and(ok);
     if (events) *events = sEvents;
     return ok != 0;
+}
+
+// The same barrier in two halves, so a CTA can work on its own data between
+// its arrival and the wait: gridArrive after the CTA's writes that others
+// read, gridWait before it reads theirs.  Between the halves the CTA writes
+// nothing that another CTA reads.
+__device__ __forceinline__ void gridArrive(GridBar* gb, unsigned& target) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        target += gridDim.x;
+        red_add_release_gpu(&gb->count[0], 1u);
+    }
+}
+
+__device__ bool gridWait(GridBar* gb, unsigned& target, DevState* st) {
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        ok = 0;
+        unsigned v = 0u;
+        for (int it = 0; it < (1 << 22); ++it) {
+            v = ld_acquire_gpu(&gb->count[0]);
+            if ((int)(v - target) >= 0) {
+                ok = 1;
+                break;
+            }
+            __nanosleep(20);
+        }
+        fence_proxy_async_global();
+        if (!ok) atomicOr(&st->error, ERR_BARRIER_TIMEOUT);
+        const unsigned k = ok ? (v - target) / BAR_EVENT : 0u;  // no events here; keep the count
+        target += k * BAR_EVENT;
+    }
+    return __syncthreads_and(ok) != 0;
 }
 
 // ------------------------------------------------------------ tile table
@@ -281,6 +315,9 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
     __shared__ int sFail;
     __shared__ int sSched;
     __shared__ int sOverflow;  // a claim of this CTA found no free CTA
+    __shared__ StepRates sRates;  // this step's source rates (every CTA computes them)
+    __shared__ StageConsts sPre;  // stage-1 constants without the step's dt
+    __shared__ CellSrc sSrc[NT];  // stage-1 sources of each thread's cell
     DevState* st = P.st;
     GridBar* const T = P.gbar;
     const int tid = threadIdx.x;
@@ -304,6 +341,8 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
     // t as every CTA computes it (st->t gets the same FP64 sum); t_stop is
     // fixed for the launch
     double tNow = st->t;
+    double dtPrev = st->dt;  // the previous step's dt (stage-1 source clamps)
+    bool haveNext = false;   // nextRates holds this step's rates (after a fused step)
     const double tStop = st->t_stop;
     int stepsDone = st->steps_done, tableSteps = st->tableSteps;  // used by CTA 0
     if (blockIdx.x == 0 && tid == 0) st->persistExit = 0;
@@ -371,13 +410,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             bool mine = tile >= 0;
             int bX, bY, i0 = 0, j0 = 0;
             float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f;
-            // t and dt of the previous step: published before the last barrier
-            double tCur = 0.0, dtOld = 0.0;
-            if (tid == 0) {
-                tCur = st->t;
-                dtOld = st->dt;
-                if (mine) issueTile(S.buf[0], &S.bar[0], &tmA, &tmE, P, tile);
-            }
+            if (tid == 0 && mine) issueTile(S.buf[0], &S.bar[0], &tmA, &tmE, P, tile);
             bool wetOld = false, live = true;
             if (mine) {
                 tileOrigin(P, tile, bX, bY, i0, j0);
@@ -417,9 +450,41 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 }
                 myTile = mine ? tile : -1;
             }
-            if (spare && tid < 32) beginStepRates(P, st);
+            // this step's source rates: computed by the spare CTA during the
+            // last step's stage 2, or here in every CTA on the first fused
+            // step of the launch (warp 1); the spare writes them to the device
+            // state during stage 2, when no CTA reads the series state any more
+            if (haveNext) {
+                if (tid == 32) {
+                    const float* r = T->nextRates;
+                    StepRates q;
+                    q.rainU = r[0];
+                    q.drainU = r[1];
+                    q.srcR = r[2];
+                    q.interp[0] = r[3];
+                    q.interp[1] = r[4];
+                    q.interp[2] = r[5];
+                    sRates = q;
+                }
+            } else if (tid >= 32 && tid < 64) {
+                const StepRates q = stepRates(P, st, tNow);
+                if (tid == 32) sRates = q;
+            }
             if (!table) resyncDeactivated(P, nDe);
-            RIFT_SYNC();
+            // split barrier: the stage-1 sources (no dt needed) are computed
+            // between this CTA's arrival and its wait
+            gridArrive(P.gbar, barTarget);
+            if (tid == 0) {
+                StageConsts c = stageConstsAt<1>(P, dtPrev, dtPrev, tNow);
+                c.rainU = sRates.rainU;
+                c.drainU = sRates.drainU;
+                c.srcR = sRates.srcR;
+                sPre = c;
+            }
+            __syncthreads();
+            // (kept in shared memory across the wait: registers stay free)
+            if (mine) sSrc[tid] = tileCellSources<1>(P, sPre, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
+            if (!gridWait(P.gbar, barTarget, st)) return;
             // dt of this step (Simulator::ComputeTimestep), by thread 0 of
             // every CTA; the FP64 arithmetic stays in one thread
             if (tid == 0) {
@@ -427,23 +492,20 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 const unsigned my0 = ld_relaxed_gpu(&T->maxb[par][1]);
                 const unsigned mx1 = ld_relaxed_gpu(&T->staleb[par][0]);
                 const unsigned my1 = ld_relaxed_gpu(&T->staleb[par][1]);
-                // the step's rates (the spare CTA wrote them before the barrier),
-                // loaded with the maxima in one round trip
-                const float rainU = __uint_as_float(ld_relaxed_gpu((const unsigned*)&st->rain_rate));
-                const float drainU = __uint_as_float(ld_relaxed_gpu((const unsigned*)&st->drain_rate));
                 int fail = 0, sched = nAct;
                 if (table) {
                     const int owned = (int)ld_relaxed_gpu((const unsigned*)&T->ownedCnt[par]);
                     sched = (int)ld_relaxed_gpu((const unsigned*)&T->schedCnt[par]);
                     fail = owned != sched;
                 }
-                const double dtNew = stepDtAt(P, tCur, (double)__uint_as_float(max(mx0, mx1)),
+                const double dtNew = stepDtAt(P, tNow, (double)__uint_as_float(max(mx0, mx1)),
                                               (double)__uint_as_float(max(my0, my1)));
-                const double tNew = tCur + dtNew;
-                StageConsts c1 = stageConstsAt<1>(P, dtNew, dtOld, tNew);
-                StageConsts c2 = stageConstsAt<2>(P, dtNew, dtOld, tNew);
-                c1.rainU = c2.rainU = rainU;
-                c1.drainU = c2.drainU = drainU;
+                const double tNew = tNow + dtNew;
+                StageConsts c1 = stageConstsAt<1>(P, dtNew, dtPrev, tNew);
+                StageConsts c2 = stageConstsAt<2>(P, dtNew, dtPrev, tNew);
+                c1.rainU = c2.rainU = sRates.rainU;
+                c1.drainU = c2.drainU = sRates.drainU;
+                c1.srcR = c2.srcR = sRates.srcR;
                 sC[0] = c1;
                 sC[1] = c2;
                 sDt = dtNew;
@@ -454,11 +516,11 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             __syncthreads();
             if (sFail) return;  // every CTA read the same counts
             tNow = sC[1].tNew;
+            dtPrev = sDt;
             nActPrev = sSched;
-            if (mine) {  // stage-1 update with this step's dt (Integrate_1_k)
+            if (mine) {  // the rest of the stage-1 update with this step's dt (Integrate_1_k)
                 const StageConsts C1 = sC[0];
-                const bool wetCell =
-                    tileCellUpdate<1>(P, C1, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
+                const bool wetCell = tileCellFinish<1>(P, C1, S.buf[0], i0, j0, sSrc[tid], pre);
                 tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
                 __syncthreads();
             }
@@ -498,6 +560,20 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 RIFT_SYNC();
                 commitTiles(P, nAct);
             }
+            if (spare && tid < 32) {
+                writeRates(P, st, sRates);
+                // the next step's rates from this step's state, at its t
+                const StepRates q = stepRatesFrom(P, sRates, tNow);
+                if (tid == 0) {
+                    float* r = T->nextRates;
+                    r[0] = q.rainU;
+                    r[1] = q.drainU;
+                    r[2] = q.srcR;
+                    r[3] = q.interp[0];
+                    r[4] = q.interp[1];
+                    r[5] = q.interp[2];
+                }
+            }
             if (spare && tid == 0) {
                 publishDt(P, st, sDt);
                 // the other parity: last read in the previous step
@@ -518,9 +594,11 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             if (!gridSync(P.gbar, barTarget, st, sOverflow != 0, &voided)) return;
             if (tid == 0) sOverflow = 0;
             table = (table || built) && voided == 0;
+            haveNext = true;
             continue;
         }
         nActPrev = nAct;
+        haveNext = false;
         // speeds of U^n, dt, t, U* re-sync (k_speed_dt), then stage 1; the
         // stale maxima of this step went to staleb[par]
         if (blockIdx.x == 0 && tid < 32) beginStepRates(P, st);
@@ -537,9 +615,11 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
         if (tid == 0) {  // the stage constants, FP64 conversions in one thread
             sC[0] = stageConsts<1>(P);
             sC[1] = stageConsts<2>(P);
+            sDt = st->dt;
         }
         __syncthreads();
         tNow = sC[1].tNew;  // published by finishDt before the barrier
+        dtPrev = sDt;
         if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph, &sC[0])) return;
         RIFT_SYNC();
         if (!euler) {
