@@ -203,7 +203,7 @@ static_assert(sizeof(TileBuf) % 128 == 0, "TMA destination alignment");
 
 struct __align__(128) StageSmem {
     TileBuf buf[2];
-    union {
+    struct {  // x and y reconstructions side by side: built in one phase
         struct {
             float P[3][TH][TW + 2];
             float M[3][TH][TW + 2];
@@ -1029,6 +1029,10 @@ template <bool SPEEDS>
 __device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, const Params& P, int i0,
                                             int j0, float& dh, float& dhu, float& dhv, float& spx,
                                             float& spy) {
+    // Two phases of the whole CTA: every thread builds one x and one y
+    // reconstruction, then one x and one y face flux (the two directions are
+    // independent until the divergence, so each thread has two chains in
+    // flight and the tile needs two barriers, not four).
     const int tid = threadIdx.x;
     const float kappa = P.kappa;
     if (tid < TH * (TW + 2)) {
@@ -1045,30 +1049,6 @@ __device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, cons
         S.rec.x.M[1][r][c] = R.uM;
         S.rec.x.M[2][r][c] = R.vM;
     }
-    __syncthreads();
-    spx = 0.f;
-    spy = 0.f;
-    // face f lies between reconstructed cells f and f+1: the east face of
-    // tile column f-1
-    if (tid < TH * (TW + 1)) {
-        int r = tid / (TW + 1), f = tid % (TW + 1);
-        float fx[3];
-        float sp = faceFlux<0>(S.rec.x.P[0][r][f], S.rec.x.P[1][r][f], S.rec.x.P[2][r][f],
-                               S.rec.x.M[0][r][f + 1], S.rec.x.M[1][r][f + 1],
-                               S.rec.x.M[2][r][f + 1], kappa, fx);
-        S.FX[0][r][f] = fx[0];
-        S.FX[1][r][f] = fx[1];
-        S.FX[2][r][f] = fx[2];
-        if (SPEEDS && f >= 1 && i0 + f - 1 <= P.nx - 3 && j0 + r <= P.ny - 3) spx = sp;
-    }
-    __syncthreads();
-    const int tx = tid % TW, ty = tid / TW;
-    dh = dhu = dhv = 0.f;
-    if (tid < TH * TW) {
-        dh = -(S.FX[0][ty][tx + 1] - S.FX[0][ty][tx]) * P.inv_dx;
-        dhu = -(S.FX[1][ty][tx + 1] - S.FX[1][ty][tx]) * P.inv_dx;
-        dhv = -(S.FX[2][ty][tx + 1] - S.FX[2][ty][tx]) * P.inv_dx;
-    }
     if (tid < (TH + 2) * TW) {
         int r = tid / TW, c = tid % TW;
         int sr = r + 1, sc = c + 2;
@@ -1084,6 +1064,22 @@ __device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, cons
         S.rec.y.M[2][r][c] = R.vM;
     }
     __syncthreads();
+    spx = 0.f;
+    spy = 0.f;
+    // x face f lies between reconstructed cells f and f+1: the east face of
+    // tile column f-1
+    if (tid < TH * (TW + 1)) {
+        int r = tid / (TW + 1), f = tid % (TW + 1);
+        float fx[3];
+        float sp = faceFlux<0>(S.rec.x.P[0][r][f], S.rec.x.P[1][r][f], S.rec.x.P[2][r][f],
+                               S.rec.x.M[0][r][f + 1], S.rec.x.M[1][r][f + 1],
+                               S.rec.x.M[2][r][f + 1], kappa, fx);
+        S.FX[0][r][f] = fx[0];
+        S.FX[1][r][f] = fx[1];
+        S.FX[2][r][f] = fx[2];
+        if (SPEEDS && f >= 1 && i0 + f - 1 <= P.nx - 3 && j0 + r <= P.ny - 3) spx = sp;
+    }
+    // y face r is the north face of tile row r-1
     if (tid < (TH + 1) * TW) {
         int r = tid / TW, c = tid % TW;
         float fy[3];
@@ -1093,11 +1089,15 @@ __device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, cons
         S.FY[0][r][c] = fy[0];
         S.FY[1][r][c] = fy[1];
         S.FY[2][r][c] = fy[2];
-        // face r is the north face of tile row r-1
         if (SPEEDS && r >= 1 && i0 + c <= P.nx - 3 && j0 + r - 1 <= P.ny - 3) spy = sp;
     }
     __syncthreads();
+    const int tx = tid % TW, ty = tid / TW;
+    dh = dhu = dhv = 0.f;
     if (tid < TH * TW) {
+        dh = -(S.FX[0][ty][tx + 1] - S.FX[0][ty][tx]) * P.inv_dx;
+        dhu = -(S.FX[1][ty][tx + 1] - S.FX[1][ty][tx]) * P.inv_dx;
+        dhv = -(S.FX[2][ty][tx + 1] - S.FX[2][ty][tx]) * P.inv_dx;
         dh += -(S.FY[0][ty + 1][tx] - S.FY[0][ty][tx]) * P.inv_dy;
         dhu += -(S.FY[1][ty + 1][tx] - S.FY[1][ty][tx]) * P.inv_dy;
         dhv += -(S.FY[2][ty + 1][tx] - S.FY[2][ty][tx]) * P.inv_dy;

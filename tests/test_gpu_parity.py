@@ -63,6 +63,37 @@ def _run_against_golden(engine_api, name, schedule="auto"):
     return eng
 
 
+def test_persistent_runs_match_reference_kernels(engine_api, name_run):
+    """Multi-step persistent launches (rift_run between the dumped steps: the
+    loop's tile table and split barriers run) against the reference kernels."""
+    name = name_run
+    fx, case = FX.load(name)
+    eng = FX.start(_scheduled(capi.Sim(case, api=engine_api), "persist"), fx)
+    step = 0
+    for s in FX.dumps(fx):
+        if s > step:
+            eng.run(s - step)
+            step = s
+        ref = FX.ref_state(fx, s)
+        wet, act = eng.tiles()
+        t = eng.time()[0]
+        assert np.array_equal(wet, ref["wet"]), f"{name}: wet tiles differ at step {s}"
+        assert np.array_equal(act, ref["active"]), f"{name}: active tiles differ at step {s}"
+        assert abs(t - ref["t"]) <= 1e-5 * max(1.0, abs(ref["t"])), f"{name}: t {t} vs {ref['t']}"
+        _close(eng.field("W"), ref["w"], f"{name} w step {s}")
+        if "F" in ref:
+            _close(eng.field("F"), ref["F"], f"{name} F step {s}")
+        if "hmax" in ref:
+            _close(eng.field("HMAX"), ref["hmax"], f"{name} hmax step {s}")
+    persist_steps, graph_steps = eng.path_stats()
+    assert graph_steps == 0 and persist_steps == step
+
+
+@pytest.fixture(params=FX.CASES)
+def name_run(request):
+    return request.param
+
+
 @pytest.mark.parametrize("schedule", ["tiles", "march", "persist"])
 @pytest.mark.parametrize("name", FX.CASES)
 def test_engine_matches_reference_kernels(engine_api, name, schedule):
