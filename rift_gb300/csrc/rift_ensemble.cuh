@@ -34,6 +34,7 @@ struct EnsDev {
     GridBar bar;
     int live[2][ENS_MAX];  // liveness per step parity
     int nAlive[2];
+    StageConsts consts[ENS_MAX][2];  // each member's stage constants of the step (phase D)
 };
 
 struct EnsArgs {
@@ -276,8 +277,11 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
         ensPrefix(n, [&](int m) { return live[m] ? E.Ps[m].nSX * E.Ps[m].nSY : 0; }, Q.offs);
         ensGrow(E, Q.offs);
         ENS_SYNC();
-        // ---- S: tile speeds of the scheduled tiles, U* re-sync of the
-        // deactivated ones (the counts are final after the barrier)
+        // ---- S: the stage-1 fluxes of the scheduled tiles give the tile
+        // speeds, and each cell's divergence (bed-slope source folded in)
+        // waits in the member's divergence planes for the update after dt;
+        // U* re-sync of the deactivated tiles (the counts are final after the
+        // barrier)
         ensPrefix(n, [&](int m) { return live[m] ? E.Ps[m].st->appendCnt[0] : 0; }, Q.offs);
         ensPrefix(n, [&](int m) { return live[m] ? E.Ps[m].st->appendCnt[1] : 0; }, Q.offs2);
         if (!ensTileLoop(S, E, Q.offs, 0, ph, [](int, int) {},
@@ -285,8 +289,22 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
                              const Params& P = E.Ps[m];
                              int bX, bY, i0, j0;
                              tileOrigin(P, tile, bX, bY, i0, j0);
-                             float mxv, myv;
-                             tileSpeeds(S, T, P, i0, j0, mxv, myv);
+                             float dh, dhu, dhv, spx, spy;
+                             tileFluxDiv<true>(S, T, P, i0, j0, dh, dhu, dhv, spx, spy);
+                             const int tx = tid % TW, ty = tid / TW;
+                             if (tid < TH * TW && i0 + tx <= P.nx - 3 && j0 + ty <= P.ny - 3) {
+                                 const int rr = ty + 2, cc = tx + 2;
+                                 const float hC = T.in[0][rr][cc];
+                                 const size_t c = cidx(P, 0, j0 + ty, i0 + tx);
+                                 const size_t pl = (size_t)P.planeSize;
+                                 P.D[c] = dh;
+                                 P.D[c + pl] =
+                                     dhu + bedSourceX(P, hC, T.e[0][rr][cc], T.e[1][rr][cc]);
+                                 P.D[c + 2 * pl] =
+                                     dhv + bedSourceY(P, hC, T.e[2][rr][cc], T.e[3][rr][cc]);
+                             }
+                             const float mxv = blockMax(spx, S.red[0]);
+                             const float myv = blockMax(spy, S.red[1]);
                              if (tid == 0) {
                                  P.mx[tile] = mxv;
                                  P.my[tile] = myv;
@@ -311,6 +329,10 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
                 const float my = fmaxf(__uint_as_float(st->max_bits[1]),
                                        __uint_as_float(st->staleBits[1]));
                 computeDt(P, st, (double)mx, (double)my);
+                // the step's stage constants, once per member (the FP64
+                // conversions stay out of the tile loops)
+                D->consts[m][0] = stageConsts<1>(P);
+                D->consts[m][1] = stageConsts<2>(P);
                 st->staleBits[0] = st->staleBits[1] = 0u;
                 st->nActive = st->appendCnt[0];
                 st->nDeact = st->appendCnt[1];
@@ -326,29 +348,36 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
             if (next) atomicAdd(&D->nAlive[cur ^ 1], 1);
         }
         ENS_SYNC();
-        // ---- 1: RK stage 1 of every scheduled tile
+        // ---- 1: the rest of RK stage 1 of every scheduled tile, one thread
+        // per cell, from U^n and the stored divergence (no staged block)
         ensPrefix(n, [&](int m) { return live[m] ? E.Ps[m].st->nActive : 0; }, Q.offs);
-        float pre[6];
-        if (!ensTileLoop(S, E, Q.offs, 0, ph,
-                         [&](int m, int tile) {
-                             const Params& P = E.Ps[m];
-                             int bX, bY, i0, j0;
-                             tileOrigin(P, tile, bX, bY, i0, j0);
-                             tilePrefetch<1>(P, stageConsts<1>(P), i0, j0, pre);
-                         },
-                         [&](int m, int tile, const TileBuf& T) {
-                             const Params& P = E.Ps[m];
-                             const StageConsts C = stageConsts<1>(P);
-                             int bX, bY, i0, j0;
-                             tileOrigin(P, tile, bX, bY, i0, j0);
-                             float dh, dhu, dhv, spx, spy;
-                             tileFluxDiv<false>(S, T, P, i0, j0, dh, dhu, dhv, spx, spy);
-                             const bool wet =
-                                 tileCellUpdate<1>(P, C, T, tile, i0, j0, dh, dhu, dhv, pre);
-                             tileFlags<1>(P, C, S, tile, wet, spx, spy);
-                         }))
-            return;
+        for (int g = blockIdx.x; g < Q.offs[n]; g += gridDim.x) {
+            const int m = ensMember(Q.offs, n, g);
+            const Params& P = E.Ps[m];
+            const StageConsts& C = D->consts[m][0];
+            const int tile = P.act[g - Q.offs[m]];
+            int bX, bY, i0, j0;
+            tileOrigin(P, tile, bX, bY, i0, j0);
+            const int tx = tid % TW, ty = tid / TW, i = i0 + tx, j = j0 + ty;
+            const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
+            bool wet = false;
+            if (tid < TH * TW && i <= P.nx - 3 && j <= P.ny - 3) {
+                const size_t c = cidx(P, 0, j, i);
+                const size_t pl = (size_t)P.planeSize;
+                const float d0 = P.D[c], d1 = P.D[c + pl], d2 = P.D[c + 2 * pl];
+                const float h = P.A[c], hu = P.A[c + pl], hv = P.A[c + 2 * pl];
+                const float pre1[1] = {P.nman[c]};
+                prefetchMaps(P, C.fl, c);
+                wet = cellUpdate<1, false, false>(P, C, tile, j, i, d0, d1, d2, h, hu, hv, 0.f,
+                                                  0.f, 0.f, 0.f, pre1, edge);
+            }
+            if (C.euler) {  // Euler mode: the tile wet flags come from this stage
+                const bool any = __syncthreads_or(wet);
+                if (tid == 0) P.wet[tile] = (uint8_t)((!(C.fl & F_TILE_ACC)) || any);
+            }
+        }
         ENS_SYNC();
+        float pre[6];
         // ---- 2: RK stage 2 of the RK members, the commit of the Euler ones
         ensPrefix(n, [&](int m) { return live[m] && !(E.Ps[m].flags & F_EULER) ? E.Ps[m].st->nActive : 0; },
                   Q.offs);
@@ -359,11 +388,11 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
                              const Params& P = E.Ps[m];
                              int bX, bY, i0, j0;
                              tileOrigin(P, tile, bX, bY, i0, j0);
-                             tilePrefetch<2>(P, stageConsts<2>(P), i0, j0, pre);
+                             tilePrefetch<2>(P, D->consts[m][1], i0, j0, pre);
                          },
                          [&](int m, int tile, const TileBuf& T) {
                              const Params& P = E.Ps[m];
-                             const StageConsts C = stageConsts<2>(P);
+                             const StageConsts& C = D->consts[m][1];
                              int bX, bY, i0, j0;
                              tileOrigin(P, tile, bX, bY, i0, j0);
                              float dh, dhu, dhv, spx, spy;
