@@ -4,7 +4,8 @@
 - rift_ref_sm103a.fatbin : the reference's own grid.cu compiled for sm_103a
   with the reference's --use_fast_math, from the sources where they lie in
   the reference tree.  Built only where that tree is present; the output goes
-  to oracle/_ref/ (git-ignored) and travels to the GPU machine with the repo.
+  to oracle/_ref/ (git-ignored) and goes with the repository to the machine
+  that has the GPU.
 - refrun : the driver-API host runner for that fatbin (oracle/refkit/refrun.cu),
   built on whichever machine runs it.
 """

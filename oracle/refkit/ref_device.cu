@@ -1,6 +1,6 @@
 // ref_device.cu -- TEST INFRASTRUCTURE: the reference's own device code,
 // compiled from its unmodified grid.cu into a device-only fatbin so that the
-// reference kernels can run on the GPU box, where neither its sources nor an
+// reference kernels can run on the GPU machine, where neither its sources nor an
 // aarch64 build of its host program exist.
 //
 // The translation unit includes grid.cu as it lies in the reference tree

@@ -2,7 +2,7 @@
 // own kernels (from oracle/_ref/rift_ref_sm103a.fatbin, the reference's
 // unmodified grid.cu compiled for sm_103a) through the CUDA driver API.
 //
-// The reference's host program cannot be built for the aarch64 GPU box from
+// The reference's host program cannot be built for the aarch64 GPU machine from
 // here, so this file restates its host orchestration: the allocations of
 // AllocateGrid (grid.cu:347-490), InitGrid + ApplyBoundaries
 // (simulator.cu:433-462,731), and per step the order of

@@ -835,7 +835,7 @@ int persistGrid(const rift_handle* h) {
 }
 
 int launchPersist(rift_handle* h, int nsteps) {
-    CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream));
+    CUDA_TRY(h, cudaMemsetAsync(h->gbar, 0, GRIDBAR_CLEAR, h->stream));
     Params P = makeParams(h);
     const int grid = persistGrid(h);
     void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
@@ -913,7 +913,7 @@ bool stepGraph(rift_handle* h, int& rc) {
             return false;
         }
         cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, h->stream);
-        cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), h->stream);
+        cudaMemsetAsync(h->gbar, 0, GRIDBAR_CLEAR, h->stream);
         cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0, h->stream);
         cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream);
         cudaError_t e = cudaStreamEndCapture(h->stream, &g);

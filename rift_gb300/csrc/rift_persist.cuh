@@ -43,6 +43,8 @@ struct GridBar {
     int schedCnt[2];       // scheduled tiles found by the scan
     int freeTop;           // entries of freeStack
     float nextRates[6];    // the next step's source rates and series state (spare CTA)
+    // (the tables below are written before they are read in every launch:
+    // only the part above is cleared, GRIDBAR_CLEAR bytes)
     int slotTile[PERSIST_MAX_CTAS];   // CTA -> its tile, or -1
     int freeStack[PERSIST_MAX_CTAS];  // CTAs without a tile
 };
@@ -80,6 +82,7 @@ __device__ __forceinline__ void fence_proxy_async_global() {
 // than BAR_EVENT in all (they raise nothing: the caller raises events at
 // one barrier only, never at the one after it).  The event count then moves
 // into `target`, so later barriers see none.
+constexpr size_t GRIDBAR_CLEAR = offsetof(GridBar, slotTile);  // bytes cleared before a launch
 constexpr unsigned BAR_EVENT = 1u << 16;  // > any grid (PERSIST_MAX_CTAS)
 static_assert(BAR_EVENT > (unsigned)PERSIST_MAX_CTAS, "event unit above the arrivals");
 

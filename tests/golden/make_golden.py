@@ -1,12 +1,12 @@
 """Generate the golden fixtures by running the REFERENCE's own kernels.
 
-Runs on the GPU machine (after __graft_entry__.build()), through
+Runs on a GB300 machine (after __graft_entry__.build()), through
 oracle/_bin/refrun and the reference device fatbin oracle/_ref/
 rift_ref_sm103a.fatbin.  Writes one .npz per case into --out; the committed
 copies live in tests/golden/.  Every input array is stored in the fixture so
 the tests never depend on regenerating the same random numbers.
 
-    python tests/golden/make_golden.py --out gpurun_out/golden
+    python tests/golden/make_golden.py --out <output directory>
 """
 from __future__ import annotations
 

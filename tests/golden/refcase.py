@@ -1,5 +1,5 @@
 """Write a workload in the format oracle/refkit/refrun.cu reads, and read back
-its dumps.  Test infrastructure: used by make_golden.py (run on the GPU machine)
+its dumps.  Test infrastructure: used by make_golden.py (run on a GB300 machine)
 and by the parity tests."""
 from __future__ import annotations
 
