@@ -457,7 +457,7 @@ def run_ensemble(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3, 5))
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")
