@@ -3,25 +3,33 @@
 // For a small or mostly dry grid the step is a chain of short phases, and
 // separate kernel launches spend more time starting and draining than
 // working.  k_persist runs many steps in one cooperative launch (all CTAs
-// resident), the phases separated by a grid barrier:
+// resident), the phases separated by grid barriers:
 //   [track]  re-wet inactive tiles under gridded rain / surge
-//   grow     each CTA appends the list entries of its chunk of strips; the
-//            last one publishes the counts (rift_grow.cuh)
+//   grow     each CTA appends the list entries of its chunk of strips; every
+//            CTA reads the counts after the barrier (rift_grow.cuh)
 //   speed    tile speeds of U^n, dt and t (last CTA), U* re-sync
 //   stage 1  RK stage 1 (per-tile code of k_stage<1>)
-// With at most one active tile per CTA, the speed and stage-1 phases become
-// one flux phase (its fluxes give the speeds) and an update after the dt
-// barrier, so a step has one tile-flux phase fewer.
 //   stage 2  RK stage 2, or the Euler commit
-// The phases run the same device functions as the per-tile kernels, so the
-// results are identical.  The kernel leaves at a step boundary when
-// t >= t_stop, after the requested number of steps, or when the active set
-// has outgrown P.persistMax (the host then continues with the per-step
-// launches, whose march kernels suit a dense grid).
+// With at most one scheduled tile per CTA (the usual case for a sparse
+// grid) a step is shorter:
+//   flux     the stage-1 fluxes of the CTA's tile give its speeds; the
+//            divergence waits in registers, the stage-1 sources are computed
+//            between the CTA's arrival at the dt barrier and its wait
+//   update   dt in every CTA, the rest of the stage-1 update
+//   stage 2  after a wait on the 4 edge neighbours' stage-1 flags, not a
+//            grid barrier
+// and, without tracking in RK2 mode, the tile table keeps each tile on its
+// CTA from step to step so the grow phase and its barrier go away (see
+// below).  The phases run the same device functions as the per-tile
+// kernels, so the results are identical.  The kernel leaves at a step
+// boundary when t >= t_stop, after the requested number of steps, or when
+// the active set has outgrown P.persistMax (the host then continues with
+// the per-step launches, whose march kernels suit a dense grid).
 //
-// Every wait is bounded: a grid barrier gives up after 2^22 polls, records
-// ERR_BARRIER_TIMEOUT and the kernel returns; no TMA copy is in flight at a
-// barrier (each tile loop consumes every load it issues).
+// Every wait is bounded: a grid barrier or a neighbour wait gives up after
+// 2^22 polls, records ERR_BARRIER_TIMEOUT and the kernel returns; no TMA
+// copy is in flight at a barrier (each tile loop consumes every load it
+// issues).
 #pragma once
 #include "rift_grow.cuh"
 #include "rift_kernels.cuh"
