@@ -60,6 +60,7 @@ struct rift_handle {
     int nx = 0, ny = 0, nBX = 0, nBY = 0, gridSize = 0, pitch = 0, rows = 0;
     int numSMs = 0, gridStage = 0, gridSpeed = 0, gridTrack = 0, gridDt = 0, gridMarch = 0;
     int gridUpdate = 0;  // k_update1: resident CTAs over half-strip items
+    int gridMarch1 = 0;  // k_march<1>: its own occupancy (fewer registers than k_march<2>)
     int nSX = 0, nSY = 0;
     int marchMin = 0;  // active strips from which the march kernels run
     int gridGrow = 0;      // CTAs of the grow kernel of the graph path
@@ -236,7 +237,7 @@ void enqueueStep(rift_handle* h) {
     // per-tile and march variants of each pass; the device keeps one of them
     // (useMarch) and the other returns at once
     k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
-    k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);  // fluxes, speeds, dt
+    k_march<1><<<h->gridMarch1, MT, 0, s>>>(h->tmAm, h->tmEm, P);  // fluxes, speeds, dt
     k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
     k_update1<<<h->gridUpdate, MT, 0, s>>>(P);
     if (!h->has(RIFT_F_EULER)) {
@@ -534,6 +535,9 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_march<2>, MT, 0);
     if (occ < 1) occ = 1;
     h->gridMarch = std::max(1, std::min(NS, h->numSMs * occ));
+    int occ1 = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_march<1>, MT, 0);
+    h->gridMarch1 = std::max(1, std::min(NS, h->numSMs * std::max(occ1, 1)));
     int occU = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1, MT, 0);
     h->gridUpdate = std::max(1, std::min(2 * NS, h->numSMs * std::max(occU, 1)));
@@ -1239,7 +1243,7 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
         k_grow<<<h->gridGrow, NT, 0, s>>>(P);
         k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
         CUDA_TRY(h, cudaEventRecord(e0, s));
-        k_march<1><<<h->gridMarch, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+        k_march<1><<<h->gridMarch1, MT, 0, s>>>(h->tmAm, h->tmEm, P);
         k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
         k_update1<<<h->gridUpdate, MT, 0, s>>>(P);
         if (!h->has(RIFT_F_EULER)) {
