@@ -258,7 +258,7 @@ def run_ours(args, device=0, sync=None):
         achieved = active_cells * bytes_per / (ms * 1e-3) / 1e9
         launches = 1
     else:
-        kernel = ("RK stages 1+2 (k_march<1>, k_march<2> or k_stage<1>, k_stage<2>; one "
+        kernel = ("RK stages 1+2 (k_march<1>, k_update1, k_march<2> or k_stage<1>, k_stage<2>; one "
                   "schedule runs, the other exits at entry)")
         achieved = stage_cells * bytes_per / (stage_ms * 1e-3) / 1e9 if stage_ms > 0 else None
         launches = graph_steps * launches_per_step(case.flags) + (1 if persist_steps else 0)

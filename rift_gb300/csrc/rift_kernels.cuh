@@ -260,6 +260,30 @@ __device__ __forceinline__ void prefetchMaps(const Params& P, uint32_t fl, size_
 }
 
 // Block-wide max (non-negative values); result valid in thread 0.
+// Both speed maxima (valid in thread 0) and the OR of a vote (every thread)
+// with one CTA barrier: the barrier of __syncthreads_or also orders the
+// per-warp maxima written to red.
+__device__ __forceinline__ bool blockMax2Or(float vx, float vy, bool vote, float (*red)[NT / 32],
+                                            float& mx, float& my) {
+    for (int o = 16; o > 0; o >>= 1) {
+        vx = fmaxf(vx, __shfl_xor_sync(0xffffffffu, vx, o));
+        vy = fmaxf(vy, __shfl_xor_sync(0xffffffffu, vy, o));
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        red[0][w] = vx;
+        red[1][w] = vy;
+    }
+    const bool any = __syncthreads_or(vote) != 0;
+    mx = my = 0.f;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+            mx = fmaxf(mx, red[0][k]);
+            my = fmaxf(my, red[1][k]);
+        }
+    return any;
+}
+
 __device__ __forceinline__ float blockMax(float v, float* red) {
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -1183,18 +1207,19 @@ template <int STAGE>
 __device__ __forceinline__ bool tileFlags(const Params& P, const StageConsts& C, StageSmem& S,
                                           int tile, bool wetCell, float spx, float spy) {
     bool wetTile = false;
-    if (STAGE == 2 || C.euler) {
-        bool any = __syncthreads_or(wetCell);
+    if (STAGE == 2) {  // wet vote and both speed maxima with one barrier
+        float mxv, myv;
+        const bool any = blockMax2Or(spx, spy, wetCell, S.red, mxv, myv);
         wetTile = (!(C.fl & F_TILE_ACC)) || any;
-        if (threadIdx.x == 0) P.wet[tile] = (uint8_t)wetTile;
-    }
-    if (STAGE == 2) {
-        float mxv = blockMax(spx, S.red[0]);
-        float myv = blockMax(spy, S.red[1]);
         if (threadIdx.x == 0) {
+            P.wet[tile] = (uint8_t)wetTile;
             P.mx[tile] = mxv;
             P.my[tile] = myv;
         }
+    } else if (C.euler) {
+        bool any = __syncthreads_or(wetCell);
+        wetTile = (!(C.fl & F_TILE_ACC)) || any;
+        if (threadIdx.x == 0) P.wet[tile] = (uint8_t)wetTile;
     }
     return wetTile;  // the tile's new wet flag (stage 2 or Euler), else false
 }
