@@ -228,6 +228,37 @@ void destroyGraph(rift_handle* h) {
 }
 
 // The launch sequence of one step (captured into the graph).
+// The fixed flag set of the march instantiation for this run (0: the
+// generic one reading the run's flags).
+uint32_t marchFix(const rift_handle* h) {
+    const uint32_t f = h->g.flags & CELL_FLAGS;
+    if (((f & F_POINT) != 0) != (h->nsrc > 0)) return 0u;
+    if (f == FIX_RAIN || f == FIX_INFIL_SRC || f == FIX_RAINMAP_DRAIN) return f;
+    return 0u;
+}
+
+template <int STAGE>
+void launchMarch(const rift_handle* h, const CUtensorMap& tmIn, const Params& P, cudaStream_t s,
+                 int grid) {
+    switch (marchFix(h)) {
+        case FIX_RAIN: k_march<STAGE, FIX_RAIN><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P); break;
+        case FIX_INFIL_SRC: k_march<STAGE, FIX_INFIL_SRC><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P); break;
+        case FIX_RAINMAP_DRAIN:
+            k_march<STAGE, FIX_RAINMAP_DRAIN><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
+            break;
+        default: k_march<STAGE><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
+    }
+}
+
+void launchUpdate1(const rift_handle* h, const Params& P, cudaStream_t s) {
+    switch (marchFix(h)) {
+        case FIX_RAIN: k_update1<FIX_RAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
+        case FIX_INFIL_SRC: k_update1<FIX_INFIL_SRC><<<h->gridUpdate, MT, 0, s>>>(P); break;
+        case FIX_RAINMAP_DRAIN: k_update1<FIX_RAINMAP_DRAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
+        default: k_update1<><<<h->gridUpdate, MT, 0, s>>>(P);
+    }
+}
+
 void enqueueStep(rift_handle* h) {
     Params P = makeParams(h);
     cudaStream_t s = h->stream;
@@ -237,12 +268,12 @@ void enqueueStep(rift_handle* h) {
     // per-tile and march variants of each pass; the device keeps one of them
     // (useMarch) and the other returns at once
     k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
-    k_march<1><<<h->gridMarch1, MT, 0, s>>>(h->tmAm, h->tmEm, P);  // fluxes, speeds, dt
+    launchMarch<1>(h, h->tmAm, P, s, h->gridMarch1);  // fluxes, speeds, dt
     k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
-    k_update1<<<h->gridUpdate, MT, 0, s>>>(P);
+    launchUpdate1(h, P, s);
     if (!h->has(RIFT_F_EULER)) {
         k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
-        k_march<2><<<h->gridMarch, MT, 0, s>>>(h->tmBm, h->tmEm, P);
+        launchMarch<2>(h, h->tmBm, P, s, h->gridMarch);
     } else {
         k_commit<<<h->gridStage, NT, 0, s>>>(P);
     }
@@ -539,7 +570,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_march<1>, MT, 0);
     h->gridMarch1 = std::max(1, std::min(NS, h->numSMs * std::max(occ1, 1)));
     int occU = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1, MT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1<>, MT, 0);
     h->gridUpdate = std::max(1, std::min(2 * NS, h->numSMs * std::max(occU, 1)));
     // the march pays off once every resident march CTA has a strip of its own
     h->marchMin = h->numSMs * occ;
@@ -1243,12 +1274,12 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
         k_grow<<<h->gridGrow, NT, 0, s>>>(P);
         k_speed_dt<<<h->gridSpeed, NT, 0, s>>>(h->tmA, h->tmE, P);
         CUDA_TRY(h, cudaEventRecord(e0, s));
-        k_march<1><<<h->gridMarch1, MT, 0, s>>>(h->tmAm, h->tmEm, P);
+        launchMarch<1>(h, h->tmAm, P, s, h->gridMarch1);
         k_stage<1><<<h->gridStage, NT, 0, s>>>(h->tmA, h->tmE, P);
-        k_update1<<<h->gridUpdate, MT, 0, s>>>(P);
+        launchUpdate1(h, P, s);
         if (!h->has(RIFT_F_EULER)) {
             k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
-            k_march<2><<<h->gridMarch, MT, 0, s>>>(h->tmBm, h->tmEm, P);
+            launchMarch<2>(h, h->tmBm, P, s, h->gridMarch);
         } else {
             k_commit<<<h->gridStage, NT, 0, s>>>(P);
         }

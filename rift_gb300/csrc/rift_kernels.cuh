@@ -50,6 +50,24 @@ constexpr uint32_t F_RAIN_U = 1u << 0, F_RAIN_G = 1u << 1, F_DRAIN_U = 1u << 2,
                    F_EULER = 1u << 6, F_SAVE_MAX = 1u << 7, F_SAVE_ARR = 1u << 8,
                    F_TILE_ACC = 1u << 9, F_POINT = 1u << 10, F_H_INIT = 1u << 11;
 
+// Flags that change the per-cell update; a kernel instantiated with a fixed
+// set FIX (!= 0) reads its flags from FIX instead of the run's flags: the
+// engine picks such an instantiation only when the run's flags, masked with
+// CELL_FLAGS, equal FIX (and point sources are present iff FIX has F_POINT).
+constexpr uint32_t CELL_FLAGS = F_RAIN_U | F_RAIN_G | F_DRAIN_U | F_DRAIN_G | F_INFIL | F_SURGE |
+                                F_EULER | F_SAVE_MAX | F_SAVE_ARR | F_TILE_ACC | F_POINT;
+// the fixed sets with march instantiations: uniform rain; infiltration with
+// a point hydrograph; gridded rain with a uniform drain (all with tile
+// acceleration)
+constexpr uint32_t FIX_RAIN = F_RAIN_U | F_TILE_ACC;
+constexpr uint32_t FIX_INFIL_SRC = F_INFIL | F_POINT | F_TILE_ACC;
+constexpr uint32_t FIX_RAINMAP_DRAIN = F_RAIN_G | F_DRAIN_U | F_TILE_ACC;
+
+template <uint32_t FIX>
+__device__ __forceinline__ uint32_t cellFlags(uint32_t runFlags) {
+    return FIX ? FIX : runFlags;
+}
+
 constexpr int ERR_TMA_TIMEOUT = 1;
 constexpr int ERR_BARRIER_TIMEOUT = 2;
 constexpr int ERR_TILE_TABLE = 4;  // persistent loop: tile table and scan disagree
@@ -898,12 +916,12 @@ struct CellSrc {
 };
 
 // BED: add the bed-slope source here (false: the caller's dhu, dhv hold it).
-template <int STAGE, bool PREF = false, bool BED = true>
+template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0>
 __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConsts& C, int tile,
                                                int j, int i, float dh, float dhu, float dhv,
                                                float hC, float hu0, float hv0, float eW, float eE,
                                                float eS, float eN, const float* pre) {
-    const uint32_t fl = C.fl;
+    const uint32_t fl = cellFlags<FIX>(C.fl);
     const size_t c = cidx(P, 0, j, i);
     const float S1 = BED ? bedSourceX(P, hC, eW, eE) : 0.f;
     const float S2 = BED ? bedSourceY(P, hC, eS, eN) : 0.f;
@@ -922,7 +940,7 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
         S0 -= (d > cap) ? cap : d;
     }
     bool srcCell = false;
-    if (P.nsrc > 0) {
+    if ((FIX == 0 || (FIX & F_POINT)) && P.nsrc > 0) {
         const int flat = j * P.nx + i;
         for (int q = P.srcTileStart[tile]; q < P.srcTileStart[tile + 1]; q++) {
             int sidx = P.srcTileList[q];
@@ -958,11 +976,12 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
 
 // edge: the work item holds a cell next to the ghost band (i or j at 2 or
 // at n - 3); false skips the ghost tests for the items inside.
-template <int STAGE, bool PREF = false>
+template <int STAGE, bool PREF = false, uint32_t FIX = 0>
 __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C, int j, int i,
                                            const CellSrc& src, float hC, float hu0, float hv0,
                                            const float* pre, bool edge) {
-    const uint32_t fl = C.fl;
+    const uint32_t fl = cellFlags<FIX>(C.fl);
+    const bool euler = FIX ? (FIX & F_EULER) != 0 : C.euler;
     const size_t c = cidx(P, 0, j, i);
     float dh = src.dh;
     const float dhu = src.dhu, dhv = src.dhv, hc = src.hc, Fc = src.Fc, dF = src.dF;
@@ -984,7 +1003,7 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
         hvN = (hv0 + dhv * dtNew) * den;
         hN = (hN > kEps) ? hN : 0.f;
         if (fl & F_INFIL) C.Fout[c] = Fc + dF * dtNew;
-        if (C.euler) {
+        if (euler) {
             // Euler-mode outputs and wet flags (grid.cu:926-1023)
             const float uC = huN * velFactor(hN, C.kappa), vC = hvN * velFactor(hN, C.kappa);
             if (fl & F_SAVE_MAX) {
@@ -1032,14 +1051,14 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
     return wetCell;
 }
 
-template <int STAGE, bool PREF = false, bool BED = true>
+template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0>
 __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
                                            int i, float dh, float dhu, float dhv, float hC,
                                            float hu0, float hv0, float eW, float eE, float eS,
                                            float eN, const float* pre, bool edge = true) {
-    const CellSrc src = cellSources<STAGE, PREF, BED>(P, C, tile, j, i, dh, dhu, dhv, hC, hu0, hv0,
-                                                      eW, eE, eS, eN, pre);
-    return cellFinish<STAGE, PREF>(P, C, j, i, src, hC, hu0, hv0, pre, edge);
+    const CellSrc src = cellSources<STAGE, PREF, BED, FIX>(P, C, tile, j, i, dh, dhu, dhv, hC, hu0,
+                                                           hv0, eW, eE, eS, eN, pre);
+    return cellFinish<STAGE, PREF, FIX>(P, C, j, i, src, hC, hu0, hv0, pre, edge);
 }
 
 

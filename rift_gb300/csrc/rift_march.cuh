@@ -104,7 +104,7 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
 //          ComputeTimestep), re-sync of U* on tiles that went inactive.
 // STAGE 2: reads U* (B) and U^n (A) at the cell -> writes U^{n+1} (A),
 //          F^{n+1} (FA), outputs, tile wet flags and tile speeds.
-template <int STAGE>
+template <int STAGE, uint32_t FIX = 0>
 __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtensorMap tmIn,
                                               const __grid_constant__ CUtensorMap tmE, Params P) {
     __shared__ MarchSmem S;
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                 nextPre[0] = P.A[cn];
                 nextPre[1] = P.A[cn + P.planeSize];
                 nextPre[2] = P.A[cn + 2 * (size_t)P.planeSize];
-                prefetchMaps(P, C.fl, cn);
+                prefetchMaps(P, cellFlags<FIX>(C.fl), cn);
             }
             const int tslot = ((R - 2) / TH) * STRIP_TX + tcol;
             const bool cellOn = colIn && S.tact[tslot] && j <= P.ny - 3;
@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                         P.D[c + 2 * (size_t)P.planeSize] = dhv + bedSourceY(P, cur.h, cur.eS, cur.eN);
                     } else {
                         const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
-                        accWet |= cellUpdate<STAGE>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
+                        accWet |= cellUpdate<STAGE, false, true, FIX>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
                                                     cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre,
                                                     edgeStrip);
                     }
@@ -315,6 +315,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
 // halo, so the work item is half a strip (one tile row of 7 tiles): finer
 // items balance the grid.  One thread per column, rows in pairs whose loads
 // are in flight together (64 registers: 8 CTAs per SM).
+template <uint32_t FIX = 0>
 __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
     __shared__ int tact[STRIP_TX];
     __shared__ int twet[STRIP_TX];
@@ -362,14 +363,14 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
                         v[q][4] = P.A[c + pl];
                         v[q][5] = P.A[c + 2 * pl];
                         v[q][6] = P.nman[c];
-                        prefetchMaps(P, C.fl, c);
+                        prefetchMaps(P, cellFlags<FIX>(C.fl), c);
                     }
                 }
 #pragma unroll
                 for (int q = 0; q < G; q++) {
                     if (!on[q]) continue;
                     const float pre[1] = {v[q][6]};
-                    wetAny |= cellUpdate<1, false, false>(P, C, tile, Y0 + r0 + q, i, v[q][0],
+                    wetAny |= cellUpdate<1, false, false, FIX>(P, C, tile, Y0 + r0 + q, i, v[q][0],
                                                           v[q][1], v[q][2], v[q][3], v[q][4],
                                                           v[q][5], 0.f, 0.f, 0.f, 0.f, pre,
                                                           edgeStrip);
