@@ -250,6 +250,15 @@ void launchMarch(const rift_handle* h, const CUtensorMap& tmIn, const Params& P,
     }
 }
 
+// The persistent loop's instantiation for this run (two fixed flag sets).
+const void* persistKernel(const rift_handle* h) {
+    switch (marchFix(h)) {
+        case FIX_RAIN: return (const void*)k_persist<FIX_RAIN>;
+        case FIX_INFIL_SRC: return (const void*)k_persist<FIX_INFIL_SRC>;
+        default: return (const void*)k_persist<>;
+    }
+}
+
 void launchUpdate1(const rift_handle* h, const Params& P, cudaStream_t s) {
     switch (marchFix(h)) {
         case FIX_RAIN: k_update1<FIX_RAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
@@ -583,7 +592,12 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     int coop = 0;
     cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
     occ = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_persist, NT, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_persist<>, NT, 0);
+    for (const void* fn : {(const void*)k_persist<FIX_RAIN>, (const void*)k_persist<FIX_INFIL_SRC>}) {
+        int o = 0;  // every instantiation must fit the same cooperative grid
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, NT, 0);
+        occ = std::min(occ, o);
+    }
     if (coop && occ > 0) {
         h->gridPersist = std::min(h->numSMs * occ, PERSIST_MAX_CTAS);
         CUDA_TRY(h, cudaMalloc(&h->gbar, sizeof(GridBar)));
@@ -874,7 +888,7 @@ int launchPersist(rift_handle* h, int nsteps) {
     Params P = makeParams(h);
     const int grid = persistGrid(h);
     void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
-    CUDA_TRY(h, cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0,
+    CUDA_TRY(h, cudaLaunchCooperativeKernel(persistKernel(h), dim3(grid), dim3(NT), args, 0,
                                             h->stream));
     return RIFT_OK;
 }
@@ -949,7 +963,7 @@ bool stepGraph(rift_handle* h, int& rc) {
         }
         cudaMemcpyAsync(h->st, h->hst, sizeof(DevState), cudaMemcpyHostToDevice, h->stream);
         cudaMemsetAsync(h->gbar, 0, GRIDBAR_CLEAR, h->stream);
-        cudaLaunchCooperativeKernel((const void*)k_persist, dim3(grid), dim3(NT), args, 0, h->stream);
+        cudaLaunchCooperativeKernel(persistKernel(h), dim3(grid), dim3(NT), args, 0, h->stream);
         cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream);
         cudaError_t e = cudaStreamEndCapture(h->stream, &g);
         if (e != cudaSuccess || !g ||

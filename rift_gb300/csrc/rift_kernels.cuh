@@ -1174,7 +1174,7 @@ __device__ __forceinline__ void tilePrefetch(const Params& P, const StageConsts&
 
 // Update of the interior cell of thread tid < 224 of a staged tile from its
 // divergence; returns its wet vote.
-template <int STAGE>
+template <int STAGE, uint32_t FIX = 0>
 __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConsts& C,
                                                const TileBuf& T, int tile, int i0, int j0, float dh,
                                                float dhu, float dhv, const float (&pre)[6]) {
@@ -1185,13 +1185,13 @@ __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConst
     const int r = ty + 2, c = tx + 2;
     // tile-uniform: does the tile reach the first or last interior row/column?
     const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
-    return cellUpdate<STAGE, true>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][r][c], T.in[1][r][c],
+    return cellUpdate<STAGE, true, true, FIX>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][r][c], T.in[1][r][c],
                                    T.in[2][r][c], T.e[0][r][c], T.e[1][r][c], T.e[2][r][c],
                                    T.e[3][r][c], pre, edge);
 }
 
 // tileCellUpdate in its two halves (see cellSources / cellFinish).
-template <int STAGE>
+template <int STAGE, uint32_t FIX = 0>
 __device__ __forceinline__ CellSrc tileCellSources(const Params& P, const StageConsts& C,
                                                    const TileBuf& T, int tile, int i0, int j0,
                                                    float dh, float dhu, float dhv,
@@ -1202,12 +1202,12 @@ __device__ __forceinline__ CellSrc tileCellSources(const Params& P, const StageC
     CellSrc r{};
     if (tid >= TH * TW || i > P.nx - 3 || j > P.ny - 3) return r;
     const int rr = ty + 2, cc = tx + 2;
-    return cellSources<STAGE, true>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][rr][cc],
+    return cellSources<STAGE, true, true, FIX>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][rr][cc],
                                     T.in[1][rr][cc], T.in[2][rr][cc], T.e[0][rr][cc],
                                     T.e[1][rr][cc], T.e[2][rr][cc], T.e[3][rr][cc], pre);
 }
 
-template <int STAGE>
+template <int STAGE, uint32_t FIX = 0>
 __device__ __forceinline__ bool tileCellFinish(const Params& P, const StageConsts& C,
                                                const TileBuf& T, int i0, int j0,
                                                const CellSrc& src, const float (&pre)[6]) {
@@ -1217,7 +1217,7 @@ __device__ __forceinline__ bool tileCellFinish(const Params& P, const StageConst
     if (tid >= TH * TW || i > P.nx - 3 || j > P.ny - 3) return false;
     const int rr = ty + 2, cc = tx + 2;
     const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
-    return cellFinish<STAGE, true>(P, C, j, i, src, T.in[0][rr][cc], T.in[1][rr][cc],
+    return cellFinish<STAGE, true, FIX>(P, C, j, i, src, T.in[0][rr][cc], T.in[1][rr][cc],
                                    T.in[2][rr][cc], pre, edge);
 }
 
@@ -1248,7 +1248,7 @@ __device__ __forceinline__ bool tileFlags(const Params& P, const StageConsts& C,
 //          (A), F^{n+1} (FA), outputs, tile wet flags and tile speeds.
 // Tile loop of RK stage STAGE over the scheduled active tiles.  False after
 // a TMA timeout (error recorded).
-template <int STAGE>
+template <int STAGE, uint32_t FIX = 0>
 __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensorMap* tmE,
                            const Params& P, int nAct, uint32_t* ph,
                            const StageConsts* given = nullptr) {
@@ -1269,7 +1269,7 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
         const TileBuf& T = S.buf[bsel];
         float dh, dhu, dhv, spx, spy;
         tileFluxDiv<STAGE == 2>(S, T, P, i0, j0, dh, dhu, dhv, spx, spy);
-        const bool wetCell = tileCellUpdate<STAGE>(P, C, T, tile, i0, j0, dh, dhu, dhv, pre);
+        const bool wetCell = tileCellUpdate<STAGE, FIX>(P, C, T, tile, i0, j0, dh, dhu, dhv, pre);
         tileFlags<STAGE>(P, C, S, tile, wetCell, spx, spy);
         __syncthreads();
     }

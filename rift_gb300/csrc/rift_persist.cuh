@@ -313,6 +313,7 @@ __device__ __forceinline__ bool waitNeighbour(const Params& P, int tile, int q, 
     return false;
 }
 
+template <uint32_t FIX = 0>
 __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUtensorMap tmA,
                                                 const __grid_constant__ CUtensorMap tmB,
                                                 const __grid_constant__ CUtensorMap tmE, Params P,
@@ -494,7 +495,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             }
             __syncthreads();
             // (kept in shared memory across the wait: registers stay free)
-            if (mine) sSrc[tid] = tileCellSources<1>(P, sPre, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
+            if (mine) sSrc[tid] = tileCellSources<1, FIX>(P, sPre, S.buf[0], tile, i0, j0, dh, dhu, dhv, pre);
             if (!gridWait(P.gbar, barTarget, st)) return;
             // dt of this step (Simulator::ComputeTimestep), by thread 0 of
             // every CTA; the FP64 arithmetic stays in one thread
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             nActPrev = sSched;
             if (mine) {  // the rest of the stage-1 update with this step's dt (Integrate_1_k)
                 const StageConsts C1 = sC[0];
-                const bool wetCell = tileCellFinish<1>(P, C1, S.buf[0], i0, j0, sSrc[tid], pre);
+                const bool wetCell = tileCellFinish<1, FIX>(P, C1, S.buf[0], i0, j0, sSrc[tid], pre);
                 tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
                 __syncthreads();
             }
@@ -561,7 +562,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                     float sx2, sy2;
                     tileFluxDiv<true>(S, S.buf[1], P, i0, j0, dh, dhu, dhv, sx2, sy2);
                     const bool wetCell =
-                        tileCellUpdate<2>(P, C2, S.buf[1], tile, i0, j0, dh, dhu, dhv, pre);
+                        tileCellUpdate<2, FIX>(P, C2, S.buf[1], tile, i0, j0, dh, dhu, dhv, pre);
                     const bool wetNew = tileFlags<2>(P, C2, S, tile, wetCell, sx2, sy2);
                     if ((table || built) && wetNew && !wetOld && tid < 4)
                         tableClaim(P, tile, &sOverflow);
@@ -631,10 +632,10 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
         __syncthreads();
         tNow = sC[1].tNew;  // published by finishDt before the barrier
         dtPrev = sDt;
-        if (!stageTiles<1>(S, &tmA, &tmE, P, nAct, ph, &sC[0])) return;
+        if (!stageTiles<1, FIX>(S, &tmA, &tmE, P, nAct, ph, &sC[0])) return;
         RIFT_SYNC();
         if (!euler) {
-            if (!stageTiles<2>(S, &tmB, &tmE, P, nAct, ph, &sC[1])) return;
+            if (!stageTiles<2, FIX>(S, &tmB, &tmE, P, nAct, ph, &sC[1])) return;
         } else {
             commitTiles(P, nAct);
         }
