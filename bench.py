@@ -1,6 +1,6 @@
 """Benchmark of the GB300 RIFT step (one JSON line on stdout).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3|5]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3|4|5]
                     [--impl ours|reference]
 
 A step is one full RK2 time step (both stages, Grow, dt) of the whole domain
@@ -9,6 +9,11 @@ seeded synthetic configs of rift_gb300.synth (no datasets are involved):
   1: 512^2 bumpy plane, uniform rain           (the reference's small case)
   2: 2048^2 fractal + channel, point-source hydrograph, Green-Ampt (default)
   3: 8192^2 urban fractal with buildings, uniform drain, interpolated rain maps
+  4: the learned flux closure: training patches from fine runs of seeded
+     1024^2 scenarios, Adam on the tensor-core kernels, then held-out
+     scenarios run fine (N^2 at 2 m) and coarse ((N/2)^2 at 4 m, plain and
+     with the closure); metric the fine/closure wall-time ratio, with the
+     peak-depth RMSE and arrival-time error against the fine run
   5: a batched ensemble (--members, --side-min/--side-max, --tf) run to tf in
      one persistent kernel; metric members/hour, per-member p50/p99, and the
      same members run one after another for comparison
@@ -71,6 +76,15 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def bf16_peak():
+    """Dense BF16 burst rate (TFLOP/s) of MEASURED_PEAKS.json, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return {"bf16_tflops": float(json.load(f)["bf16_tflops"]), "kind": "measured"}
+    except Exception:
+        return {"bf16_tflops": 1900.0, "kind": "fallback"}
 
 
 class ClockSampler:
@@ -454,12 +468,154 @@ def run_ensemble(args):
     return line
 
 
+def _timed_chunks(run_to, tf, every_s, depth):
+    """Run to tf in chunks of every_s simulated seconds; returns the wall time
+    of the runs alone and the first time each interior cell's depth exceeded
+    ARRIVAL_DEPTH at a chunk end (inf where it never did)."""
+    import torch
+    wall, t = 0.0, 0.0
+    arrival = None
+    while t < tf:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        t = run_to(min(t + every_s, tf))
+        torch.cuda.synchronize()
+        wall += time.perf_counter() - t0
+        h = depth()
+        if arrival is None:
+            arrival = np.full(h.shape, np.inf)
+        arrival[(h > ARRIVAL_DEPTH) & np.isinf(arrival)] = t
+    return wall, arrival
+
+
+ARRIVAL_DEPTH = 0.05  # m: a cell has "arrived" once its depth passes 5 cm
+
+
+def run_closure(args):
+    """Config 4: train the closure on fine runs of --closure-seeds scenarios
+    (1024^2 at 2 m), then run held-out scenarios fine (N^2 at 2 m) and
+    coarse ((N/2)^2 at 4 m, plain and with the closure) to --tf."""
+    import torch
+
+    from rift_gb300 import closure
+
+    def log(m):
+        print(m, file=sys.stderr, flush=True)
+
+    N = args.N or 4096
+    t0 = time.perf_counter()
+    ds = closure.generate(list(range(args.closure_seeds)), N=args.closure_train_N, cell=2.0, log=log)
+    t_gen = time.perf_counter() - t0
+    log(f"{len(ds.feats)} patches in {t_gen:.1f} s")
+    t0 = time.perf_counter()
+    model, loss = closure.train(ds, steps=args.train_steps, batch=256, log=log)
+    t_train = time.perf_counter() - t0
+    n_patches = len(ds.feats)
+    del ds
+    clocks = ClockSampler().start()
+    evals = []
+    for k in range(args.eval_seeds):
+        seed = 100_000 + k
+        fc = closure.scenario(seed, N=N, cell=2.0, tf=args.tf)
+        cc = closure.coarse_case(fc)
+        res = {"seed": seed, "generator": "config1" if seed % 2 == 0 else "config2"}
+
+        def interior_depth(sim):
+            return (sim.field("W") - bc_of[id(sim)])[2:-2, 2:-2]
+
+        bc_of = {}
+        fine = capi.Sim(fc).setup()
+        bc_of[id(fine)] = fine.field("BC")
+        w_f, arr_f = _timed_chunks(lambda t: fine.run(2 ** 31 - 1, t)[0], args.tf, 120.0,
+                                   lambda: interior_depth(fine))
+        hmax_f = closure.restrict(fine.field("HMAX")[2:-2, 2:-2])
+        fine.close()
+        n2 = arr_f.shape[0] // 2
+        arr_f = arr_f.reshape(n2, 2, n2, 2).min(axis=(1, 3))
+        wet = hmax_f > 0.01
+        for mode in ("plain", "closure"):
+            sim = capi.Sim(cc).setup()
+            bc_of[id(sim)] = sim.field("BC")
+            if mode == "closure":
+                cr = closure.ClosureRun(sim, model, every=args.closure_every)
+                w, arr = _timed_chunks(cr.run, args.tf, 120.0, lambda: interior_depth(sim))
+                res["closure_blocks"], res["closure_fallback_blocks"] = cr.block_counts()
+                res["closure_applies"] = cr.applies
+            else:
+                w, arr = _timed_chunks(lambda t: sim.run(2 ** 31 - 1, t)[0], args.tf, 120.0,
+                                       lambda: interior_depth(sim))
+            hmax = sim.field("HMAX")[2:-2, 2:-2]
+            both = np.isfinite(arr) & np.isfinite(arr_f)
+            res[mode] = {"wall_s": w,
+                         "peak_depth_rmse_m": float(np.sqrt(np.mean((hmax - hmax_f)[wet] ** 2))),
+                         "arrival_mae_s": float(np.mean(np.abs(arr - arr_f)[both])) if both.any() else None,
+                         "arrival_missed_frac": float(np.mean(np.isinf(arr) & np.isfinite(arr_f)))}
+            sim.close()
+        res["fine_wall_s"] = w_f
+        res["wet_cells"] = int(wet.sum())
+        res["speedup_closure"] = w_f / res["closure"]["wall_s"]
+        res["speedup_plain"] = w_f / res["plain"]["wall_s"]
+        evals.append(res)
+        log(json.dumps(res))
+    clk = clocks.stop()
+    # tensor-core rate of the closure step: re-run the apply kernels on the
+    # last coarse state, timed with CUDA events on the engine's stream
+    sim = capi.Sim(cc).setup()
+    sim.run(2 ** 31 - 1, min(args.tf, 1800.0))
+    cr = closure.ClosureRun(sim, model, every=args.closure_every)
+    st = torch.cuda.ExternalStream(cr.view.stream)
+    cr.apply(1e-3, 1800.0)
+    torch.cuda.synchronize()
+    b0 = cr.block_counts()[0]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    e0.record(st)
+    for _ in range(reps):
+        cr.apply(1e-3, 1800.0)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    blocks = (cr.block_counts()[0] - b0) / reps
+    sim.close()
+    flops = blocks * 256 * 2 * (150 * 32 + 288 * 32 + 32 * 4)
+    pk = bf16_peak()
+    achieved = flops / (ms * 1e-3) / 1e12
+    sp = float(np.mean([r["speedup_closure"] for r in evals]))
+    line = {"metric": "closure vs fine-grid wall-time ratio", "value": sp, "unit": "x",
+            "n_gpus": 1, "steps": None, "warmup": 0, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 net / f32 solver",
+            "data": "synthetic",
+            "config": {"workload": "config4", "fine": f"{N}^2 at 2 m", "coarse": f"{N // 2}^2 at 4 m",
+                       "tf_s": args.tf, "train_scenarios": args.closure_seeds,
+                       "train_grid": f"{args.closure_train_N}^2 at 2 m", "train_patches": n_patches,
+                       "train_steps": args.train_steps, "batch": 256, "closure_every_steps": args.closure_every,
+                       "eval_scenarios": args.eval_seeds},
+            "peak_depth_rmse_m": {"closure": float(np.mean([r["closure"]["peak_depth_rmse_m"] for r in evals])),
+                                  "plain_coarse": float(np.mean([r["plain"]["peak_depth_rmse_m"] for r in evals]))},
+            "speedup_plain_coarse": float(np.mean([r["speedup_plain"] for r in evals])),
+            "evals": evals,
+            "training": {"generate_s": t_gen, "train_s": t_train, "loss_first": float(loss[:20].mean()),
+                         "loss_last": float(loss[-20:].mean())},
+            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"],
+                         "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                         "peak_kind": pk["kind"], "kernel": "k_closure + k_apply (one closure step)",
+                         "ms_per_apply": ms, "blocks_per_apply": blocks},
+            "clocks": clk, "gpu_launches": None}
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3, 5))
+    ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3, 4, 5))
+    ap.add_argument("--closure-seeds", type=int, default=48, help="config 4: training scenarios")
+    ap.add_argument("--closure-train-N", type=int, default=1024, help="config 4: training grid side")
+    ap.add_argument("--train-steps", type=int, default=1500, help="config 4: Adam steps")
+    ap.add_argument("--eval-seeds", type=int, default=2, help="config 4: held-out scenarios")
+    ap.add_argument("--closure-every", type=int, default=4,
+                    help="config 4: coarse steps between closure applications")
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")
     ap.add_argument("--side-min", type=int, default=128, help="config 5: smallest side (cells)")
     ap.add_argument("--side-max", type=int, default=512, help="config 5: largest side (cells)")
@@ -485,6 +641,10 @@ def main():
     if args.config == 5 and args.impl != "reference":
         if rank == 0:
             print(json.dumps(run_ensemble(args)))
+        return
+    if args.config == 4 and args.impl != "reference":
+        if rank == 0:
+            print(json.dumps(run_closure(args)))
         return
     if args.impl == "reference":
         if rank != 0:

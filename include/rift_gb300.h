@@ -242,6 +242,32 @@ int rift_get_table_steps(rift_handle* h, int64_t* table_steps);
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
 
+/* Device-side view of a handle's state, for kernels of other libraries that
+ * run between steps on the handle's stream (the learned flux closure).  No
+ * reference counterpart.  Every plane is FP32 with `pitch` floats per row and
+ * `rows` rows; cell (j, i) of the h-grid (ghost ring included) sits at
+ * [j*pitch + i].  h, hu, hv hold U^n between calls; e holds four planes one
+ * plane (rows*pitch floats) apart: eW, eE, eS, eN, each face elevation minus
+ * the cell's reference elevation.  t and dt point at the device FP64
+ * simulated time and the last step's dt, valid once the previous call has
+ * returned.  A caller may change h, hu and hv of interior cells that are not
+ * next to the ghost ring (3 <= i <= h_nx-4, 3 <= j <= h_ny-4) between calls,
+ * on `stream`, provided no wet cell (h > 1.19e-7 m) becomes dry and no dry
+ * cell wet: the tile activity the engine tracks then stays exact. */
+typedef struct rift_device_view {
+    float* h;
+    float* hu;
+    float* hv;
+    const float* e;
+    const float* n;
+    const double* t;
+    const double* dt;
+    void* stream;        /* cudaStream_t */
+    int32_t h_nx, h_ny, pitch, rows;
+    double dx, dy, kappa;
+} rift_device_view;
+int rift_get_device_view(rift_handle* h, rift_device_view* v);
+
 /* Volume sum for callers that cannot allocate device memory.  This entry
  * point has no counterpart in the reference.
  *

@@ -56,17 +56,36 @@ def build_host(force: bool = False) -> str:
     return HOST_LIB
 
 
+CLOSURE_LIB = os.path.join(LIB_DIR, "librift_closure.so")
+CLOSURE_DEPS = ["rift_closure.cu", "rift_device.cuh"]
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
+    """The engine and the closure library, compiled side by side."""
     os.makedirs(LIB_DIR, exist_ok=True)
-    deps = [os.path.join(SRC, d) for d in DEPS]
-    deps.append(os.path.join(os.path.dirname(HERE), "include", "rift_gb300.h"))
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    jobs = []
+    deps = [os.path.join(SRC, d) for d in DEPS] + [os.path.join(inc, "rift_gb300.h")]
     if force or _stale(LIB, deps):
-        cmd = ["nvcc", *ARCH, *FLAGS, "-o", LIB, *[os.path.join(SRC, s) for s in SOURCES]]
-        if verbose:
+        jobs.append(["nvcc", *ARCH, *FLAGS, "-o", LIB, *[os.path.join(SRC, s) for s in SOURCES]])
+    cdeps = [os.path.join(SRC, d) for d in CLOSURE_DEPS]
+    cdeps += [os.path.join(inc, "rift_closure.h"), os.path.join(inc, "rift_gb300.h")]
+    if force or _stale(CLOSURE_LIB, cdeps):
+        jobs.append(["nvcc", *ARCH, *FLAGS, "-o", CLOSURE_LIB, os.path.join(SRC, "rift_closure.cu")])
+    if verbose:
+        for cmd in jobs:
             cmd.insert(1, "-Xptxas=-v")
-        r = _run(cmd)
-        if verbose:
-            print(r.stderr)
+    procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+             for cmd in jobs]
+    errors = []
+    for cmd, p in zip(jobs, procs):
+        out, err = p.communicate()
+        if p.returncode != 0:
+            errors.append(f"{cmd[0]} failed:\n{out}\n{err}")
+        elif verbose:
+            print(err)
+    if errors:
+        raise RuntimeError("\n".join(errors))
     return LIB
 
 

@@ -29,6 +29,14 @@ class GridDesc(C.Structure):
                 ("device", C.c_int32)]
 
 
+class DeviceView(C.Structure):
+    """rift_device_view: device pointers of a handle's state (include/rift_gb300.h)."""
+    _fields_ = [("h", C.c_void_p), ("hu", C.c_void_p), ("hv", C.c_void_p), ("e", C.c_void_p),
+                ("n", C.c_void_p), ("t", C.c_void_p), ("dt", C.c_void_p), ("stream", C.c_void_p),
+                ("h_nx", C.c_int32), ("h_ny", C.c_int32), ("pitch", C.c_int32), ("rows", C.c_int32),
+                ("dx", C.c_double), ("dy", C.c_double), ("kappa", C.c_double)]
+
+
 class RiftError(RuntimeError):
     pass
 
@@ -88,6 +96,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                     [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)])
         ns["get_table_steps"] = _sig(lib, p + "get_table_steps", C.c_int,
                                      [_P, C.POINTER(C.c_int64)])
+    if hasattr(lib, p + "get_device_view"):
+        ns["get_device_view"] = _sig(lib, p + "get_device_view", C.c_int, [_P, C.POINTER(DeviceView)])
     ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
     ns["step"] = _sig(lib, p + "step", C.c_int, [_P, _D, _D])
     ns["run"] = _sig(lib, p + "run", C.c_int, [_P, C.c_int32, C.c_double, _D, _D, _I])
@@ -292,6 +302,12 @@ class Sim:
         my = np.zeros(self.grid_size)
         self._check(self.f["get_tile_speeds"](self.h, _dp(mx), _dp(my)), "get_tile_speeds")
         return mx, my
+
+    def device_view(self):
+        """Device pointers of U^n, the face offsets and n (DeviceView)."""
+        v = DeviceView()
+        self._check(self.f["get_device_view"](self.h, C.byref(v)), "get_device_view")
+        return v
 
     def time(self):
         t, dt = C.c_double(), C.c_double()

@@ -1,0 +1,896 @@
+// rift_closure.cu -- learned sub-grid flux closure on a 2x-coarsened grid.
+//
+// The net (6 -> 32 channels 5x5, 32 -> 32 3x3, 32 -> 4 1x1, ReLU between)
+// runs tile by tile: a CTA stages a 22 x 22 block of the six input channels,
+// computes layer 1 on the 18 x 18 cells that layer 2 needs, and layers 2 and
+// 3 on the 16 x 16 output cells.  Every contraction is an implicit GEMM on
+// the BF16 tensor cores (mma.sync m16n8k16, FP32 accumulation): the rows of
+// an MMA tile are 16 cells, the columns output channels, and the reduction
+// runs over (tap, input channel).  Layer 1 activations stay in shared memory
+// as BF16 in channels-last rows of 40 (32 channels + 8 of padding, so the
+// fragment loads of eight consecutive cells fall in distinct banks); layer 2
+// outputs stay in registers, and their accumulator fragments are the A
+// fragments of layer 3 without leaving the thread.
+//
+// The training kernel recomputes the forward pass of its tile and runs the
+// backward pass in the same CTA: layer-3 gradients on the CUDA cores (4 x 32
+// weights), the layer-2 and layer-1 weight gradients and the layer-1
+// activation gradient as tensor-core GEMMs.  Weight gradients stay in
+// registers across every tile a CTA visits and are added to the global
+// gradient once per CTA.
+//
+// The flux kernel evaluates the step's central-upwind face flux
+// (rift_device.cuh) on a handle's state, for the time-integrated fluxes
+// through coarse faces that make the training targets.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/rift_closure.h"
+#include "rift_device.cuh"
+
+namespace rc {
+
+constexpr int CIN = 6, C1 = 32, COUT = 4;
+constexpr int K1 = 150, K1P = 160, K2 = 288;
+constexpr int OT = 16;           // output tile side
+constexpr int R1 = OT + 2;       // layer-1 region side (18)
+constexpr int RI = OT + 6;       // input region side (22)
+constexpr int NR1 = R1 * R1;     // 324
+constexpr int NRI = RI * RI;     // 484
+constexpr int M1T = (NR1 + 15) / 16;  // 21 MMA row tiles of layer 1
+constexpr int SA = 40;           // BF16 row stride of the activation tiles
+constexpr int SW1 = 168, SW2 = 296, SW3 = 40;  // BF16 row strides of the weights
+constexpr int NT = 256;
+constexpr int BEDBIT = 1 << 20, OFFMASK = BEDBIT - 1;
+
+constexpr int OFF_W1 = RIFT_CLOSURE_OFF_W1, OFF_B1 = RIFT_CLOSURE_OFF_B1;
+constexpr int OFF_W2 = RIFT_CLOSURE_OFF_W2, OFF_B2 = RIFT_CLOSURE_OFF_B2;
+constexpr int OFF_W3 = RIFT_CLOSURE_OFF_W3, OFF_B3 = RIFT_CLOSURE_OFF_B3;
+static_assert(OFF_B1 == OFF_W1 + C1 * K1P && OFF_W2 == OFF_B1 + C1 && OFF_B2 == OFF_W2 + C1 * K2 &&
+                  OFF_W3 == OFF_B2 + C1 && OFF_B3 == OFF_W3 + 8 * C1 &&
+                  RIFT_CLOSURE_NPARAM == OFF_B3 + 8,
+              "parameter layout");
+
+struct NetSmem {
+    float xs[NRI * CIN];       // scaled inputs, channels last
+    uint16_t a1[NR1 * SA];     // layer-1 activations (BF16); dZ1 in the backward pass
+    uint16_t w1[C1 * SW1];     // W1[o][k]
+    uint16_t w2[C1 * SW2];     // W2[o][k]
+    uint16_t w3[8 * SW3];      // W3[o][c], rows 4..7 zero
+    float b1[C1], b2[C1], b3[8];
+    int koffP[K1P / 2];        // layer-1 A fragments: offset of the k pair (2kp, 2kp+1) in xs
+    int koffE[K1P];            // the same per element (layer-1 weight gradient)
+    int red[4];
+};
+
+struct TrainSmem {
+    NetSmem n;
+    uint16_t a2[OT * OT * SA];  // layer-2 activations, then dZ2
+    uint16_t w2t[K2 * SA];      // W2 transposed: [k][o]
+    float dout[OT * OT * 4];
+    float w3f[4 * C1];
+    double red[NT / 32];
+};
+
+__device__ __forceinline__ uint16_t bf(float x) { return __bfloat16_as_ushort(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float fb(uint16_t x) { return __bfloat162float(__ushort_as_bfloat16(x)); }
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+    return (uint32_t)bf(lo) | ((uint32_t)bf(hi) << 16);
+}
+__device__ __forceinline__ uint32_t pack16(uint16_t lo, uint16_t hi) {
+    return (uint32_t)lo | ((uint32_t)hi << 16);
+}
+__device__ __forceinline__ uint32_t ld32(const uint16_t* p) {
+    return *reinterpret_cast<const uint32_t*>(p);
+}
+__device__ __forceinline__ void st32(uint16_t* p, uint32_t v) { *reinterpret_cast<uint32_t*>(p) = v; }
+__device__ __forceinline__ float relu(float x) { return fmaxf(x, 0.f); }
+
+// D += A(16x16, row) * B(16x8, col), BF16 inputs, FP32 accumulators.
+// Fragments (g = lane/4, t = lane%4): a[0] rows g, cols 2t..2t+1; a[1] rows
+// g+8; a[2] rows g, cols 2t+8..; a[3] rows g+8, cols 2t+8..; b0 rows (k)
+// 2t..2t+1 of col g, b1 rows 2t+8..; d[0..1] row g cols 2t..2t+1, d[2..3]
+// row g+8.
+__device__ __forceinline__ void mma16816(float d[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Weights (BF16), biases and the layer-1 offset tables, once per CTA.
+__device__ void stageNet(NetSmem& S, const float* __restrict__ P) {
+    const int tid = threadIdx.x;
+    for (int i = tid; i < C1 * SW1; i += NT) {
+        int o = i / SW1, k = i % SW1;
+        S.w1[i] = bf(k < K1 ? P[OFF_W1 + o * K1P + k] : 0.f);
+    }
+    for (int i = tid; i < C1 * SW2; i += NT) {
+        int o = i / SW2, k = i % SW2;
+        S.w2[i] = bf(k < K2 ? P[OFF_W2 + o * K2 + k] : 0.f);
+    }
+    for (int i = tid; i < 8 * SW3; i += NT) {
+        int o = i / SW3, k = i % SW3;
+        S.w3[i] = bf(o < COUT && k < C1 ? P[OFF_W3 + o * C1 + k] : 0.f);
+    }
+    if (tid < C1) {
+        S.b1[tid] = P[OFF_B1 + tid];
+        S.b2[tid] = P[OFF_B2 + tid];
+    }
+    if (tid < 8) S.b3[tid] = tid < COUT ? P[OFF_B3 + tid] : 0.f;
+    for (int k = tid; k < K1P; k += NT) {
+        int e = -1;
+        if (k < K1) {
+            int tap = k / CIN, c = k % CIN;
+            e = ((tap / 5) * RI + tap % 5) * CIN + c;
+            if (c == 3) e |= BEDBIT;
+        }
+        S.koffE[k] = e;
+        if ((k & 1) == 0) {
+            int p = -1;
+            if (k < K1) {
+                int tap = k / CIN, c = k % CIN;
+                p = ((tap / 5) * RI + tap % 5) * CIN + c;
+                if (c == 2) p |= BEDBIT;  // the pair (hv, b): its second element is the bed
+            }
+            S.koffP[k >> 1] = p;
+        }
+    }
+}
+
+// The 22 x 22 input block whose corner is image cell (Y0, X0) of sample s.
+__device__ void stageInput(NetSmem& S, const rift_closure_src& src, int s, int Y0, int X0) {
+    const size_t sbase = (size_t)s * (size_t)src.sample_stride;
+    for (int i = threadIdx.x; i < NRI; i += NT) {
+        int ry = i / RI, rx = i % RI;
+        int y = min(max(Y0 + ry, 0), src.H - 1), x = min(max(X0 + rx, 0), src.W - 1);
+        size_t off = sbase + (size_t)y * (size_t)src.pitch + (size_t)x;
+#pragma unroll
+        for (int c = 0; c < CIN; c++) {
+            float v = src.plane[c] ? __ldg(src.plane[c] + off) : src.value[c];
+            S.xs[i * CIN + c] = v * src.scale[c];
+        }
+    }
+}
+
+// Layer-1 input pair (k, k+1) of the cell whose 5x5 window starts at xs
+// offset `base`: the bed enters relative to the window's centre bc.
+__device__ __forceinline__ uint32_t featPair(const NetSmem& S, int base, float bc, int e) {
+    if (e < 0) return 0u;
+    float2 v = *reinterpret_cast<const float2*>(&S.xs[base + (e & OFFMASK)]);
+    if (e & BEDBIT) v.y -= bc;
+    return pack2(v.x, v.y);
+}
+__device__ __forceinline__ float featElem(const NetSmem& S, int base, float bc, int e) {
+    if (e < 0) return 0.f;
+    float v = S.xs[base + (e & OFFMASK)];
+    return (e & BEDBIT) ? v - bc : v;
+}
+__device__ __forceinline__ int winBase(int q) { return ((q / R1) * RI + q % R1) * CIN; }
+__device__ __forceinline__ float winBed(const NetSmem& S, int base) {
+    return S.xs[base + (2 * RI + 2) * CIN + 3];
+}
+
+// Layer 1 on the 18 x 18 region: a1 = relu(W1 x + b1), BF16.
+__device__ void conv1(NetSmem& S, int warp, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    for (int mt = warp; mt < M1T; mt += NT / 32) {
+        const int r0 = mt * 16 + g, r1 = r0 + 8;
+        const int q0 = min(r0, NR1 - 1), q1 = min(r1, NR1 - 1);
+        const int base0 = winBase(q0), base1 = winBase(q1);
+        const float bc0 = winBed(S, base0), bc1 = winBed(S, base1);
+        float acc[4][4] = {};
+#pragma unroll
+        for (int ks = 0; ks < K1P / 16; ks++) {
+            const int e0 = S.koffP[ks * 8 + t], e1 = S.koffP[ks * 8 + 4 + t];
+            uint32_t a[4];
+            a[0] = featPair(S, base0, bc0, e0);
+            a[1] = featPair(S, base1, bc1, e0);
+            a[2] = featPair(S, base0, bc0, e1);
+            a[3] = featPair(S, base1, bc1, e1);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const uint16_t* w = &S.w1[(nt * 8 + g) * SW1 + ks * 16 + 2 * t];
+                mma16816(acc[nt], a, ld32(w), ld32(w + 8));
+            }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+            const int o = nt * 8 + 2 * t;
+            if (r0 < NR1)
+                st32(&S.a1[r0 * SA + o], pack2(relu(acc[nt][0] + S.b1[o]), relu(acc[nt][1] + S.b1[o + 1])));
+            if (r1 < NR1)
+                st32(&S.a1[r1 * SA + o], pack2(relu(acc[nt][2] + S.b1[o]), relu(acc[nt][3] + S.b1[o + 1])));
+        }
+    }
+}
+
+// Layers 2 and 3 on output rows warp and warp+8.  z2: layer-2
+// pre-activations (accumulator fragments); out[m]: layer-3 outputs of rows
+// g and g+8 of output row warp+8m, channels 2t and 2t+1 (t < 2 valid).
+__device__ void conv23(const NetSmem& S, int warp, int lane, float z2[2][4][4], float out[2][4]) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+        const int oy = warp + 8 * m;
+        float acc[4][4] = {};
+#pragma unroll 1
+        for (int tap = 0; tap < 9; tap++) {
+            const int dy = tap / 3, dx = tap % 3;
+            const uint16_t* p0 = &S.a1[((oy + dy) * R1 + g + dx) * SA + 2 * t];
+            const uint16_t* p1 = p0 + 8 * SA;
+#pragma unroll
+            for (int kb = 0; kb < 2; kb++) {
+                uint32_t a[4];
+                a[0] = ld32(p0 + kb * 16);
+                a[1] = ld32(p1 + kb * 16);
+                a[2] = ld32(p0 + kb * 16 + 8);
+                a[3] = ld32(p1 + kb * 16 + 8);
+                const int kk = tap * 32 + kb * 16 + 2 * t;
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++) {
+                    const uint16_t* w = &S.w2[(nt * 8 + g) * SW2 + kk];
+                    mma16816(acc[nt], a, ld32(w), ld32(w + 8));
+                }
+            }
+        }
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+            const int o = nt * 8 + 2 * t;
+            z2[m][nt][0] = acc[nt][0] + S.b2[o];
+            z2[m][nt][1] = acc[nt][1] + S.b2[o + 1];
+            z2[m][nt][2] = acc[nt][2] + S.b2[o];
+            z2[m][nt][3] = acc[nt][3] + S.b2[o + 1];
+        }
+        float acc3[4] = {};
+#pragma unroll
+        for (int kb = 0; kb < 2; kb++) {
+            uint32_t a[4];
+            a[0] = pack2(relu(z2[m][2 * kb][0]), relu(z2[m][2 * kb][1]));
+            a[1] = pack2(relu(z2[m][2 * kb][2]), relu(z2[m][2 * kb][3]));
+            a[2] = pack2(relu(z2[m][2 * kb + 1][0]), relu(z2[m][2 * kb + 1][1]));
+            a[3] = pack2(relu(z2[m][2 * kb + 1][2]), relu(z2[m][2 * kb + 1][3]));
+            const uint16_t* w = &S.w3[g * SW3 + kb * 16 + 2 * t];
+            mma16816(acc3, a, ld32(w), ld32(w + 8));
+        }
+        const int c = 2 * t;  // b3 holds 8 entries, zero past the fourth
+        out[m][0] = acc3[0] + S.b3[c];
+        out[m][1] = acc3[1] + S.b3[c + 1];
+        out[m][2] = acc3[2] + S.b3[c];
+        out[m][3] = acc3[3] + S.b3[c + 1];
+    }
+}
+
+struct TileGeom {
+    int s, Y, X;  // sample and image coordinates of the tile's first output cell
+};
+__device__ __forceinline__ TileGeom tileGeom(const rift_closure_src& src, int tile) {
+    const int tx = (src.OW + OT - 1) / OT, ty = (src.OH + OT - 1) / OT;
+    TileGeom G;
+    G.s = tile / (tx * ty);
+    int r = tile % (tx * ty);
+    G.Y = src.oy0 + (r / tx) * OT;
+    G.X = src.ox0 + (r % tx) * OT;
+    return G;
+}
+__host__ __device__ __forceinline__ int tileCount(const rift_closure_src& src) {
+    return src.samples * ((src.OW + OT - 1) / OT) * ((src.OH + OT - 1) / OT);
+}
+
+// ------------------------------------------------------------------ forward
+// Raw net outputs of every output cell of src.
+__global__ void __launch_bounds__(NT, 2) k_forward(rift_closure_src src, const float* __restrict__ P,
+                                                   float* __restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NetSmem& S = *reinterpret_cast<NetSmem*>(smem_raw);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    stageNet(S, P);
+    const int ntile = tileCount(src);
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const TileGeom G = tileGeom(src, tile);
+        __syncthreads();
+        stageInput(S, src, G.s, G.Y - 3, G.X - 3);
+        __syncthreads();
+        conv1(S, warp, lane);
+        __syncthreads();
+        float z2[2][4][4], o[2][4];
+        conv23(S, warp, lane, z2, o);
+        if (t < 2) {
+#pragma unroll
+            for (int m = 0; m < 2; m++)
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    const int y = G.Y + warp + 8 * m - src.oy0, x = G.X + g + 8 * r - src.ox0;
+                    if (y >= src.OH || x >= src.OW) continue;
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int ch = 2 * t + e;
+                        out[(((size_t)G.s * COUT + ch) * src.OH + y) * src.OW + x] = o[m][2 * r + e];
+                    }
+                }
+        }
+    }
+}
+
+// ----------------------------------------------------------------- training
+struct TrainArgs {
+    rift_closure_src src;
+    const float* P;
+    const float* target;
+    const float* weight;
+    float lossScale;
+    float* grad;
+    double* loss;
+};
+
+__global__ void __launch_bounds__(NT, 1) k_train(TrainArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TrainSmem& T = *reinterpret_cast<TrainSmem*>(smem_raw);
+    NetSmem& S = T.n;
+    const rift_closure_src& src = A.src;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    stageNet(S, A.P);
+    for (int i = tid; i < K2 * SA; i += NT) {
+        int k = i / SA, o = i % SA;
+        T.w2t[i] = bf(o < C1 ? A.P[OFF_W2 + o * K2 + k] : 0.f);
+    }
+    for (int i = tid; i < 4 * C1; i += NT) T.w3f[i] = A.P[OFF_W3 + i];
+
+    // gradient accumulators held across tiles
+    float gW2[9][4] = {};   // layer-2 weight tiles (rows k, cols o), see w2Tile
+    float gW1[5][4] = {};   // layer-1 weight tiles, see w1Tile
+    float gW3 = 0.f, gB3 = 0.f, gB2 = 0.f, gB1 = 0.f;
+    double lossAcc = 0.0;
+
+    const int ntile = tileCount(src);
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const TileGeom G = tileGeom(src, tile);
+        __syncthreads();
+        stageInput(S, src, G.s, G.Y - 3, G.X - 3);
+        __syncthreads();
+        conv1(S, warp, lane);
+        __syncthreads();
+        float z2[2][4][4], o[2][4];
+        conv23(S, warp, lane, z2, o);
+
+        // loss and d loss / d out; layer-2 activations to shared memory
+#pragma unroll
+        for (int m = 0; m < 2; m++) {
+            const int oy = warp + 8 * m;
+#pragma unroll
+            for (int r = 0; r < 2; r++) {
+                const int ox = g + 8 * r, p = oy * OT + ox;
+                if (t < 2) {
+                    const int y = G.Y + oy - src.oy0, x = G.X + ox - src.ox0;
+                    const bool in = y < src.OH && x < src.OW;
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int ch = 2 * t + e;
+                        float d = 0.f;
+                        if (in) {
+                            size_t at = (((size_t)G.s * COUT + ch) * src.OH + y) * src.OW + x;
+                            float w = __ldg(A.weight + at);
+                            float diff = o[m][2 * r + e] - __ldg(A.target + at);
+                            lossAcc += (double)(w * diff * diff);
+                            d = 2.f * w * diff * A.lossScale;
+                        }
+                        T.dout[p * 4 + ch] = d;
+                    }
+                }
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++)
+                    st32(&T.a2[p * SA + nt * 8 + 2 * t],
+                         pack2(relu(z2[m][nt][2 * r]), relu(z2[m][nt][2 * r + 1])));
+            }
+        }
+        __syncthreads();
+        // layer 3: dW3, db3 (CUDA cores)
+        {
+            const int pr = tid & 127, half = tid >> 7, oc = pr >> 5, c = pr & 31;
+            float acc = 0.f;
+            for (int p = half * 128; p < half * 128 + 128; p++) acc += T.dout[p * 4 + oc] * fb(T.a2[p * SA + c]);
+            gW3 += acc;
+            if (tid < COUT) {
+                float b = 0.f;
+                for (int p = 0; p < OT * OT; p++) b += T.dout[p * 4 + tid];
+                gB3 += b;
+            }
+        }
+        __syncthreads();
+        // dZ2 = (W3^T dout) * relu'(z2), in place of a2
+        {
+            const int p = tid;
+            const float d0 = T.dout[p * 4], d1 = T.dout[p * 4 + 1], d2 = T.dout[p * 4 + 2],
+                        d3 = T.dout[p * 4 + 3];
+#pragma unroll 8
+            for (int c = 0; c < C1; c++) {
+                float a = fb(T.a2[p * SA + c]);
+                float v = d0 * T.w3f[c] + d1 * T.w3f[C1 + c] + d2 * T.w3f[2 * C1 + c] + d3 * T.w3f[3 * C1 + c];
+                T.a2[p * SA + c] = bf(a > 0.f ? v : 0.f);
+            }
+        }
+        __syncthreads();
+        {
+            const int c = tid & 31, part = tid >> 5;
+            float b = 0.f;
+            for (int p = part; p < OT * OT; p += 8) b += fb(T.a2[p * SA + c]);
+            gB2 += b;
+        }
+        // dW2[k][o] += sum_p a1[p + tap(k)][ch(k)] dZ2[p][o]: 18 x 4 MMA tiles,
+        // nine per warp (rows w and w+8 with every column tile, then one of
+        // the rows 16..17)
+#pragma unroll 1
+        for (int oyp = 0; oyp < OT; oyp++) {
+            uint32_t bfr[4][2];
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const uint16_t* d = &T.a2[(oyp * OT + 2 * t) * SA + nt * 8 + g];
+                bfr[nt][0] = pack16(d[0], d[SA]);
+                bfr[nt][1] = pack16(d[8 * SA], d[9 * SA]);
+            }
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const int mt = j < 2 ? warp + 8 * j : 16 + (warp >> 2);
+                const int tap = mt >> 1, ch = (mt & 1) * 16 + g, dy = tap / 3, dx = tap % 3;
+                const uint16_t* r = &S.a1[((oyp + dy) * R1 + 2 * t + dx) * SA + ch];
+                uint32_t a[4];
+                a[0] = pack16(r[0], r[SA]);
+                a[1] = pack16(r[8], r[SA + 8]);
+                a[2] = pack16(r[8 * SA], r[9 * SA]);
+                a[3] = pack16(r[8 * SA + 8], r[9 * SA + 8]);
+                if (j < 2) {
+#pragma unroll
+                    for (int nt = 0; nt < 4; nt++) mma16816(gW2[4 * j + nt], a, bfr[nt][0], bfr[nt][1]);
+                } else {
+                    const int nt = warp & 3;
+                    mma16816(gW2[8], a, bfr[nt][0], bfr[nt][1]);
+                }
+            }
+        }
+        __syncthreads();
+        // dA1[q][c] = sum_{tap,o} dZ2[q - tap][o] W2[o][tap*32 + c]; dZ1 = dA1 * relu'(z1),
+        // written over a1 (each element read and written by the same thread)
+        for (int mt = warp; mt < M1T; mt += NT / 32) {
+            const int q0 = mt * 16 + g, q1 = q0 + 8;
+            const int qy0 = q0 / R1, qx0 = q0 % R1, qy1 = q1 / R1, qx1 = q1 % R1;
+            float acc[4][4] = {};
+#pragma unroll 1
+            for (int tap = 0; tap < 9; tap++) {
+                const int dy = tap / 3, dx = tap % 3;
+                const int py0 = qy0 - dy, px0 = qx0 - dx, py1 = qy1 - dy, px1 = qx1 - dx;
+                const bool v0 = q0 < NR1 && py0 >= 0 && py0 < OT && px0 >= 0 && px0 < OT;
+                const bool v1 = q1 < NR1 && py1 >= 0 && py1 < OT && px1 >= 0 && px1 < OT;
+                const uint16_t* d0 = &T.a2[(v0 ? py0 * OT + px0 : 0) * SA + 2 * t];
+                const uint16_t* d1 = &T.a2[(v1 ? py1 * OT + px1 : 0) * SA + 2 * t];
+#pragma unroll
+                for (int ob = 0; ob < 2; ob++) {
+                    uint32_t a[4];
+                    a[0] = v0 ? ld32(d0 + ob * 16) : 0u;
+                    a[1] = v1 ? ld32(d1 + ob * 16) : 0u;
+                    a[2] = v0 ? ld32(d0 + ob * 16 + 8) : 0u;
+                    a[3] = v1 ? ld32(d1 + ob * 16 + 8) : 0u;
+#pragma unroll
+                    for (int nt = 0; nt < 4; nt++) {
+                        const uint16_t* w = &T.w2t[(tap * 32 + nt * 8 + g) * SA + ob * 16 + 2 * t];
+                        mma16816(acc[nt], a, ld32(w), ld32(w + 8));
+                    }
+                }
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const int c = nt * 8 + 2 * t;
+                if (q0 < NR1) {
+                    uint16_t* z = &S.a1[q0 * SA + c];
+                    st32(z, pack2(fb(z[0]) > 0.f ? acc[nt][0] : 0.f, fb(z[1]) > 0.f ? acc[nt][1] : 0.f));
+                }
+                if (q1 < NR1) {
+                    uint16_t* z = &S.a1[q1 * SA + c];
+                    st32(z, pack2(fb(z[0]) > 0.f ? acc[nt][2] : 0.f, fb(z[1]) > 0.f ? acc[nt][3] : 0.f));
+                }
+            }
+        }
+        __syncthreads();
+        {
+            const int c = tid & 31, part = tid >> 5;
+            float b = 0.f;
+            for (int q = part; q < NR1; q += 8) b += fb(S.a1[q * SA + c]);
+            gB1 += b;
+        }
+        // dW1[k][o] += sum_q x(q, k) dZ1[q][o]: 10 x 4 MMA tiles, five per warp
+        {
+            const int mtA = warp, mtB = 8 + (warp >> 2), ntB = warp & 3;
+            const int eA0 = S.koffE[mtA * 16 + g], eA1 = S.koffE[mtA * 16 + g + 8];
+            const int eB0 = S.koffE[mtB * 16 + g], eB1 = S.koffE[mtB * 16 + g + 8];
+#pragma unroll 1
+            for (int ks = 0; ks < M1T; ks++) {
+                int bs[4];
+                float bc[4];
+                uint16_t dz[4][4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const int q = ks * 16 + 2 * t + (u & 1) + 8 * (u >> 1);
+                    bs[u] = winBase(min(q, NR1 - 1));
+                    bc[u] = winBed(S, bs[u]);
+#pragma unroll
+                    for (int nt = 0; nt < 4; nt++) dz[u][nt] = q < NR1 ? S.a1[q * SA + nt * 8 + g] : (uint16_t)0;
+                }
+                uint32_t a[4];
+                a[0] = pack2(featElem(S, bs[0], bc[0], eA0), featElem(S, bs[1], bc[1], eA0));
+                a[1] = pack2(featElem(S, bs[0], bc[0], eA1), featElem(S, bs[1], bc[1], eA1));
+                a[2] = pack2(featElem(S, bs[2], bc[2], eA0), featElem(S, bs[3], bc[3], eA0));
+                a[3] = pack2(featElem(S, bs[2], bc[2], eA1), featElem(S, bs[3], bc[3], eA1));
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++)
+                    mma16816(gW1[nt], a, pack16(dz[0][nt], dz[1][nt]), pack16(dz[2][nt], dz[3][nt]));
+                a[0] = pack2(featElem(S, bs[0], bc[0], eB0), featElem(S, bs[1], bc[1], eB0));
+                a[1] = pack2(featElem(S, bs[0], bc[0], eB1), featElem(S, bs[1], bc[1], eB1));
+                a[2] = pack2(featElem(S, bs[2], bc[2], eB0), featElem(S, bs[3], bc[3], eB0));
+                a[3] = pack2(featElem(S, bs[2], bc[2], eB1), featElem(S, bs[3], bc[3], eB1));
+                mma16816(gW1[4], a, pack16(dz[0][ntB], dz[1][ntB]), pack16(dz[2][ntB], dz[3][ntB]));
+            }
+        }
+    }
+
+    // one addition per CTA of every gradient it holds
+#pragma unroll
+    for (int j = 0; j < 9; j++) {
+        const int mt = j < 8 ? warp + 8 * (j >> 2) : 16 + (warp >> 2);
+        const int nt = j < 8 ? (j & 3) : (warp & 3);
+        const int k0 = mt * 16 + g, o0 = nt * 8 + 2 * t;
+        atomicAdd(&A.grad[OFF_W2 + o0 * K2 + k0], gW2[j][0]);
+        atomicAdd(&A.grad[OFF_W2 + (o0 + 1) * K2 + k0], gW2[j][1]);
+        atomicAdd(&A.grad[OFF_W2 + o0 * K2 + k0 + 8], gW2[j][2]);
+        atomicAdd(&A.grad[OFF_W2 + (o0 + 1) * K2 + k0 + 8], gW2[j][3]);
+    }
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+        const int mt = j < 4 ? warp : 8 + (warp >> 2);
+        const int nt = j < 4 ? j : (warp & 3);
+        const int k0 = mt * 16 + g, o0 = nt * 8 + 2 * t;
+        if (k0 < K1) {
+            atomicAdd(&A.grad[OFF_W1 + o0 * K1P + k0], gW1[j][0]);
+            atomicAdd(&A.grad[OFF_W1 + (o0 + 1) * K1P + k0], gW1[j][1]);
+        }
+        if (k0 + 8 < K1) {
+            atomicAdd(&A.grad[OFF_W1 + o0 * K1P + k0 + 8], gW1[j][2]);
+            atomicAdd(&A.grad[OFF_W1 + (o0 + 1) * K1P + k0 + 8], gW1[j][3]);
+        }
+    }
+    atomicAdd(&A.grad[OFF_W3 + (tid & 127)], gW3);
+    if (tid < COUT) atomicAdd(&A.grad[OFF_B3 + tid], gB3);
+    atomicAdd(&A.grad[OFF_B2 + (tid & 31)], gB2);
+    atomicAdd(&A.grad[OFF_B1 + (tid & 31)], gB1);
+    // loss: warp sums, then one atomic per CTA
+    for (int s = 16; s > 0; s >>= 1) lossAcc += __shfl_xor_sync(0xffffffffu, lossAcc, s);
+    if (lane == 0) T.red[warp] = lossAcc;
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < NT / 32; w++) s += T.red[w];
+        atomicAdd(A.loss, s * (double)A.lossScale);
+    }
+}
+
+// --------------------------------------------------------------------- Adam
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ gr, float* __restrict__ m,
+                       float* __restrict__ v, int n, float lr, float b1, float b2, float eps,
+                       float bias1, float bias2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float gi = gr[i];
+        float mi = b1 * m[i] + (1.f - b1) * gi;
+        float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / bias1) / (sqrtf(vi / bias2) + eps);
+        gr[i] = 0.f;
+    }
+}
+
+// ------------------------------------------------------------ face fluxes
+// Central-upwind flux through the east (DIR 0) or north (DIR 1) face of
+// cell (j, i) of a handle's U^n, built as the step builds it: the
+// reconstruction of both cells (construct) and the face flux (faceFlux).
+template <int DIR>
+__device__ __forceinline__ void faceFluxAt(const rift_device_view& V, int j, int i, float f[3]) {
+    const size_t pitch = (size_t)V.pitch, pl = (size_t)V.rows * pitch;
+    const int sj = DIR ? 1 : 0, si = DIR ? 0 : 1;
+    auto at = [&](const float* P, int jj, int ii) { return __ldg(P + (size_t)jj * pitch + ii); };
+    const float* eM = V.e + (DIR ? 2 : 0) * pl;  // eW / eS
+    const float* eP = V.e + (DIR ? 3 : 1) * pl;  // eE / eN
+    float hh[4], uu[4], vv[4], em[4], ep[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {  // cells -1 .. +2 along DIR
+        const int jj = j + (k - 1) * sj, ii = i + (k - 1) * si;
+        hh[k] = at(V.h, jj, ii);
+        uu[k] = at(V.hu, jj, ii);
+        vv[k] = at(V.hv, jj, ii);
+        em[k] = at(eM, jj, ii);
+        ep[k] = at(eP, jj, ii);
+    }
+    const float kappa = (float)V.kappa;
+    rift::Rec L = rift::construct(hh[1], uu[1], vv[1], hh[2], uu[2], vv[2], hh[0], uu[0], vv[0], em[1],
+                                  ep[1], ep[1] - em[2], ep[0] - em[1]);
+    rift::Rec R = rift::construct(hh[2], uu[2], vv[2], hh[3], uu[3], vv[3], hh[1], uu[1], vv[1], em[2],
+                                  ep[2], ep[2] - em[3], ep[1] - em[2]);
+    rift::faceFlux<DIR>(L.hP, L.uP, L.vP, R.hM, R.uM, R.vM, kappa, f);
+}
+
+__global__ void k_faceflux(rift_device_view V, int ratio, float w, float* __restrict__ acc,
+                           int apitch, int arows, int anx, int any) {
+    const int I = 2 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = 2 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (I > anx - 3 || J > any - 3) return;
+    const size_t pl = (size_t)arows * apitch, c = (size_t)J * apitch + I;
+    float fe[3], fn[3];
+    float e0, e1, n0, n2;
+    if (ratio == 1) {
+        faceFluxAt<0>(V, J, I, fe);
+        faceFluxAt<1>(V, J, I, fn);
+        e0 = fe[0], e1 = fe[1], n0 = fn[0], n2 = fn[2];
+    } else {
+        const int jf = 2 * (J - 2) + 2, jf2 = jf + 1, i0 = 2 * (I - 2) + 2;
+        float fa[3], fb2[3];
+        faceFluxAt<0>(V, jf, i0 + 1, fa);
+        faceFluxAt<0>(V, jf2, i0 + 1, fb2);
+        e0 = 0.5f * (fa[0] + fb2[0]);
+        e1 = 0.5f * (fa[1] + fb2[1]);
+        faceFluxAt<1>(V, jf2, i0, fa);
+        faceFluxAt<1>(V, jf2, i0 + 1, fb2);
+        n0 = 0.5f * (fa[0] + fb2[0]);
+        n2 = 0.5f * (fa[2] + fb2[2]);
+    }
+    acc[c] += w * e0;
+    acc[pl + c] += w * e1;
+    acc[2 * pl + c] += w * n0;
+    acc[3 * pl + c] += w * n2;
+}
+
+// ----------------------------------------------------------- closure step
+struct ApplyArgs {
+    rift_closure_src src;
+    const float* P;
+    float osc[4];
+    float* corr;
+    size_t plane;
+    int pitch, nx, ny;
+    float dtw, inv_dx, inv_dy, hmin, lim, tau;
+    int* counters;
+};
+
+// Net outputs -> gated, limited face corrections of every 16 x 16 block of
+// interior cells (zeros for dry blocks and blocks that fall back).
+__global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NetSmem& S = *reinterpret_cast<NetSmem*>(smem_raw);
+    const rift_closure_src& src = A.src;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    stageNet(S, A.P);
+    const float hminS = A.hmin * src.scale[0], invS0 = 1.f / src.scale[0];
+    const int ntile = tileCount(src);
+    for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+        const TileGeom G = tileGeom(src, tile);
+        __syncthreads();
+        if (tid == 0) S.red[0] = 0;
+        stageInput(S, src, 0, G.Y - 3, G.X - 3);
+        __syncthreads();
+        int wet = 0;
+        for (int i = tid; i < (OT + 1) * (OT + 1); i += NT) {
+            int ry = 3 + i / (OT + 1), rx = 3 + i % (OT + 1);
+            wet |= S.xs[(ry * RI + rx) * CIN] > hminS;
+        }
+        if (!__syncthreads_or(wet)) {
+            for (int i = tid; i < OT * OT; i += NT) {
+                int y = G.Y + i / OT, x = G.X + i % OT;
+                if (y - src.oy0 >= src.OH || x - src.ox0 >= src.OW) continue;
+                size_t c = (size_t)y * A.pitch + x;
+#pragma unroll
+                for (int ch = 0; ch < 4; ch++) A.corr[ch * A.plane + c] = 0.f;
+            }
+            continue;
+        }
+        conv1(S, warp, lane);
+        __syncthreads();
+        float z2[2][4][4], o[2][4];
+        conv23(S, warp, lane, z2, o);
+        float cm[2][2] = {}, cq[2][2] = {}, ind = 0.f;
+        if (t < 2) {
+            const bool east = t == 0;
+            const float inv = east ? A.inv_dx : A.inv_dy;
+#pragma unroll
+            for (int m = 0; m < 2; m++)
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    const int oy = warp + 8 * m, ox = g + 8 * r;
+                    const int y = G.Y + oy, x = G.X + ox;
+                    const int yn = east ? y : y + 1, xn = east ? x + 1 : x;
+                    bool ok = x >= 3 && y >= 3 && xn <= A.nx - 4 && yn <= A.ny - 4;
+                    const float hc = S.xs[((oy + 3) * RI + ox + 3) * CIN] * invS0;
+                    const float hn = S.xs[((oy + 3 + (east ? 0 : 1)) * RI + ox + 3 + (east ? 1 : 0)) * CIN] * invS0;
+                    ok = ok && hc > A.hmin && hn > A.hmin;
+                    float vm = ok ? o[m][2 * r] * A.osc[2 * t] : 0.f;
+                    float vq = ok ? o[m][2 * r + 1] * A.osc[2 * t + 1] : 0.f;
+                    const float hd = vm > 0.f ? hc : hn;
+                    if (ok) {
+                        ind = fmaxf(ind, fabsf(vm) * A.dtw * inv / hd);
+                        const float cap = A.lim * hd / (A.dtw * inv);
+                        vm = fminf(fmaxf(vm, -cap), cap);
+                    }
+                    cm[m][r] = vm;
+                    cq[m][r] = vq;
+                }
+        }
+        for (int s = 16; s > 0; s >>= 1) ind = fmaxf(ind, __shfl_xor_sync(0xffffffffu, ind, s));
+        if (lane == 0) atomicMax(&S.red[0], __float_as_int(ind));
+        __syncthreads();
+        const bool fallback = __int_as_float(S.red[0]) > A.tau;
+        if (t < 2) {
+#pragma unroll
+            for (int m = 0; m < 2; m++)
+#pragma unroll
+                for (int r = 0; r < 2; r++) {
+                    const int y = G.Y + warp + 8 * m, x = G.X + g + 8 * r;
+                    if (y - src.oy0 >= src.OH || x - src.ox0 >= src.OW) continue;
+                    size_t c = (size_t)y * A.pitch + x;
+                    A.corr[(2 * t) * A.plane + c] = fallback ? 0.f : cm[m][r];
+                    A.corr[(2 * t + 1) * A.plane + c] = fallback ? 0.f : cq[m][r];
+                }
+        }
+        if (tid == 0) {
+            atomicAdd(&A.counters[0], 1);
+            if (fallback) atomicAdd(&A.counters[1], 1);
+        }
+    }
+}
+
+// U^n -= dtw x divergence of the face corrections (cells one inside the
+// ghost ring and beyond).
+__global__ void k_apply(float* __restrict__ h, float* __restrict__ hu, float* __restrict__ hv,
+                        const float* __restrict__ corr, size_t plane, int pitch, int nx, int ny,
+                        float sx, float sy) {
+    const int i = 3 + blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = 3 + blockIdx.y * blockDim.y + threadIdx.y;
+    if (i > nx - 4 || j > ny - 4) return;
+    const size_t c = (size_t)j * pitch + i;
+    const float mE = corr[c], mW = corr[c - 1], mN = corr[2 * plane + c], mS = corr[2 * plane + c - pitch];
+    const float uE = corr[plane + c], uW = corr[plane + c - 1];
+    const float vN = corr[3 * plane + c], vS = corr[3 * plane + c - pitch];
+    if (mE == 0.f && mW == 0.f && mN == 0.f && mS == 0.f && uE == 0.f && uW == 0.f && vN == 0.f &&
+        vS == 0.f)
+        return;
+    h[c] -= sx * (mE - mW) + sy * (mN - mS);
+    hu[c] -= sx * (uE - uW);
+    hv[c] -= sy * (vN - vS);
+}
+
+}  // namespace rc
+
+// ------------------------------------------------------------------- C ABI
+namespace {
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+int launched(const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(RIFT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    return RIFT_OK;
+}
+
+bool srcOk(const rift_closure_src* s) {
+    return s && s->samples >= 1 && s->H >= 1 && s->W >= 1 && s->pitch >= s->W && s->OH >= 1 &&
+           s->OW >= 1 && s->oy0 >= 0 && s->ox0 >= 0 && s->sample_stride >= 0 &&
+           (s->samples == 1 || s->sample_stride >= (int64_t)s->pitch * s->H);
+}
+
+// Resident CTAs of kernel k with `smem` bytes, over every SM, capped by the
+// tile count.
+int residentGrid(const void* k, size_t smem, int tiles, int* out) {
+    int dev = 0, sms = 0, occ = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return fail(RIFT_ERR_CUDA, "no device");
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return fail(RIFT_ERR_CUDA, cudaGetErrorString(e));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, rc::NT, smem);
+    if (e != cudaSuccess || occ < 1) return fail(RIFT_ERR_CUDA, "closure kernel does not fit an SM");
+    *out = tiles < sms * occ ? tiles : sms * occ;
+    return RIFT_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int rift_closure_forward(const rift_closure_src* src, const float* params, float* out, void* stream) {
+    if (!srcOk(src) || !params || !out) return fail(RIFT_ERR_ARG, "rift_closure_forward: bad argument");
+    const size_t smem = sizeof(rc::NetSmem);
+    const int tiles = rc::tileCount(*src);
+    int grid = 0, rc_;
+    if ((rc_ = residentGrid((const void*)rc::k_forward, smem, tiles, &grid))) return rc_;
+    rc::k_forward<<<grid, rc::NT, smem, (cudaStream_t)stream>>>(*src, params, out);
+    return launched("k_forward");
+}
+
+int rift_closure_train(const rift_closure_src* src, const float* params, const float* target,
+                       const float* weight, float loss_scale, float* grad, double* loss, void* stream) {
+    if (!srcOk(src) || !params || !target || !weight || !grad || !loss)
+        return fail(RIFT_ERR_ARG, "rift_closure_train: bad argument");
+    const size_t smem = sizeof(rc::TrainSmem);
+    const int tiles = rc::tileCount(*src);
+    int grid = 0, rc_;
+    if ((rc_ = residentGrid((const void*)rc::k_train, smem, tiles, &grid))) return rc_;
+    rc::TrainArgs A{*src, params, target, weight, loss_scale, grad, loss};
+    rc::k_train<<<grid, rc::NT, smem, (cudaStream_t)stream>>>(A);
+    return launched("k_train");
+}
+
+int rift_closure_adam(float* params, float* grad, float* m, float* v, int32_t n, float lr, float beta1,
+                      float beta2, float eps, float bias1, float bias2, void* stream) {
+    if (!params || !grad || !m || !v || n < 1 || !(bias1 > 0.f) || !(bias2 > 0.f))
+        return fail(RIFT_ERR_ARG, "rift_closure_adam: bad argument");
+    const int blocks = (n + 255) / 256;
+    rc::k_adam<<<blocks, 256, 0, (cudaStream_t)stream>>>(params, grad, m, v, n, lr, beta1, beta2, eps,
+                                                         bias1, bias2);
+    return launched("k_adam");
+}
+
+int rift_closure_face_flux(const rift_device_view* view, int32_t ratio, float weight, float* acc,
+                           int32_t acc_pitch, int32_t acc_rows, int32_t acc_nx, int32_t acc_ny) {
+    if (!view || !acc || (ratio != 1 && ratio != 2) || acc_nx < 5 || acc_ny < 5 || acc_pitch < acc_nx ||
+        acc_rows < acc_ny)
+        return fail(RIFT_ERR_ARG, "rift_closure_face_flux: bad argument");
+    if (view->h_nx - 4 != ratio * (acc_nx - 4) || view->h_ny - 4 != ratio * (acc_ny - 4))
+        return fail(RIFT_ERR_ARG, "rift_closure_face_flux: grids do not match the ratio");
+    dim3 blk(32, 8), grd((acc_nx - 4 + 31) / 32, (acc_ny - 4 + 7) / 8);
+    rc::k_faceflux<<<grd, blk, 0, (cudaStream_t)view->stream>>>(*view, ratio, weight, acc, acc_pitch,
+                                                                 acc_rows, acc_nx, acc_ny);
+    return launched("k_faceflux");
+}
+
+int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src, const float* params,
+                       const float* oscale_host, float dtw, float hmin, float lim, float tau, float* corr,
+                       int32_t* counters) {
+    if (!view || !srcOk(src) || !params || !oscale_host || !corr || !counters || !(hmin > 0.f) ||
+        !(lim > 0.f) || !(src->scale[0] > 0.f) || src->samples != 1)
+        return fail(RIFT_ERR_ARG, "rift_closure_apply: bad argument");
+    if (src->H != view->h_ny || src->W != view->h_nx || src->pitch != view->pitch || src->oy0 != 2 ||
+        src->ox0 != 2 || src->OH != view->h_ny - 4 || src->OW != view->h_nx - 4)
+        return fail(RIFT_ERR_ARG, "rift_closure_apply: src is not the view's interior");
+    if (!(dtw > 0.f)) return RIFT_OK;
+    cudaStream_t st = (cudaStream_t)view->stream;
+    rc::ApplyArgs A{};
+    A.src = *src;
+    A.P = params;
+    for (int c = 0; c < 4; c++) A.osc[c] = oscale_host[c];
+    A.corr = corr;
+    A.plane = (size_t)view->rows * view->pitch;
+    A.pitch = view->pitch;
+    A.nx = view->h_nx;
+    A.ny = view->h_ny;
+    A.dtw = dtw;
+    A.inv_dx = (float)(1.0 / view->dx);
+    A.inv_dy = (float)(1.0 / view->dy);
+    A.hmin = hmin;
+    A.lim = lim;
+    A.tau = tau;
+    A.counters = counters;
+    const size_t smem = sizeof(rc::NetSmem);
+    const int tiles = rc::tileCount(*src);
+    int grid = 0, rc_;
+    if ((rc_ = residentGrid((const void*)rc::k_closure, smem, tiles, &grid))) return rc_;
+    rc::k_closure<<<grid, rc::NT, smem, st>>>(A);
+    if ((rc_ = launched("k_closure"))) return rc_;
+    dim3 blk(32, 8), grd((view->h_nx - 6 + 31) / 32, (view->h_ny - 6 + 7) / 8);
+    rc::k_apply<<<grd, blk, 0, st>>>(view->h, view->hu, view->hv, corr, A.plane, view->pitch, view->h_nx,
+                                     view->h_ny, (float)(dtw / view->dx), (float)(dtw / view->dy));
+    return launched("k_apply");
+}
+
+const char* rift_closure_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"

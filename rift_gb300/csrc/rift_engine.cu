@@ -1040,6 +1040,28 @@ int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY) {
     return RIFT_OK;
 }
 
+int rift_get_device_view(rift_handle* h, rift_device_view* v) {
+    if (!h || !v) return RIFT_ERR_ARG;
+    if (!h->haveStatic) return fail(h, RIFT_ERR_STATE, "upload the static fields first");
+    const size_t pl = h->plane();
+    v->h = h->A;
+    v->hu = h->A + pl;
+    v->hv = h->A + 2 * pl;
+    v->e = h->E;
+    v->n = h->nman;
+    v->t = &h->st->t;
+    v->dt = &h->st->dt;
+    v->stream = (void*)h->stream;
+    v->h_nx = h->nx;
+    v->h_ny = h->ny;
+    v->pitch = h->pitch;
+    v->rows = h->rows;
+    v->dx = h->g.dx;
+    v->dy = h->g.dy;
+    v->kappa = h->g.kappa;
+    return RIFT_OK;
+}
+
 int rift_get_field(rift_handle* h, int32_t which, double* host, size_t ld) {
     if (!h || !host || ld < (size_t)h->nx) return RIFT_ERR_ARG;
     const int nx = h->nx, ny = h->ny;

@@ -39,3 +39,24 @@ def test_product_has_no_cpu_fallback():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".hpp", ".cpp")):
                 txt = open(os.path.join(dirpath, f)).read()
                 assert "rift_oracle" not in txt, f
+
+
+def test_closure_library_exports_every_declared_symbol():
+    eb.build()
+    lib = ctypes.CDLL(eb.CLOSURE_LIB)
+    names = declared_symbols("rift_closure.h")
+    assert len(names) >= 6
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_closure_struct_layouts_match_the_header():
+    """The ctypes mirrors of rift_closure_src and rift_device_view have the
+    C layout (offsets of the last members, total sizes)."""
+    from rift_gb300 import capi, closure
+
+    assert ctypes.sizeof(closure.Src) == 136
+    assert closure.Src.samples.offset == 132
+    assert closure.Src.sample_stride.offset == 96
+    assert ctypes.sizeof(capi.DeviceView) == 104
+    assert capi.DeviceView.kappa.offset == 96

@@ -1,0 +1,334 @@
+"""Learned flux closure kernels on the GPU, each against an FP32 statement of
+the same arithmetic: the net's forward pass and its parameter gradient
+against PyTorch autograd (BF16 tensor-core operands, so the tolerances are
+BF16-sized), Adam against its formula, the face-flux kernel against a numpy
+FP32 restatement of the step's reconstruction and central-upwind flux, and
+the closure step's volume conservation."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from rift_gb300 import build as eb
+from rift_gb300 import capi, closure, synth
+
+pytestmark = pytest.mark.gpu
+
+# BF16 operands (8-bit mantissa) in every contraction, FP32 accumulation
+FWD_TOL = 3e-2      # max |out - ref| / max |ref|
+GRAD_TOL = 6e-2     # |g - g_ref| / |g_ref| per parameter block
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch
+    eb.build()
+    closure.load()
+    return torch
+
+
+def _patches(rng, S=3, H=70):
+    x = np.zeros((S, 6, H, H), np.float32)
+    x[:, 0] = np.abs(rng.normal(0.3, 0.3, (S, H, H)))
+    x[:, 1] = rng.normal(0, 0.2, (S, H, H))
+    x[:, 2] = rng.normal(0, 0.2, (S, H, H))
+    yy, xx = np.mgrid[0:H, 0:H]
+    for s in range(S):
+        x[s, 3] = 30.0 + 0.05 * xx - 0.03 * yy + rng.normal(0, 0.2, (H, H))
+    x[:, 4] = rng.uniform(0.02, 0.08, (S, H, H))
+    x[:, 5] = 1.4e-5
+    return x
+
+
+SCALE = np.array([2.0, 3.0, 3.0, 1.0, 20.0, closure.RAIN_SCALE], np.float32)
+
+
+def _params(rng):
+    p = closure.init_params(3)
+    p[closure.OFF_B1:closure.OFF_W2] = rng.normal(0, 0.1, 32)
+    p[closure.OFF_B2:closure.OFF_W3] = rng.normal(0, 0.1, 32)
+    w3 = p[closure.OFF_W3:closure.OFF_B3].reshape(8, 32)
+    w3[:4] *= 10.0
+    p[closure.OFF_B3:closure.OFF_B3 + 4] = rng.normal(0, 0.1, 4)
+    return p
+
+
+def test_forward_matches_torch(torch):
+    rng = np.random.default_rng(0)
+    x = torch.as_tensor(_patches(rng), device="cuda")
+    p = torch.as_tensor(_params(rng), device="cuda")
+    out = closure.forward(x, p, SCALE)
+    torch.cuda.synchronize()
+    xs = x * torch.as_tensor(SCALE, device="cuda").view(1, 6, 1, 1)
+    ref = closure.torch_forward(xs, p)
+    assert out.shape == ref.shape == (3, 4, 64, 64)
+    err = (out - ref).abs().max().item() / ref.abs().max().item()
+    assert err < FWD_TOL, err
+
+
+def test_forward_partial_blocks_and_clamped_edges(torch):
+    """Output extents that are not multiples of 16 (the last block partial,
+    its input reads clamped to the patch): every output cell matches torch."""
+    rng = np.random.default_rng(1)
+    H = 45  # 39 output cells per side: three blocks, the last one partial
+    x = torch.as_tensor(_patches(rng, S=2, H=H), device="cuda")
+    p = torch.as_tensor(_params(rng), device="cuda")
+    out = closure.forward(x, p, SCALE)
+    xs = x * torch.as_tensor(SCALE, device="cuda").view(1, 6, 1, 1)
+    ref = closure.torch_forward(xs, p)
+    assert out.shape == ref.shape == (2, 4, 39, 39)
+    err = (out - ref).abs().max().item() / ref.abs().max().item()
+    assert err < FWD_TOL, err
+
+
+def test_gradient_matches_autograd(torch):
+    rng = np.random.default_rng(2)
+    x = torch.as_tensor(_patches(rng, S=4), device="cuda")
+    pn = _params(rng)
+    p = torch.as_tensor(pn, device="cuda")
+    tgt = torch.as_tensor(rng.normal(0, 1, (4, 4, 64, 64)).astype(np.float32), device="cuda")
+    w = torch.as_tensor((rng.uniform(0, 1, (4, 4, 64, 64)) > 0.3).astype(np.float32), device="cuda")
+    ls = 1.0 / (4 * 64 * 64)
+    grad = torch.zeros(closure.NPARAM, device="cuda")
+    loss = torch.zeros(1, device="cuda", dtype=torch.float64)
+    closure.train_pass(x, p, SCALE, tgt, w, ls, grad, loss)
+    torch.cuda.synchronize()
+    pr = p.clone().requires_grad_(True)
+    xs = x * torch.as_tensor(SCALE, device="cuda").view(1, 6, 1, 1)
+    ref = closure.torch_forward(xs, pr)
+    lref = ls * (w * (ref - tgt) ** 2).sum()
+    lref.backward()
+    g = pr.grad
+    assert abs(loss.item() - lref.item()) / lref.item() < FWD_TOL
+    blocks = {"W1": (closure.OFF_W1, closure.OFF_B1), "b1": (closure.OFF_B1, closure.OFF_W2),
+              "W2": (closure.OFF_W2, closure.OFF_B2), "b2": (closure.OFF_B2, closure.OFF_W3),
+              "W3": (closure.OFF_W3, closure.OFF_W3 + 128), "b3": (closure.OFF_B3, closure.OFF_B3 + 4)}
+    for name, (a, b) in blocks.items():
+        gk, gr = grad[a:b], g[a:b]
+        rel = (gk - gr).norm().item() / gr.norm().item()
+        assert rel < GRAD_TOL, (name, rel)
+    # padding columns of W1 and rows 4..7 of W3 get no gradient
+    assert grad[closure.OFF_W1:closure.OFF_B1].view(32, 160)[:, 150:].abs().max().item() == 0.0
+    assert grad[closure.OFF_W3 + 128:closure.OFF_B3].abs().max().item() == 0.0
+
+
+def test_adam_matches_formula(torch):
+    rng = np.random.default_rng(3)
+    n = 1000
+    p0 = rng.normal(0, 1, n).astype(np.float32)
+    g0 = rng.normal(0, 1, n).astype(np.float32)
+    p, g = torch.as_tensor(p0, device="cuda"), torch.as_tensor(g0, device="cuda")
+    m, v = torch.zeros_like(p), torch.zeros_like(p)
+    closure.adam(p, g, m, v, 1, 1e-2)
+    torch.cuda.synchronize()
+    mm = 0.1 * g0
+    vv = 0.001 * g0 * g0
+    ref = p0 - 1e-2 * (mm / 0.1) / (np.sqrt(vv / 0.001) + 1e-8)
+    np.testing.assert_allclose(p.cpu().numpy(), ref, rtol=1e-5, atol=1e-6)
+    assert g.abs().max().item() == 0.0
+
+
+# ------------------------------------------------------------- face fluxes
+def _cudart():
+    for name in ("libcudart.so", "libcudart.so.13", "libcudart.so.12"):
+        try:
+            lib = ctypes.CDLL(name)
+            lib.cudaMemcpy.restype = ctypes.c_int
+            lib.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
+            return lib
+        except OSError:
+            continue
+    pytest.skip("no CUDA runtime library to read device planes")
+
+
+def _plane(view, ptr, k=0):
+    out = np.zeros((view.rows, view.pitch), np.float32)
+    src = ptr + k * view.rows * view.pitch * 4
+    assert _cudart().cudaMemcpy(out.ctypes.data, src, out.nbytes, 2) == 0
+    return out
+
+
+def _np_flux(h, u, v, eM, eP, j, i, axis, kappa):
+    """FP32 numpy statement of the step's reconstruction + face flux through
+    the + face of cell (j, i) along axis (1: x, 0: y)."""
+    f32 = np.float32
+    G = f32(9.80665)
+
+    def cell(k):
+        jj, ii = (j, i + k) if axis == 1 else (j + k, i)
+        return h[jj, ii], u[jj, ii], v[jj, ii], eM[jj, ii], eP[jj, ii]
+
+    def slope(dp, dm):
+        a = f32(1.3) * abs(dp)
+        b = f32(0.5) * abs(f32(dp + dm))
+        c = f32(1.3) * abs(dm)
+        return f32(0.5) * min(min(a, b), c)
+
+    def rec(k):
+        h0, u0, v0, em, ep = cell(k)
+        hp, up, vp, emp, _ = cell(k + 1)
+        hm, um, vm, _, epm = cell(k - 1)
+        sw = slope(f32(f32(ep - emp) + f32(hp - h0)), f32(f32(epm - em) + f32(h0 - hm)))
+        su = slope(f32(up - u0), f32(u0 - um))
+        sv = slope(f32(vp - v0), f32(v0 - vm))
+        hP = f32(f32(h0 + sw) - ep)
+        hM = f32(f32(h0 - sw) - em)
+        hb = f32(f32(h0 + h0) - f32(ep + em))
+        if hP < 0:
+            hP, hM = f32(0), hb
+        if hM < 0:
+            hP, hM = hb, f32(0)
+        return (hP, f32(u0 + su), f32(v0 + sv)), (hM, f32(u0 - su), f32(v0 - sv))
+
+    L, _ = rec(0)
+    _, R = rec(1)
+
+    def side(hh, qu, qv):
+        h2 = f32(hh * hh)
+        r = f32(f32(2) * hh) / f32(h2 + max(h2, f32(kappa)))
+        uu, vv = f32(qu * r), f32(qv * r)
+        return hh, uu, vv, f32(hh * uu), f32(hh * vv), f32(np.sqrt(f32(G * hh)))
+
+    hL, uL, vL, quL, qvL, cL = side(*L)
+    hR, uR, vR, quR, qvR, cR = side(*R)
+    nL, nR = (uL, uR) if axis == 1 else (vL, vR)
+    ap = max(max(f32(nL + cL), f32(nR + cR)), f32(0))
+    am = min(min(f32(nL - cL), f32(nR - cR)), f32(0))
+    pL, pR = f32(f32(0.5) * G * hL * hL), f32(f32(0.5) * G * hR * hR)
+    if axis == 1:
+        FL = [quL, f32(quL * uL + pL), f32(quL * vL)]
+        FR = [quR, f32(quR * uR + pR), f32(quR * vR)]
+    else:
+        FL = [qvL, f32(qvL * uL), f32(qvL * vL + pL)]
+        FR = [qvR, f32(qvR * uR), f32(qvR * vR + pR)]
+    if not hL > 0:
+        FL = [f32(0)] * 3
+    if not hR > 0:
+        FR = [f32(0)] * 3
+    d = f32(ap - am)
+    if not d > 0:
+        return [0.0, 0.0, 0.0]
+    k = f32(ap * am / d)
+    qs = [(hR, hL), (quR, quL), (qvR, qvL)]
+    return [float(f32((ap * FL[c] - am * FR[c]) / d) + k * f32(qs[c][0] - qs[c][1])) for c in range(3)]
+
+
+@pytest.fixture(scope="module")
+def wet_small(torch):
+    case = synth.small_case(nx_cells=40, ny_cells=36, seed=5, cell=10.0, rain_mmhr=400.0, rim=True)
+    sim = capi.Sim(case).setup()
+    sim.run(400)
+    return sim
+
+
+def test_face_flux_matches_numpy_statement(torch, wet_small):
+    sim = wet_small
+    v = sim.device_view()
+    acc = torch.zeros((4, v.rows, v.pitch), device="cuda")
+    torch.cuda.synchronize()
+    closure.face_flux(v, 1, 1.0, acc, v.h_nx, v.h_ny)
+    torch.cuda.synchronize()
+    a = acc.cpu().numpy()
+    h, u, w = _plane(v, v.h), _plane(v, v.hu), _plane(v, v.hv)
+    eW, eE, eS, eN = (_plane(v, v.e, k) for k in range(4))
+    rng = np.random.default_rng(4)
+    wet = np.argwhere(h[3:v.h_ny - 3, 3:v.h_nx - 3] > 0.01) + 3
+    assert len(wet) > 50
+    pick = wet[rng.choice(len(wet), 40, replace=False)]
+    worst = 0.0
+    for j, i in pick:
+        fx = _np_flux(h, u, w, eW, eE, j, i, 1, v.kappa)
+        fy = _np_flux(h, u, w, eS, eN, j, i, 0, v.kappa)
+        ref = [fx[0], fx[1], fy[0], fy[2]]
+        got = a[:, j, i]
+        for c in range(4):
+            worst = max(worst, abs(got[c] - ref[c]) / (abs(ref[c]) + 1e-4))
+    assert worst < 1e-4, worst
+
+
+def test_face_flux_ratio2_is_the_mean_of_fine_faces(torch, wet_small):
+    sim = wet_small
+    v = sim.device_view()
+    ncx, ncy = (v.h_nx - 4) // 2 + 4, (v.h_ny - 4) // 2 + 4
+    fine = torch.zeros((4, v.rows, v.pitch), device="cuda")
+    coarse = torch.zeros((4, ncy + 2, ncx + 2), device="cuda")
+    torch.cuda.synchronize()
+    closure.face_flux(v, 1, 1.0, fine, v.h_nx, v.h_ny)
+    closure.face_flux(v, 2, 1.0, coarse, ncx, ncy)
+    torch.cuda.synchronize()
+    f, c = fine.cpu().numpy(), coarse.cpu().numpy()
+    J, I = np.mgrid[2:ncy - 2, 2:ncx - 2]
+    jf, i0 = 2 * (J - 2) + 2, 2 * (I - 2) + 2
+    east = 0.5 * (f[0][jf, i0 + 1] + f[0][jf + 1, i0 + 1])
+    north = 0.5 * (f[2][jf + 1, i0] + f[2][jf + 1, i0 + 1])
+    np.testing.assert_allclose(c[0][2:ncy - 2, 2:ncx - 2], east, rtol=1e-5, atol=1e-7)
+    np.testing.assert_allclose(c[2][2:ncy - 2, 2:ncx - 2], north, rtol=1e-5, atol=1e-7)
+
+
+def test_face_flux_rejects_mismatched_grids(torch, wet_small):
+    v = wet_small.device_view()
+    acc = torch.zeros((4, v.rows, v.pitch), device="cuda")
+    with pytest.raises(capi.RiftError):
+        closure.face_flux(v, 2, 1.0, acc, v.h_nx, v.h_ny)
+
+
+# ------------------------------------------------------------ closure step
+def test_closure_step_conserves_volume(torch):
+    """Corrections move volume between cells only: the total changes by
+    rounding, no cell goes negative, dry cells stay untouched."""
+    case = synth.small_case(nx_cells=64, ny_cells=64, seed=9, cell=4.0, rain_mmhr=600.0, rim=True)
+    sim = capi.Sim(case).setup()
+    sim.run(300)
+    rng = np.random.default_rng(5)
+    p = _params(rng)
+    model = closure.Model(p, SCALE, np.array([2e-3, 2e-3, 2e-3, 2e-3], np.float32))
+    run = closure.ClosureRun(sim, model, hmin=0.01, lim=0.2, tau=1e9)
+    h0 = sim.field("W") - sim.field("BC")
+    v0 = sim.volume()
+    run.apply(2.0, sim.time()[0])
+    torch.cuda.synchronize()
+    h1 = sim.field("W") - sim.field("BC")
+    v1 = sim.volume()
+    ev, fb = run.block_counts()
+    assert ev >= 1 and fb == 0
+    changed = np.abs(h1 - h0)[2:-2, 2:-2] > 0
+    assert changed.sum() > 10
+    assert abs(v1 - v0) <= 1e-6 * v0, (v0, v1)
+    inner = (slice(2, -2), slice(2, -2))
+    assert (h1[inner] >= 0).all()
+    dry = h0[inner] <= 0.01
+    assert np.array_equal(h1[inner][dry], h0[inner][dry])
+
+
+def test_closure_fallback_blocks_leave_the_state(torch):
+    """With tau = 0 every evaluated block falls back: the step changes nothing."""
+    case = synth.small_case(nx_cells=48, ny_cells=48, seed=9, cell=4.0, rain_mmhr=600.0, rim=True)
+    sim = capi.Sim(case).setup()
+    sim.run(300)
+    rng = np.random.default_rng(6)
+    model = closure.Model(_params(rng), SCALE, np.full(4, 2e-3, np.float32))
+    run = closure.ClosureRun(sim, model, tau=0.0)
+    w0 = sim.field("W")
+    run.apply(2.0, sim.time()[0])
+    ev, fb = run.block_counts()
+    assert ev >= 1 and fb >= 1
+    assert np.array_equal(sim.field("W"), w0)
+
+
+def test_generate_train_and_run_end_to_end(torch):
+    """Small-grid version of the whole closure workflow: training patches
+    from the solver, a few Adam steps that lower the loss, a coarse run with
+    the closure that stays finite and conserves the rain volume."""
+    ds = closure.generate([0, 1], N=256, cell=4.0, sample_times=(600.0, 1200.0), window=10.0,
+                          hmin=0.005, min_frac=0.02)
+    assert ds.feats.shape[1:] == (6, 70, 70) and ds.target.shape[1:] == (4, 64, 64)
+    assert len(ds.feats) >= 2 and np.isfinite(ds.target).all()
+    model, loss = closure.train(ds, steps=60, batch=16, lr=3e-3)
+    assert np.isfinite(loss).all() and loss[-10:].mean() < loss[:10].mean()
+    cc = closure.coarse_case(closure.scenario(6, N=256, cell=4.0, tf=900.0))  # rimmed: closed
+    sim = capi.Sim(cc).setup()
+    run = closure.ClosureRun(sim, model, every=4)
+    t = run.run(600.0)
+    assert t >= 600.0 and run.applies > 0
+    vol, added = sim.mass_ledger()
+    assert abs(vol - added) <= 1e-5 * added
