@@ -515,7 +515,7 @@ def run_closure(args):
     clocks = ClockSampler().start()
     evals = []
     for k in range(args.eval_seeds):
-        seed = 100_000 + k
+        seed = 100_001 + k  # scenario 100000 chose the correction gain
         fc = closure.scenario(seed, N=N, cell=2.0, tf=args.tf)
         cc = closure.coarse_case(fc)
         res = {"seed": seed, "generator": "config1" if seed % 2 == 0 else "config2"}
@@ -537,7 +537,7 @@ def run_closure(args):
             sim = capi.Sim(cc).setup()
             bc_of[id(sim)] = sim.field("BC")
             if mode == "closure":
-                cr = closure.ClosureRun(sim, model, every=args.closure_every)
+                cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain)
                 w, arr = _timed_chunks(cr.run, args.tf, 120.0, lambda: interior_depth(sim))
                 res["closure_blocks"], res["closure_fallback_blocks"] = cr.block_counts()
                 res["closure_applies"] = cr.applies
@@ -548,7 +548,7 @@ def run_closure(args):
             both = np.isfinite(arr) & np.isfinite(arr_f)
             res[mode] = {"wall_s": w,
                          "peak_depth_rmse_m": float(np.sqrt(np.mean((hmax - hmax_f)[wet] ** 2))),
-                         "arrival_mae_s": float(np.mean(np.abs(arr - arr_f)[both])) if both.any() else None,
+                         "arrival_mae_s": float(np.mean(np.abs(arr[both] - arr_f[both]))) if both.any() else None,
                          "arrival_missed_frac": float(np.mean(np.isinf(arr) & np.isfinite(arr_f)))}
             sim.close()
         res["fine_wall_s"] = w_f
@@ -562,7 +562,7 @@ def run_closure(args):
     # last coarse state, timed with CUDA events on the engine's stream
     sim = capi.Sim(cc).setup()
     sim.run(2 ** 31 - 1, min(args.tf, 1800.0))
-    cr = closure.ClosureRun(sim, model, every=args.closure_every)
+    cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain)
     st = torch.cuda.ExternalStream(cr.view.stream)
     cr.apply(1e-3, 1800.0)
     torch.cuda.synchronize()
@@ -589,6 +589,7 @@ def run_closure(args):
                        "tf_s": args.tf, "train_scenarios": args.closure_seeds,
                        "train_grid": f"{args.closure_train_N}^2 at 2 m", "train_patches": n_patches,
                        "train_steps": args.train_steps, "batch": 256, "closure_every_steps": args.closure_every,
+                       "closure_gain": args.closure_gain,
                        "eval_scenarios": args.eval_seeds},
             "peak_depth_rmse_m": {"closure": float(np.mean([r["closure"]["peak_depth_rmse_m"] for r in evals])),
                                   "plain_coarse": float(np.mean([r["plain"]["peak_depth_rmse_m"] for r in evals]))},
@@ -610,12 +611,14 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--config", type=int, default=2, choices=(1, 2, 3, 4, 5))
-    ap.add_argument("--closure-seeds", type=int, default=48, help="config 4: training scenarios")
+    ap.add_argument("--closure-seeds", type=int, default=32, help="config 4: training scenarios")
     ap.add_argument("--closure-train-N", type=int, default=1024, help="config 4: training grid side")
     ap.add_argument("--train-steps", type=int, default=1500, help="config 4: Adam steps")
     ap.add_argument("--eval-seeds", type=int, default=2, help="config 4: held-out scenarios")
     ap.add_argument("--closure-every", type=int, default=4,
                     help="config 4: coarse steps between closure applications")
+    ap.add_argument("--closure-gain", type=float, default=0.25,
+                    help="config 4: strength of the applied corrections (chosen on scenario 100000)")
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")
     ap.add_argument("--side-min", type=int, default=128, help="config 5: smallest side (cells)")
     ap.add_argument("--side-max", type=int, default=512, help="config 5: largest side (cells)")

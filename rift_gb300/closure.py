@@ -371,6 +371,23 @@ def output_scales(ds: Dataset) -> np.ndarray:
     return o
 
 
+def loss_on(ds: Dataset, model: Model, batch=256) -> float:
+    """Mean masked squared error of the scaled targets over a dataset (the
+    training loss, without an optimiser step)."""
+    torch = _torch()
+    P = torch.as_tensor(model.params, device="cuda")
+    G = torch.zeros_like(P)
+    loss = torch.zeros(1, device="cuda", dtype=torch.float64)
+    n = len(ds.feats)
+    for a in range(0, n, batch):
+        xb = torch.as_tensor(ds.feats[a:a + batch], device="cuda").contiguous()
+        tb = torch.as_tensor(ds.target[a:a + batch] / model.oscale.reshape(1, 4, 1, 1), device="cuda")
+        wb = torch.as_tensor(ds.mask[a:a + batch], device="cuda")
+        train_pass(xb, P, model.scale, tb.contiguous(), wb.contiguous(), 1.0 / (n * PATCH * PATCH), G, loss)
+    torch.cuda.synchronize()
+    return float(loss.item())
+
+
 def train(ds: Dataset, steps=1500, batch=256, lr=2e-3, seed=0, log=None, log_every=250):
     """Adam on the masked squared error of the scaled targets; returns the
     Model and the loss history (one value per step, FP64 from the device)."""
@@ -406,7 +423,7 @@ class ClosureRun:
     """A coarse handle stepped by the engine, with the closure applied every
     `every` steps over the time those steps covered."""
 
-    def __init__(self, sim: capi.Sim, model: Model, every=4, hmin=0.01, lim=0.2, tau=0.5):
+    def __init__(self, sim: capi.Sim, model: Model, every=4, hmin=0.01, lim=0.2, tau=0.5, gain=1.0):
         torch = _torch()
         self.sim, self.model = sim, model
         self.every, self.hmin, self.lim, self.tau = every, hmin, lim, tau
@@ -425,7 +442,10 @@ class ClosureRun:
         self.params = torch.as_tensor(model.params, device="cuda")
         self.corr = torch.zeros((4, rows, pitch), device="cuda", dtype=torch.float32)
         self.counters = torch.zeros(2, device="cuda", dtype=torch.int32)
-        self.osc = (C.c_float * 4)(*[float(x) for x in model.oscale])
+        # gain: strength of each correction (east mass, east x momentum,
+        # north mass, north y momentum), multiplying the output scales
+        g = np.broadcast_to(np.asarray(gain, dtype=np.float64), (4,))
+        self.osc = (C.c_float * 4)(*[float(x) for x in model.oscale * g])
         torch.cuda.synchronize()
         self.applies = 0
 

@@ -175,76 +175,108 @@ __device__ __forceinline__ float winBed(const NetSmem& S, int base) {
     return S.xs[base + (2 * RI + 2) * CIN + 3];
 }
 
-// Layer 1 on the 18 x 18 region: a1 = relu(W1 x + b1), BF16.
+// Layer 1 on the 18 x 18 region: a1 = relu(W1 x + b1), BF16.  A warp owns
+// row tiles warp, warp+8 and (warps 0..4) warp+16, and loads each weight
+// fragment once for all of them.
 __device__ void conv1(NetSmem& S, int warp, int lane) {
     const int g = lane >> 2, t = lane & 3;
-    for (int mt = warp; mt < M1T; mt += NT / 32) {
-        const int r0 = mt * 16 + g, r1 = r0 + 8;
-        const int q0 = min(r0, NR1 - 1), q1 = min(r1, NR1 - 1);
-        const int base0 = winBase(q0), base1 = winBase(q1);
-        const float bc0 = winBed(S, base0), bc1 = winBed(S, base1);
-        float acc[4][4] = {};
+    constexpr int MPW = (M1T + 7) / 8;  // 3
+    const bool third = warp + 16 < M1T;
+    int base[MPW][2];
+    float bc[MPW][2];
 #pragma unroll
-        for (int ks = 0; ks < K1P / 16; ks++) {
-            const int e0 = S.koffP[ks * 8 + t], e1 = S.koffP[ks * 8 + 4 + t];
-            uint32_t a[4];
-            a[0] = featPair(S, base0, bc0, e0);
-            a[1] = featPair(S, base1, bc1, e0);
-            a[2] = featPair(S, base0, bc0, e1);
-            a[3] = featPair(S, base1, bc1, e1);
+    for (int j = 0; j < MPW; j++)
 #pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
-                const uint16_t* w = &S.w1[(nt * 8 + g) * SW1 + ks * 16 + 2 * t];
-                mma16816(acc[nt], a, ld32(w), ld32(w + 8));
-            }
+        for (int r = 0; r < 2; r++) {
+            const int q = min(min(warp + 8 * j, M1T - 1) * 16 + g + 8 * r, NR1 - 1);
+            base[j][r] = winBase(q);
+            bc[j][r] = winBed(S, base[j][r]);
         }
+    float acc[MPW][4][4] = {};
+#pragma unroll 2
+    for (int ks = 0; ks < K1P / 16; ks++) {
+        const int e0 = S.koffP[ks * 8 + t], e1 = S.koffP[ks * 8 + 4 + t];
+        uint32_t bw[4][2];
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++) {
+            const uint16_t* w = &S.w1[(nt * 8 + g) * SW1 + ks * 16 + 2 * t];
+            bw[nt][0] = ld32(w);
+            bw[nt][1] = ld32(w + 8);
+        }
+#pragma unroll
+        for (int j = 0; j < MPW; j++) {
+            if (j == MPW - 1 && !third) break;
+            uint32_t a[4];
+            a[0] = featPair(S, base[j][0], bc[j][0], e0);
+            a[1] = featPair(S, base[j][1], bc[j][1], e0);
+            a[2] = featPair(S, base[j][0], bc[j][0], e1);
+            a[3] = featPair(S, base[j][1], bc[j][1], e1);
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) mma16816(acc[j][nt], a, bw[nt][0], bw[nt][1]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < MPW; j++) {
+        const int mt = warp + 8 * j;
+        if (mt >= M1T) break;
+        const int r0 = mt * 16 + g, r1 = r0 + 8;
 #pragma unroll
         for (int nt = 0; nt < 4; nt++) {
             const int o = nt * 8 + 2 * t;
             if (r0 < NR1)
-                st32(&S.a1[r0 * SA + o], pack2(relu(acc[nt][0] + S.b1[o]), relu(acc[nt][1] + S.b1[o + 1])));
+                st32(&S.a1[r0 * SA + o],
+                     pack2(relu(acc[j][nt][0] + S.b1[o]), relu(acc[j][nt][1] + S.b1[o + 1])));
             if (r1 < NR1)
-                st32(&S.a1[r1 * SA + o], pack2(relu(acc[nt][2] + S.b1[o]), relu(acc[nt][3] + S.b1[o + 1])));
+                st32(&S.a1[r1 * SA + o],
+                     pack2(relu(acc[j][nt][2] + S.b1[o]), relu(acc[j][nt][3] + S.b1[o + 1])));
         }
     }
 }
 
-// Layers 2 and 3 on output rows warp and warp+8.  z2: layer-2
-// pre-activations (accumulator fragments); out[m]: layer-3 outputs of rows
-// g and g+8 of output row warp+8m, channels 2t and 2t+1 (t < 2 valid).
+// Layers 2 and 3 on output rows warp and warp+8 (one weight fragment load
+// for both).  z2: layer-2 pre-activations (accumulator fragments); out[m]:
+// layer-3 outputs of rows g and g+8 of output row warp+8m, channels 2t and
+// 2t+1 (t < 2 valid).
 __device__ void conv23(const NetSmem& S, int warp, int lane, float z2[2][4][4], float out[2][4]) {
     const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int m = 0; m < 2; m++) {
-        const int oy = warp + 8 * m;
-        float acc[4][4] = {};
+    float acc[2][4][4] = {};
 #pragma unroll 1
-        for (int tap = 0; tap < 9; tap++) {
-            const int dy = tap / 3, dx = tap % 3;
-            const uint16_t* p0 = &S.a1[((oy + dy) * R1 + g + dx) * SA + 2 * t];
-            const uint16_t* p1 = p0 + 8 * SA;
+    for (int tap = 0; tap < 9; tap++) {
+        const int dy = tap / 3, dx = tap % 3;
+        const uint16_t* p0 = &S.a1[((warp + dy) * R1 + g + dx) * SA + 2 * t];
+        const uint16_t* p1 = p0 + 8 * R1 * SA;
 #pragma unroll
-            for (int kb = 0; kb < 2; kb++) {
+        for (int kb = 0; kb < 2; kb++) {
+            const int kk = tap * 32 + kb * 16 + 2 * t;
+            uint32_t bw[4][2];
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const uint16_t* w = &S.w2[(nt * 8 + g) * SW2 + kk];
+                bw[nt][0] = ld32(w);
+                bw[nt][1] = ld32(w + 8);
+            }
+#pragma unroll
+            for (int m = 0; m < 2; m++) {
+                const uint16_t* pm = m ? p1 : p0;
                 uint32_t a[4];
-                a[0] = ld32(p0 + kb * 16);
-                a[1] = ld32(p1 + kb * 16);
-                a[2] = ld32(p0 + kb * 16 + 8);
-                a[3] = ld32(p1 + kb * 16 + 8);
-                const int kk = tap * 32 + kb * 16 + 2 * t;
+                a[0] = ld32(pm + kb * 16);
+                a[1] = ld32(pm + 8 * SA + kb * 16);
+                a[2] = ld32(pm + kb * 16 + 8);
+                a[3] = ld32(pm + 8 * SA + kb * 16 + 8);
 #pragma unroll
-                for (int nt = 0; nt < 4; nt++) {
-                    const uint16_t* w = &S.w2[(nt * 8 + g) * SW2 + kk];
-                    mma16816(acc[nt], a, ld32(w), ld32(w + 8));
-                }
+                for (int nt = 0; nt < 4; nt++) mma16816(acc[m][nt], a, bw[nt][0], bw[nt][1]);
             }
         }
+    }
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
 #pragma unroll
         for (int nt = 0; nt < 4; nt++) {
             const int o = nt * 8 + 2 * t;
-            z2[m][nt][0] = acc[nt][0] + S.b2[o];
-            z2[m][nt][1] = acc[nt][1] + S.b2[o + 1];
-            z2[m][nt][2] = acc[nt][2] + S.b2[o];
-            z2[m][nt][3] = acc[nt][3] + S.b2[o + 1];
+            z2[m][nt][0] = acc[m][nt][0] + S.b2[o];
+            z2[m][nt][1] = acc[m][nt][1] + S.b2[o + 1];
+            z2[m][nt][2] = acc[m][nt][2] + S.b2[o];
+            z2[m][nt][3] = acc[m][nt][3] + S.b2[o + 1];
         }
         float acc3[4] = {};
 #pragma unroll
