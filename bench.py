@@ -491,6 +491,42 @@ def _timed_chunks(run_to, tf, every_s, depth):
 ARRIVAL_DEPTH = 0.05  # m: a cell has "arrived" once its depth passes 5 cm
 
 
+def closure_step_rate(cc, model, args, t_spin=1800.0, reps=20):
+    """Tensor-core rate of the closure step (k_closure + k_apply) on a wet
+    state: the coarse case spun up to t_spin by the engine alone, then one
+    untimed and `reps` timed applications, CUDA events on the engine's
+    stream.  Algorithmic FLOPs: 2 x 14,144 multiply-adds per output cell of
+    every evaluated 16 x 16 block."""
+    import torch
+
+    from rift_gb300 import closure
+
+    sim = capi.Sim(cc).setup()
+    sim.run(2 ** 31 - 1, min(args.tf, t_spin))
+    cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain)
+    st = torch.cuda.ExternalStream(cr.view.stream)
+    t = sim.time()[0]
+    cr.apply(1e-3, t)
+    torch.cuda.synchronize()
+    b0 = cr.block_counts()[0]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        cr.apply(1e-3, t)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    blocks = (cr.block_counts()[0] - b0) / reps
+    sim.close()
+    flops = blocks * 256 * 2 * (150 * 32 + 288 * 32 + 32 * 4)
+    pk = bf16_peak()
+    achieved = flops / (ms * 1e-3) / 1e12
+    return {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / pk["bf16_tflops"], "traffic": None, "peak_kind": pk["kind"],
+            "kernel": "k_closure + k_apply (one closure step)", "ms_per_apply": ms,
+            "blocks_per_apply": blocks, "coarse_cells": (cc.h_nx - 4) * (cc.h_ny - 4)}
+
+
 def run_closure(args):
     """Config 4: train the closure on fine runs of --closure-seeds scenarios
     (1024^2 at 2 m), then run held-out scenarios fine (N^2 at 2 m) and
@@ -503,6 +539,12 @@ def run_closure(args):
         print(m, file=sys.stderr, flush=True)
 
     N = args.N or 4096
+    if args.closure_profile:
+        # the closure step alone on a wet coarse state (ncu target): untrained
+        # weights, unit scales
+        cc = closure.coarse_case(closure.scenario(100_001, N=N, cell=2.0, tf=args.tf))
+        model = closure.Model(closure.init_params(0), np.ones(6, np.float32), np.full(4, 1e-4, np.float32))
+        return {"workload": "config4 closure step", "roofline": closure_step_rate(cc, model, args)}
     t0 = time.perf_counter()
     ds = closure.generate(list(range(args.closure_seeds)), N=args.closure_train_N, cell=2.0, log=log)
     t_gen = time.perf_counter() - t0
@@ -558,28 +600,7 @@ def run_closure(args):
         evals.append(res)
         log(json.dumps(res))
     clk = clocks.stop()
-    # tensor-core rate of the closure step: re-run the apply kernels on the
-    # last coarse state, timed with CUDA events on the engine's stream
-    sim = capi.Sim(cc).setup()
-    sim.run(2 ** 31 - 1, min(args.tf, 1800.0))
-    cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain)
-    st = torch.cuda.ExternalStream(cr.view.stream)
-    cr.apply(1e-3, 1800.0)
-    torch.cuda.synchronize()
-    b0 = cr.block_counts()[0]
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 20
-    e0.record(st)
-    for _ in range(reps):
-        cr.apply(1e-3, 1800.0)
-    e1.record(st)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    blocks = (cr.block_counts()[0] - b0) / reps
-    sim.close()
-    flops = blocks * 256 * 2 * (150 * 32 + 288 * 32 + 32 * 4)
-    pk = bf16_peak()
-    achieved = flops / (ms * 1e-3) / 1e12
+    roof = closure_step_rate(cc, model, args)
     sp = float(np.mean([r["speedup_closure"] for r in evals]))
     line = {"metric": "closure vs fine-grid wall-time ratio", "value": sp, "unit": "x",
             "n_gpus": 1, "steps": None, "warmup": 0, "ms_per_step": None,
@@ -597,10 +618,7 @@ def run_closure(args):
             "evals": evals,
             "training": {"generate_s": t_gen, "train_s": t_train, "loss_first": float(loss[:20].mean()),
                          "loss_last": float(loss[-20:].mean())},
-            "roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"],
-                         "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"], "traffic": None,
-                         "peak_kind": pk["kind"], "kernel": "k_closure + k_apply (one closure step)",
-                         "ms_per_apply": ms, "blocks_per_apply": blocks},
+            "roofline": roof,
             "clocks": clk, "gpu_launches": None}
     return line
 
@@ -617,6 +635,8 @@ def main():
     ap.add_argument("--eval-seeds", type=int, default=2, help="config 4: held-out scenarios")
     ap.add_argument("--closure-every", type=int, default=4,
                     help="config 4: coarse steps between closure applications")
+    ap.add_argument("--closure-profile", action="store_true",
+                    help="config 4: time only the closure step on a wet coarse state")
     ap.add_argument("--closure-gain", type=float, default=0.25,
                     help="config 4: strength of the applied corrections (chosen on scenario 100000)")
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")

@@ -335,6 +335,9 @@ def generate(seeds, N=1024, cell=2.0, sample_times=(600.0, 1200.0, 1800.0, 2400.
         coarse.close()
         if log:
             log(f"scenario {seed}: {got} patches ({time.time() - t0:.1f} s)")
+    if not feats:
+        raise ValueError("no training patches: no 64 x 64 block had enough corrected faces "
+                         "(more or larger scenarios, later sample times or a smaller min_frac)")
     return Dataset(np.stack(feats), np.stack(targets), np.stack(masks))
 
 

@@ -42,7 +42,10 @@ constexpr int NR1 = R1 * R1;     // 324
 constexpr int NRI = RI * RI;     // 484
 constexpr int M1T = (NR1 + 15) / 16;  // 21 MMA row tiles of layer 1
 constexpr int SA = 40;           // BF16 row stride of the activation tiles
-constexpr int SW1 = 168, SW2 = 296, SW3 = 40;  // BF16 row strides of the weights
+constexpr int CB = 8;            // BF16 input channels per cell: h, hu, hv, b_hi, b_lo, n, rain, 0
+constexpr int NTAP1 = 26;        // layer-1 taps, the 26th a zero-weight pad
+constexpr int K1B = NTAP1 * CB;  // 208: layer-1 reduction over the BF16 inputs
+constexpr int SW1 = K1B + 8, SW2 = 296, SW3 = 40;  // BF16 row strides of the weights
 constexpr int NT = 256;
 constexpr int BEDBIT = 1 << 20, OFFMASK = BEDBIT - 1;
 
@@ -55,14 +58,17 @@ static_assert(OFF_B1 == OFF_W1 + C1 * K1P && OFF_W2 == OFF_B1 + C1 && OFF_B2 == 
               "parameter layout");
 
 struct NetSmem {
-    float xs[NRI * CIN];       // scaled inputs, channels last
+    float xs[NRI * CIN];       // scaled inputs (FP32), channels last
+    uint16_t xb[NRI * CB];     // the same as BF16 rows of 8; the bed relative to bref, in two halves
     uint16_t a1[NR1 * SA];     // layer-1 activations (BF16); dZ1 in the backward pass
-    uint16_t w1[C1 * SW1];     // W1[o][k]
+    uint16_t w1[C1 * SW1];     // W1 over the BF16 inputs: [o][tap*8 + c8]
     uint16_t w2[C1 * SW2];     // W2[o][k]
     uint16_t w3[8 * SW3];      // W3[o][c], rows 4..7 zero
     float b1[C1], b2[C1], b3[8];
-    int koffP[K1P / 2];        // layer-1 A fragments: offset of the k pair (2kp, 2kp+1) in xs
-    int koffE[K1P];            // the same per element (layer-1 weight gradient)
+    float sbed[C1];            // sum over taps of layer 1's (BF16) bed weights
+    int toff[NTAP1];           // cell offset of each layer-1 tap in the input block
+    int koffE[K1P];            // xs offset of each layer-1 reduction index (weight gradient)
+    float bref;                // the block's reference bed (scaled)
     int red[4];
 };
 
@@ -102,12 +108,26 @@ __device__ __forceinline__ void mma16816(float d[4], const uint32_t a[4], uint32
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
+// Four 8x8 BF16 matrices from shared memory; lane l gives the address of
+// row l%8 of matrix l/8, and r[i] receives matrix i in the MMA fragment
+// layout (thread T: row T/4, columns 2(T%4), 2(T%4)+1).  Row addresses are
+// 16-byte aligned.
+__device__ __forceinline__ void ldsm4(uint32_t r[4], const void* p) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+
 // Weights (BF16), biases and the layer-1 offset tables, once per CTA.
+// Layer 1 reads the BF16 input rows (h, hu, hv, b_hi, b_lo, n, rain, 0):
+// both bed halves take the bed weight.
 __device__ void stageNet(NetSmem& S, const float* __restrict__ P) {
     const int tid = threadIdx.x;
+    constexpr int MAP[CB] = {0, 1, 2, 3, 3, 4, 5, -1};
     for (int i = tid; i < C1 * SW1; i += NT) {
-        int o = i / SW1, k = i % SW1;
-        S.w1[i] = bf(k < K1 ? P[OFF_W1 + o * K1P + k] : 0.f);
+        const int o = i / SW1, k = i % SW1, tap = k / CB, c = MAP[k % CB];
+        S.w1[i] = bf(k < K1B && tap < 25 && c >= 0 ? P[OFF_W1 + o * K1P + tap * CIN + c] : 0.f);
     }
     for (int i = tid; i < C1 * SW2; i += NT) {
         int o = i / SW2, k = i % SW2;
@@ -120,8 +140,12 @@ __device__ void stageNet(NetSmem& S, const float* __restrict__ P) {
     if (tid < C1) {
         S.b1[tid] = P[OFF_B1 + tid];
         S.b2[tid] = P[OFF_B2 + tid];
+        float sb = 0.f;
+        for (int tap = 0; tap < 25; tap++) sb += fb(bf(P[OFF_W1 + tid * K1P + tap * CIN + 3]));
+        S.sbed[tid] = sb;
     }
     if (tid < 8) S.b3[tid] = tid < COUT ? P[OFF_B3 + tid] : 0.f;
+    if (tid < NTAP1) S.toff[tid] = tid < 25 ? (tid / 5) * RI + tid % 5 : 0;
     for (int k = tid; k < K1P; k += NT) {
         int e = -1;
         if (k < K1) {
@@ -130,41 +154,43 @@ __device__ void stageNet(NetSmem& S, const float* __restrict__ P) {
             if (c == 3) e |= BEDBIT;
         }
         S.koffE[k] = e;
-        if ((k & 1) == 0) {
-            int p = -1;
-            if (k < K1) {
-                int tap = k / CIN, c = k % CIN;
-                p = ((tap / 5) * RI + tap % 5) * CIN + c;
-                if (c == 2) p |= BEDBIT;  // the pair (hv, b): its second element is the bed
-            }
-            S.koffP[k >> 1] = p;
-        }
     }
 }
 
-// The 22 x 22 input block whose corner is image cell (Y0, X0) of sample s.
+// The 22 x 22 input block whose corner is image cell (Y0, X0) of sample s:
+// FP32 (xs) and BF16 rows (xb).  The BF16 bed is b - bref, bref the bed of
+// the block's centre cell, split into a BF16 value and its BF16 remainder
+// (16 significant bits together).
 __device__ void stageInput(NetSmem& S, const rift_closure_src& src, int s, int Y0, int X0) {
     const size_t sbase = (size_t)s * (size_t)src.sample_stride;
-    for (int i = threadIdx.x; i < NRI; i += NT) {
-        int ry = i / RI, rx = i % RI;
+    auto at = [&](int ry, int rx) {
         int y = min(max(Y0 + ry, 0), src.H - 1), x = min(max(X0 + rx, 0), src.W - 1);
-        size_t off = sbase + (size_t)y * (size_t)src.pitch + (size_t)x;
+        return sbase + (size_t)y * (size_t)src.pitch + (size_t)x;
+    };
+    const float bref = (src.plane[3] ? __ldg(src.plane[3] + at(RI / 2, RI / 2)) : src.value[3]) * src.scale[3];
+    if (threadIdx.x == 0) S.bref = bref;
+    for (int i = threadIdx.x; i < NRI; i += NT) {
+        const size_t off = at(i / RI, i % RI);
+        float v[CIN];
 #pragma unroll
         for (int c = 0; c < CIN; c++) {
-            float v = src.plane[c] ? __ldg(src.plane[c] + off) : src.value[c];
-            S.xs[i * CIN + c] = v * src.scale[c];
+            v[c] = (src.plane[c] ? __ldg(src.plane[c] + off) : src.value[c]) * src.scale[c];
+            S.xs[i * CIN + c] = v[c];
         }
+        const float br = v[3] - bref;
+        const uint16_t bh = bf(br);
+        const uint16_t bl = bf(br - fb(bh));
+        uint4 w;
+        w.x = pack2(v[0], v[1]);
+        w.y = pack16(bf(v[2]), bh);
+        w.z = pack16(bl, bf(v[4]));
+        w.w = pack16(bf(v[5]), 0);
+        *reinterpret_cast<uint4*>(&S.xb[i * CB]) = w;
     }
 }
 
-// Layer-1 input pair (k, k+1) of the cell whose 5x5 window starts at xs
-// offset `base`: the bed enters relative to the window's centre bc.
-__device__ __forceinline__ uint32_t featPair(const NetSmem& S, int base, float bc, int e) {
-    if (e < 0) return 0u;
-    float2 v = *reinterpret_cast<const float2*>(&S.xs[base + (e & OFFMASK)]);
-    if (e & BEDBIT) v.y -= bc;
-    return pack2(v.x, v.y);
-}
+// Layer-1 input k (tap, channel) of the cell whose 5x5 window starts at xs
+// offset `base`, FP32: the bed relative to the window's centre bc.
 __device__ __forceinline__ float featElem(const NetSmem& S, int base, float bc, int e) {
     if (e < 0) return 0.f;
     float v = S.xs[base + (e & OFFMASK)];
@@ -176,93 +202,104 @@ __device__ __forceinline__ float winBed(const NetSmem& S, int base) {
 }
 
 // Layer 1 on the 18 x 18 region: a1 = relu(W1 x + b1), BF16.  A warp owns
-// row tiles warp, warp+8 and (warps 0..4) warp+16, and loads each weight
-// fragment once for all of them.
+// row tiles warp, warp+8 and (warps 0..4) warp+16.  One k step covers two
+// taps of the 8-channel BF16 input rows, so each 8 x 8 block of an A
+// fragment is 8 cells' rows of one tap and comes with one ldmatrix; the
+// bed enters relative to bref and the epilogue subtracts (centre bed -
+// bref) x (sum of the bed weights), which makes it relative to the
+// window's centre.
 __device__ void conv1(NetSmem& S, int warp, int lane) {
     const int g = lane >> 2, t = lane & 3;
     constexpr int MPW = (M1T + 7) / 8;  // 3
     const bool third = warp + 16 < M1T;
-    int base[MPW][2];
-    float bc[MPW][2];
+    // this lane's ldmatrix rows: row (lane & 15) of each of its row tiles,
+    // the tap of the k step's second half for lanes 16..31
+    const int lrow = lane & 15, lhalf = lane >> 4;
+    int rowCell[MPW];
 #pragma unroll
-    for (int j = 0; j < MPW; j++)
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-            const int q = min(min(warp + 8 * j, M1T - 1) * 16 + g + 8 * r, NR1 - 1);
-            base[j][r] = winBase(q);
-            bc[j][r] = winBed(S, base[j][r]);
-        }
+    for (int j = 0; j < MPW; j++) {
+        const int q = min(min(warp + 8 * j, M1T - 1) * 16 + lrow, NR1 - 1);
+        rowCell[j] = (q / R1) * RI + q % R1;
+    }
+    // weights: lanes address rows n (two column tiles per ldmatrix)
+    const int wrow = (lane & 7) + ((lane >> 4) << 3), wk = ((lane >> 3) & 1) * 8;
     float acc[MPW][4][4] = {};
-#pragma unroll 2
-    for (int ks = 0; ks < K1P / 16; ks++) {
-        const int e0 = S.koffP[ks * 8 + t], e1 = S.koffP[ks * 8 + 4 + t];
+#pragma unroll 1
+    for (int ks = 0; ks < K1B / 16; ks++) {
         uint32_t bw[4][2];
 #pragma unroll
-        for (int nt = 0; nt < 4; nt++) {
-            const uint16_t* w = &S.w1[(nt * 8 + g) * SW1 + ks * 16 + 2 * t];
-            bw[nt][0] = ld32(w);
-            bw[nt][1] = ld32(w + 8);
+        for (int np = 0; np < 2; np++) {
+            uint32_t r[4];
+            ldsm4(r, &S.w1[(np * 16 + wrow) * SW1 + ks * 16 + wk]);
+            bw[2 * np][0] = r[0];
+            bw[2 * np][1] = r[1];
+            bw[2 * np + 1][0] = r[2];
+            bw[2 * np + 1][1] = r[3];
         }
+        const int toff = S.toff[2 * ks + lhalf];
 #pragma unroll
         for (int j = 0; j < MPW; j++) {
             if (j == MPW - 1 && !third) break;
             uint32_t a[4];
-            a[0] = featPair(S, base[j][0], bc[j][0], e0);
-            a[1] = featPair(S, base[j][1], bc[j][1], e0);
-            a[2] = featPair(S, base[j][0], bc[j][0], e1);
-            a[3] = featPair(S, base[j][1], bc[j][1], e1);
+            ldsm4(a, &S.xb[(rowCell[j] + toff) * CB]);
+            // ldmatrix order: rows 0-7 tap A, rows 8-15 tap A, rows 0-7 tap B, rows 8-15 tap B
 #pragma unroll
             for (int nt = 0; nt < 4; nt++) mma16816(acc[j][nt], a, bw[nt][0], bw[nt][1]);
         }
     }
+    const float bref = S.bref;
 #pragma unroll
     for (int j = 0; j < MPW; j++) {
         const int mt = warp + 8 * j;
         if (mt >= M1T) break;
         const int r0 = mt * 16 + g, r1 = r0 + 8;
+        const float c0 = winBed(S, winBase(min(r0, NR1 - 1))) - bref;
+        const float c1 = winBed(S, winBase(min(r1, NR1 - 1))) - bref;
 #pragma unroll
         for (int nt = 0; nt < 4; nt++) {
             const int o = nt * 8 + 2 * t;
+            const float s0 = S.sbed[o], s1 = S.sbed[o + 1];
             if (r0 < NR1)
-                st32(&S.a1[r0 * SA + o],
-                     pack2(relu(acc[j][nt][0] + S.b1[o]), relu(acc[j][nt][1] + S.b1[o + 1])));
+                st32(&S.a1[r0 * SA + o], pack2(relu(acc[j][nt][0] + S.b1[o] - c0 * s0),
+                                               relu(acc[j][nt][1] + S.b1[o + 1] - c0 * s1)));
             if (r1 < NR1)
-                st32(&S.a1[r1 * SA + o],
-                     pack2(relu(acc[j][nt][2] + S.b1[o]), relu(acc[j][nt][3] + S.b1[o + 1])));
+                st32(&S.a1[r1 * SA + o], pack2(relu(acc[j][nt][2] + S.b1[o] - c1 * s0),
+                                               relu(acc[j][nt][3] + S.b1[o + 1] - c1 * s1)));
         }
     }
 }
 
 // Layers 2 and 3 on output rows warp and warp+8 (one weight fragment load
-// for both).  z2: layer-2 pre-activations (accumulator fragments); out[m]:
-// layer-3 outputs of rows g and g+8 of output row warp+8m, channels 2t and
-// 2t+1 (t < 2 valid).
+// for both; A and B fragments by ldmatrix).  z2: layer-2 pre-activations
+// (accumulator fragments); out[m]: layer-3 outputs of rows g and g+8 of
+// output row warp+8m, channels 2t and 2t+1 (t < 2 valid).
 __device__ void conv23(const NetSmem& S, int warp, int lane, float z2[2][4][4], float out[2][4]) {
     const int g = lane >> 2, t = lane & 3;
+    const int lrow = lane & 15, lk = (lane >> 4) * 8;  // A: row, k offset of this lane's address
+    const int wrow = (lane & 7) + ((lane >> 4) << 3), wk = ((lane >> 3) & 1) * 8;
     float acc[2][4][4] = {};
 #pragma unroll 1
     for (int tap = 0; tap < 9; tap++) {
         const int dy = tap / 3, dx = tap % 3;
-        const uint16_t* p0 = &S.a1[((warp + dy) * R1 + g + dx) * SA + 2 * t];
+        const uint16_t* p0 = &S.a1[((warp + dy) * R1 + lrow + dx) * SA + lk];
         const uint16_t* p1 = p0 + 8 * R1 * SA;
 #pragma unroll
         for (int kb = 0; kb < 2; kb++) {
-            const int kk = tap * 32 + kb * 16 + 2 * t;
+            const int kk = tap * 32 + kb * 16;
             uint32_t bw[4][2];
 #pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
-                const uint16_t* w = &S.w2[(nt * 8 + g) * SW2 + kk];
-                bw[nt][0] = ld32(w);
-                bw[nt][1] = ld32(w + 8);
+            for (int np = 0; np < 2; np++) {
+                uint32_t r[4];
+                ldsm4(r, &S.w2[(np * 16 + wrow) * SW2 + kk + wk]);
+                bw[2 * np][0] = r[0];
+                bw[2 * np][1] = r[1];
+                bw[2 * np + 1][0] = r[2];
+                bw[2 * np + 1][1] = r[3];
             }
 #pragma unroll
             for (int m = 0; m < 2; m++) {
-                const uint16_t* pm = m ? p1 : p0;
                 uint32_t a[4];
-                a[0] = ld32(pm + kb * 16);
-                a[1] = ld32(pm + 8 * SA + kb * 16);
-                a[2] = ld32(pm + kb * 16 + 8);
-                a[3] = ld32(pm + 8 * SA + kb * 16 + 8);
+                ldsm4(a, (m ? p1 : p0) + kb * 16);
 #pragma unroll
                 for (int nt = 0; nt < 4; nt++) mma16816(acc[m][nt], a, bw[nt][0], bw[nt][1]);
             }

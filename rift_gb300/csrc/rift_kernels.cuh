@@ -32,6 +32,7 @@
 #include <cstdint>
 
 #include "rift_device.cuh"
+#include "rift_divdf.h"
 
 namespace rift {
 
@@ -110,6 +111,10 @@ struct Params {
     float dx, dy, inv_dx, inv_dy, kappa, psiDtheta, nodata;
     double dxd, dyd, kappad, courant;
     float courantScale;  // 1/courant when courant is a power of two, else 0
+    float kappaf;        // (float)kappa
+    bool squareCells;    // dx == dy
+    unsigned long long dxMant;  // dx = dxMant * 2^dxExp, dxMant a 53-bit integer (top bit 52)
+    int dxExp;
     uint32_t flags;
     float* A;          // [3][rows][pitch]  U^n / U^{n+1}: h, hu, hv
     float* B;          // [3][rows][pitch]  U*
@@ -323,25 +328,30 @@ __device__ __forceinline__ float blockMax(float v, float* red) {
 // with square cells min(dx / fx, dx / fy) = dx / max(fx, fy) (rounded
 // division is monotone in the divisor): one FP64 division instead of four,
 // with the same result.
-__device__ __forceinline__ double stepDtAt(const Params& P, double t, double maxx, double maxy) {
+// dt of a step (Simulator::ComputeTimestep's arithmetic, simulator.cu:540-566)
+// from the float speed maxima; t == 0 gives the reference's first-step dt.
+__device__ __forceinline__ double stepDtAt(const Params& P, double t, float maxx, float maxy) {
     double dt;
     if (P.courantScale > 0.f) {
-        const float kap = (float)P.kappad;
-        const float fx = fmaxf((float)maxx * P.courantScale, kap);
-        const float fy = fmaxf((float)maxy * P.courantScale, kap);
-        if (P.dxd == P.dyd) {
-            dt = P.dxd / (double)fmaxf(fx, fy);
+        const float fx = fmaxf(maxx * P.courantScale, P.kappaf);
+        const float fy = fmaxf(maxy * P.courantScale, P.kappaf);
+        if (P.squareCells) {
+            const float f = fmaxf(fx, fy);
+            if (!divDF(P.dxMant, P.dxExp, f, &dt)) dt = P.dxd / (double)f;
         } else {
             const double cx = P.dxd / (double)fx, cy = P.dyd / (double)fy;
             dt = cx < cy ? cx : cy;
         }
     } else {
-        double cx = P.dxd / (double)fmaxf((float)(maxx / P.courant), (float)P.kappad);
-        double cy = P.dyd / (double)fmaxf((float)(maxy / P.courant), (float)P.kappad);
+        double cx = P.dxd / (double)fmaxf((float)((double)maxx / P.courant), P.kappaf);
+        double cy = P.dyd / (double)fmaxf((float)((double)maxy / P.courant), P.kappaf);
         dt = cx < cy ? cx : cy;
     }
-    if (t == 0.0) dt = (double)0.000001f;
+    if ((__double_as_longlong(t) << 1) == 0) dt = (double)0.000001f;  // t == 0.0
     return dt;
+}
+__device__ __forceinline__ double stepDtAt(const Params& P, double t, double maxx, double maxy) {
+    return stepDtAt(P, t, (float)maxx, (float)maxy);
 }
 
 __device__ __forceinline__ double stepDt(const Params& P, const DevState* st, double maxx,

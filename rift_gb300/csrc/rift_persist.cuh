@@ -510,8 +510,8 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                     sched = (int)ld_relaxed_gpu((const unsigned*)&T->schedCnt[par]);
                     fail = owned != sched;
                 }
-                const double dtNew = stepDtAt(P, tNow, (double)__uint_as_float(max(mx0, mx1)),
-                                              (double)__uint_as_float(max(my0, my1)));
+                const double dtNew = stepDtAt(P, tNow, __uint_as_float(max(mx0, mx1)),
+                                              __uint_as_float(max(my0, my1)));
                 const double tNew = tNow + dtNew;
                 StageConsts c1 = stageConstsAt<1>(P, dtNew, dtPrev, tNew);
                 StageConsts c2 = stageConstsAt<2>(P, dtNew, dtPrev, tNew);
