@@ -633,7 +633,7 @@ def main():
     ap.add_argument("--closure-train-N", type=int, default=1024, help="config 4: training grid side")
     ap.add_argument("--train-steps", type=int, default=1500, help="config 4: Adam steps")
     ap.add_argument("--eval-seeds", type=int, default=2, help="config 4: held-out scenarios")
-    ap.add_argument("--closure-every", type=int, default=4,
+    ap.add_argument("--closure-every", type=int, default=8,
                     help="config 4: coarse steps between closure applications")
     ap.add_argument("--closure-profile", action="store_true",
                     help="config 4: time only the closure step on a wet coarse state")
