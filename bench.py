@@ -421,16 +421,35 @@ def run_ensemble(args):
     (rift_ensemble_run), timed on the host around the synchronous call, then
     the same members run one after another for comparison."""
     cases = synth.config5(members=args.members, side=(args.side_min, args.side_max), tf=args.tf)
+    model = None
+    if args.closure:
+        # members coarsened 2x (10 m cells) with the learned closure, trained
+        # on scenarios at the members' fine resolution (5 m -> 10 m)
+        from rift_gb300 import closure
+        ds = closure.generate(list(range(args.closure_seeds)), N=args.closure_train_N, cell=5.0,
+                              log=lambda m: print(m, file=sys.stderr, flush=True))
+        model, _ = closure.train(ds, steps=args.train_steps, batch=256)
+        del ds
+        cases = [closure.coarse_case(closure.even_side(c)) for c in cases]
 
     def setup():
         return [capi.Sim(c).setup() for c in cases]
 
+    if model is not None:
+        args.sequential = False  # the one-after-another comparison runs members without it
     members = setup()
     ens = capi.Ensemble(members)
     ens.run(max_steps=args.warmup)  # warm-up steps (counted in t, not timed)
+    runner = None
+    if model is not None:
+        runner = closure.EnsembleClosure(ens, members, model, every=args.closure_every,
+                                         gain=args.closure_gain)
     clocks = ClockSampler().start()
     t0 = time.perf_counter()
-    t_end, k = ens.run(t_stop=args.tf)
+    if runner is None:
+        t_end, k = ens.run(t_stop=args.tf)
+    else:
+        t_end, k = runner.run(args.tf)
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     ens.close()
@@ -465,6 +484,15 @@ def run_ensemble(args):
     if args.sequential:
         line["sequential_s"] = seq
         line["ensemble_speedup_vs_sequential"] = seq / wall
+    if runner is not None:
+        ev, fbk = 0, 0
+        for r in runner.runs:
+            a, b = r.block_counts()
+            ev, fbk = ev + a, fbk + b
+        line["config"]["closure"] = {"grid": "members coarsened 2x (10 m cells)",
+                                     "every_steps": args.closure_every, "gain": args.closure_gain,
+                                     "train_scenarios": args.closure_seeds,
+                                     "blocks_evaluated": ev, "blocks_fallen_back": fbk}
     return line
 
 
@@ -635,6 +663,8 @@ def main():
     ap.add_argument("--eval-seeds", type=int, default=2, help="config 4: held-out scenarios")
     ap.add_argument("--closure-every", type=int, default=8,
                     help="config 4: coarse steps between closure applications")
+    ap.add_argument("--closure", action="store_true",
+                    help="config 5: members coarsened 2x with the learned closure")
     ap.add_argument("--closure-profile", action="store_true",
                     help="config 4: time only the closure step on a wet coarse state")
     ap.add_argument("--closure-gain", type=float, default=0.25,

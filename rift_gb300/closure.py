@@ -194,9 +194,33 @@ def coarse_case(fine: synth.Case) -> synth.Case:
         out[2:-2, 2:-2] = restrict(a[2:-2, 2:-2])
         return out
 
+    src = None
+    if fine.src_idx is not None:
+        # a point source stays a volume rate at the coarse cell holding it
+        ny_c, nx_c = B.shape[0] + 3, B.shape[1] + 3
+        j, i = np.divmod(np.asarray(fine.src_idx, dtype=np.int64), fine.h_nx)
+        J = np.clip(2 + (j - 2) // 2, 2, ny_c - 3)
+        I = np.clip(2 + (i - 2) // 2, 2, nx_c - 3)
+        src = (J * nx_c + I).astype(np.int32)
     return dataclasses.replace(fine, name=fine.name + "_coarse", B=B, cell=2.0 * fine.cell,
                                n=restrict_cells(fine.n), K=restrict_cells(fine.K),
-                               h0=restrict_cells(fine.h0), src_idx=None, rain_maps=None)
+                               h0=restrict_cells(fine.h0), src_idx=src, rain_maps=None)
+
+
+def even_side(case: synth.Case) -> synth.Case:
+    """The case cropped to an even number of cells per side (the last corner
+    row and column dropped), so that it coarsens 2x."""
+    N = case.b_nx - 1
+    if N % 2 == 0:
+        return case
+    crop = lambda a: None if a is None else a[:-1, :-1].copy()
+    src = None
+    if case.src_idx is not None:
+        j, i = np.divmod(np.asarray(case.src_idx, dtype=np.int64), case.h_nx)
+        j, i = np.minimum(j, case.h_ny - 4), np.minimum(i, case.h_nx - 4)
+        src = (j * (case.h_nx - 1) + i).astype(np.int32)
+    return dataclasses.replace(case, B=case.B[:-1, :-1].copy(), n=crop(case.n), K=crop(case.K),
+                               h0=crop(case.h0), src_idx=src)
 
 
 def restrict(a):
@@ -485,5 +509,36 @@ class ClosureRun:
 
     def block_counts(self):
         """(blocks evaluated, blocks that fell back) over every apply."""
+        _torch().cuda.synchronize()
         c = self.counters.cpu().numpy()
         return int(c[0]), int(c[1])
+
+
+class EnsembleClosure:
+    """An ensemble (capi.Ensemble) of coarse members with the closure: the
+    persistent ensemble kernel advances every live member by `every` of its
+    own steps, then each member that moved gets the closure over the time it
+    covered; repeated until every member reaches t_stop."""
+
+    def __init__(self, ens, sims, model: Model, every=8, **kw):
+        self.ens, self.sims, self.every = ens, list(sims), every
+        self.runs = [ClosureRun(s, model, every=every, **kw) for s in self.sims]
+
+    def run(self, t_stop):
+        torch = _torch()
+        t_prev = np.array([s.time()[0] for s in self.sims])
+        steps = np.zeros(len(self.sims), dtype=np.int64)
+        while True:
+            t, k = self.ens.run(t_stop=t_stop, max_steps=self.every)
+            if k.max() == 0:
+                break
+            steps += k
+            for m in np.nonzero(t > t_prev)[0]:
+                self.runs[m].apply(t[m] - t_prev[m], t[m])
+            # the closure kernels run on the members' streams, the ensemble
+            # kernel on its own: finish them before the next launch
+            torch.cuda.synchronize()
+            t_prev = t
+            if (t >= t_stop).all():
+                break
+        return t_prev, steps

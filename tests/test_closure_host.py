@@ -91,3 +91,18 @@ def test_patch_cutter_repeats_edges_and_filters():
     assert f.shape == (6, 70, 70) and t.shape == (4, 64, 64)
     assert f[0, 0, 0] == 0 and f[0, 0, 3] == 0 and f[0, 0, 4] == 1
     assert (t == 2).all() and (m == 1).all()
+
+
+def test_even_side_and_coarse_point_sources():
+    cases = synth.config5(members=2, side=(33, 33), tf=600.0)
+    c = cases[1]                      # odd side, with a point source
+    assert (c.b_nx - 1) % 2 == 1 and c.src_idx is not None
+    e = closure.even_side(c)
+    assert e.b_nx - 1 == 32 and e.n.shape == (e.h_ny, e.h_nx)
+    j, i = divmod(int(c.src_idx[0]), c.h_nx)
+    je, ie = divmod(int(e.src_idx[0]), e.h_nx)
+    assert (je, ie) == (min(j, e.h_ny - 3), min(i, e.h_nx - 3))
+    k = closure.coarse_case(e)
+    J, I = divmod(int(k.src_idx[0]), k.h_nx)
+    assert (J, I) == (2 + (je - 2) // 2, 2 + (ie - 2) // 2)
+    assert 2 <= J <= k.h_ny - 3 and 2 <= I <= k.h_nx - 3

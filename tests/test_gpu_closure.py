@@ -333,3 +333,27 @@ def test_generate_train_and_run_end_to_end(torch):
     assert t >= 600.0 and run.applies > 0
     vol, added = sim.mass_ledger()
     assert abs(vol - added) <= 1e-5 * added
+
+
+def test_ensemble_with_closure_matches_members_alone(torch):
+    """Coarse members stepped by the ensemble kernel with the closure every
+    4 steps end where each ends run alone with the same closure."""
+    rng = np.random.default_rng(7)
+    model = closure.Model(_params(rng), SCALE, np.full(4, 2e-3, np.float32))
+    cases = [closure.coarse_case(closure.even_side(c))
+             for c in synth.config5(members=3, side=(96, 160), tf=900.0)]
+    alone = []
+    for c in cases:
+        sim = capi.Sim(c).setup()
+        closure.ClosureRun(sim, model, every=4).run(600.0)
+        alone.append((sim.time()[0], sim.field("W")))
+        sim.close()
+    sims = [capi.Sim(c).setup() for c in cases]
+    ens = capi.Ensemble(sims)
+    t, steps = closure.EnsembleClosure(ens, sims, model, every=4).run(600.0)
+    for m, s in enumerate(sims):
+        ta, wa = alone[m]
+        assert abs(t[m] - ta) <= 1e-6 * ta
+        d = np.abs(s.field("W") - wa)[2:-2, 2:-2].max()
+        assert d < 1e-3, (m, d)
+    ens.close()
