@@ -489,6 +489,7 @@ def run_ensemble(args):
         for r in runner.runs:
             a, b = r.block_counts()
             ev, fbk = ev + a, fbk + b
+        line["gpu_launches"] = runner.launches()
         line["config"]["closure"] = {"grid": "members coarsened 2x (10 m cells)",
                                      "every_steps": args.closure_every, "gain": args.closure_gain,
                                      "train_scenarios": args.closure_seeds,

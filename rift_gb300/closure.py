@@ -523,6 +523,7 @@ class EnsembleClosure:
     def __init__(self, ens, sims, model: Model, every=8, **kw):
         self.ens, self.sims, self.every = ens, list(sims), every
         self.runs = [ClosureRun(s, model, every=every, **kw) for s in self.sims]
+        self.chunks = 0  # ensemble launches (one kernel each)
 
     def run(self, t_stop):
         torch = _torch()
@@ -530,6 +531,7 @@ class EnsembleClosure:
         steps = np.zeros(len(self.sims), dtype=np.int64)
         while True:
             t, k = self.ens.run(t_stop=t_stop, max_steps=self.every)
+            self.chunks += 1
             if k.max() == 0:
                 break
             steps += k
@@ -542,3 +544,7 @@ class EnsembleClosure:
             if (t >= t_stop).all():
                 break
         return t_prev, steps
+
+    def launches(self):
+        """Kernels launched: one ensemble kernel per chunk, two per closure step."""
+        return self.chunks + 2 * sum(r.applies for r in self.runs)
