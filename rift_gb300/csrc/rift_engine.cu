@@ -148,11 +148,6 @@ Params makeParams(rift_handle* h) {
     P.kappad = h->g.kappa;
     P.kappaf = (float)h->g.kappa;
     P.squareCells = h->g.dx == h->g.dy;
-    {
-        uint64_t mx;
-        rift::splitDouble(h->g.dx, &mx, &P.dxExp);
-        P.dxMant = mx;
-    }
     P.courant = h->g.courant;
     {
         int e = 0;

@@ -32,7 +32,6 @@
 #include <cstdint>
 
 #include "rift_device.cuh"
-#include "rift_divdf.h"
 
 namespace rift {
 
@@ -113,8 +112,6 @@ struct Params {
     float courantScale;  // 1/courant when courant is a power of two, else 0
     float kappaf;        // (float)kappa
     bool squareCells;    // dx == dy
-    unsigned long long dxMant;  // dx = dxMant * 2^dxExp, dxMant a 53-bit integer (top bit 52)
-    int dxExp;
     uint32_t flags;
     float* A;          // [3][rows][pitch]  U^n / U^{n+1}: h, hu, hv
     float* B;          // [3][rows][pitch]  U*
@@ -337,7 +334,7 @@ __device__ __forceinline__ double stepDtAt(const Params& P, double t, float maxx
         const float fy = fmaxf(maxy * P.courantScale, P.kappaf);
         if (P.squareCells) {
             const float f = fmaxf(fx, fy);
-            if (!divDF(P.dxMant, P.dxExp, f, &dt)) dt = P.dxd / (double)f;
+            dt = P.dxd / (double)f;
         } else {
             const double cx = P.dxd / (double)fx, cy = P.dyd / (double)fy;
             dt = cx < cy ? cx : cy;
