@@ -242,6 +242,18 @@ int rift_get_table_steps(rift_handle* h, int64_t* table_steps);
 /* Sizes: GridSize (tiles) and the tile grid. */
 int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
 
+/* Host-array access path (no reference counterpart).  Where the device
+ * reads and writes pageable host memory through the host's page tables
+ * (Grace + GB300 over NVLink-C2C: cudaDevAttrPageableMemoryAccess and
+ * ...UsesHostPageTables both 1), rift_set_state converts the caller's FP64
+ * arrays on the device, reading them in place, and rift_get_field writes the
+ * FP64 field straight into the caller's array; the results are bit for bit
+ * those of the staged host path.  On by default where supported;
+ * rift_set_host_access(h, 0) selects the staged path, (h, 1) where the
+ * device cannot returns RIFT_ERR_UNSUPPORTED. */
+int rift_set_host_access(rift_handle* h, int32_t on);
+int rift_get_host_access(rift_handle* h, int32_t* on);
+
 /* Device-side view of a handle's state, for kernels of other libraries that
  * run between steps on the handle's stream (the learned flux closure).  No
  * reference counterpart.  Every plane is FP32 with `pitch` floats per row and

@@ -96,6 +96,9 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                     [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)])
         ns["get_table_steps"] = _sig(lib, p + "get_table_steps", C.c_int,
                                      [_P, C.POINTER(C.c_int64)])
+    if hasattr(lib, p + "set_host_access"):
+        ns["set_host_access"] = _sig(lib, p + "set_host_access", C.c_int, [_P, C.c_int32])
+        ns["get_host_access"] = _sig(lib, p + "get_host_access", C.c_int, [_P, C.POINTER(C.c_int32)])
     if hasattr(lib, p + "get_device_view"):
         ns["get_device_view"] = _sig(lib, p + "get_device_view", C.c_int, [_P, C.POINTER(DeviceView)])
     ns["set_series"] = _sig(lib, p + "set_series", C.c_int, [_P, C.c_int32, _F, _F, C.c_int32])
@@ -302,6 +305,17 @@ class Sim:
         my = np.zeros(self.grid_size)
         self._check(self.f["get_tile_speeds"](self.h, _dp(mx), _dp(my)), "get_tile_speeds")
         return mx, my
+
+    def host_access(self):
+        """True when state uploads and field reads run as device kernels on
+        the caller's host arrays (pageable memory through the host page tables)."""
+        v = C.c_int32()
+        self._check(self.f["get_host_access"](self.h, C.byref(v)), "get_host_access")
+        return bool(v.value)
+
+    def set_host_access(self, on):
+        self._check(self.f["set_host_access"](self.h, 1 if on else 0), "set_host_access")
+        return self
 
     def device_view(self):
         """Device pointers of U^n, the face offsets and n (DeviceView)."""

@@ -106,11 +106,92 @@ struct rift_handle {
     int stepNext = 0;
     bool stepGraphBroken = false;
     bool haveStatic = false, inited = false;
+    // the device reads and writes pageable host memory through the host's
+    // page tables (Grace: NVLink-C2C, address translation services): state
+    // import and field export run as kernels on the caller's arrays
+    bool hostAccessOk = false;  // the device supports it
+    bool hostAccess = false;    // and this handle uses it (rift_set_host_access)
+    double* BrefD = nullptr;  // [ny][nx] FP64 reference elevations (host-access path)
     std::string err;
 
     bool has(uint32_t f) const { return (g.flags & f) != 0; }
     size_t plane() const { return (size_t)rows * pitch; }
 };
+
+// ---------------------------------------------------------------- host access
+// State import straight from the caller's FP64 host arrays, read in place
+// through the host's page tables: the same conversions as the host path
+// (h = float(w - Bref) in FP64, then FP32), without a staging copy.
+__global__ void k_import(const double* __restrict__ w, const double* __restrict__ hu,
+                         const double* __restrict__ hv, const double* __restrict__ F,
+                         const double* __restrict__ Bref, float* __restrict__ A, float* __restrict__ FA,
+                         float* __restrict__ FB, size_t pl, int pitch, int nx, int ny) {
+    const size_t n = (size_t)nx * ny;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(c / (size_t)nx), i = (int)(c % (size_t)nx);
+        const size_t d = (size_t)j * pitch + i;
+        A[d] = __double2float_rn(__dsub_rn(w[c], Bref[c]));
+        A[pl + d] = __double2float_rn(hu[c]);
+        A[2 * pl + d] = __double2float_rn(hv[c]);
+        if (F) {
+            const float f = __double2float_rn(F[c]);
+            FA[d] = f;
+            FB[d] = f;
+        }
+    }
+}
+
+// Ghost cells from host-computed border triples (h, hu, hv): rows 2..ny-3
+// (west pair, east pair), then columns 2..nx-3 (south pair, north pair).
+__global__ void k_ghostsFromBorder(const float* __restrict__ gb, float* __restrict__ A, size_t pl,
+                                   int pitch, int nx, int ny) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nr = ny - 4, nc = nx - 4;
+    auto put = [&](int j, int i, const float* v) {
+        const size_t d = (size_t)j * pitch + i;
+        A[d] = v[0];
+        A[pl + d] = v[1];
+        A[2 * pl + d] = v[2];
+    };
+    if (k < nr) {
+        const int j = k + 2;
+        const float* v = gb + 6 * (size_t)k;
+        put(j, 0, v);
+        put(j, 1, v);
+        put(j, nx - 2, v + 3);
+        put(j, nx - 1, v + 3);
+    } else if (k < nr + nc) {
+        const int i = k - nr + 2;
+        const float* v = gb + 6 * (size_t)nr + 6 * (size_t)(k - nr);
+        put(0, i, v);
+        put(1, i, v);
+        put(ny - 2, i, v + 3);
+        put(ny - 1, i, v + 3);
+    }
+}
+
+// Field export straight into the caller's FP64 host array (row stride ld):
+// mode 0 the value, 1 w = Bref + h, 2 the clamped interior depth map.
+__global__ void k_export(const float* __restrict__ src, const double* __restrict__ Bref,
+                         double* __restrict__ out, size_t ld, int pitch, int nx, int ny, int mode) {
+    const size_t n = (size_t)nx * ny;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n;
+         c += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(c / (size_t)nx), i = (int)(c % (size_t)nx);
+        const float v = src[(size_t)j * pitch + i];
+        double r;
+        if (mode == 1) {
+            r = __dadd_rn(Bref[c], (double)v);
+        } else if (mode == 2) {
+            const bool in = i >= 2 && j >= 2 && i <= nx - 3 && j <= ny - 3;
+            r = in ? (double)((v > kEps) ? v : 0.f) : 0.0;
+        } else {
+            r = (double)v;
+        }
+        out[(size_t)j * ld + i] = r;
+    }
+}
 
 namespace {
 
@@ -463,9 +544,9 @@ int uploadState(rift_handle* h, const float* H, const float* U, const float* V,
                 const std::vector<uint8_t>& activeFlags, const std::vector<int>& inactList) {
     const size_t pl = h->plane();
     int r;
-    if ((r = upField(h, h->A, H)) || (r = upField(h, h->A + pl, U)) ||
-        (r = upField(h, h->A + 2 * pl, V)))
-        return r;
+    if (H && ((r = upField(h, h->A, H)) || (r = upField(h, h->A + pl, U)) ||
+              (r = upField(h, h->A + 2 * pl, V))))
+        return r;  // (H null: U^n is already on the device)
     CUDA_TRY(h, cudaMemcpyAsync(h->B, h->A, 3 * pl * 4, cudaMemcpyDeviceToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->wet, wet.data(), h->gridSize, cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->prevAct, activeFlags.data(), h->gridSize,
@@ -514,6 +595,12 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     if (e != cudaSuccess) return fail(h, RIFT_ERR_CUDA, cudaGetErrorString(e));
     int dev = g->device;
     cudaDeviceGetAttribute(&h->numSMs, cudaDevAttrMultiProcessorCount, dev);
+    {
+        int pageable = 0, hostTables = 0;
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
+        cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+        h->hostAccessOk = h->hostAccess = pageable == 1 && hostTables == 1;
+    }
     CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t pl = h->plane() * 4;
     CUDA_TRY(h, cudaMalloc(&h->A, 3 * pl));
@@ -642,6 +729,11 @@ int rift_upload_static(rift_handle* h, const double* BX, const double* BY, const
         if ((rc = upField(h, h->K, tmp))) return rc;
     }
     h->h0_.assign(h0 ? h0 : nullptr, h0 ? h0 + (size_t)nx * ny : nullptr);
+    if (h->hostAccessOk) {
+        if (!h->BrefD) CUDA_TRY(h, cudaMalloc(&h->BrefD, (size_t)nx * ny * 8));
+        CUDA_TRY(h, cudaMemcpyAsync(h->BrefD, h->Bref.data(), (size_t)nx * ny * 8, cudaMemcpyHostToDevice,
+                                    h->stream));
+    }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     h->haveStatic = true;
     return RIFT_OK;
@@ -1042,6 +1134,19 @@ int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY) {
     return RIFT_OK;
 }
 
+int rift_set_host_access(rift_handle* h, int32_t on) {
+    if (!h) return RIFT_ERR_ARG;
+    if (on && !h->hostAccessOk) return fail(h, RIFT_ERR_UNSUPPORTED, "device cannot access pageable host memory");
+    h->hostAccess = on != 0;
+    return RIFT_OK;
+}
+
+int rift_get_host_access(rift_handle* h, int32_t* on) {
+    if (!h || !on) return RIFT_ERR_ARG;
+    *on = h->hostAccess ? 1 : 0;
+    return RIFT_OK;
+}
+
 int rift_get_device_view(rift_handle* h, rift_device_view* v) {
     if (!h || !v) return RIFT_ERR_ARG;
     if (!h->haveStatic) return fail(h, RIFT_ERR_STATE, "upload the static fields first");
@@ -1069,6 +1174,30 @@ int rift_get_field(rift_handle* h, int32_t which, double* host, size_t ld) {
     const int nx = h->nx, ny = h->ny;
     const size_t pl = h->plane();
     const size_t N = (size_t)nx * ny;
+    if (h->hostAccess) {
+        // written by the device straight into the caller's array
+        const float* src = nullptr;
+        int mode = 0;
+        switch (which) {
+            case RIFT_FIELD_W: src = h->BrefD ? h->A : nullptr; mode = 1; break;
+            case RIFT_FIELD_HU: src = h->A + pl; break;
+            case RIFT_FIELD_HV: src = h->A + 2 * pl; break;
+            case RIFT_FIELD_H: src = h->A; mode = 2; break;
+            case RIFT_FIELD_F: src = h->FA; break;
+            case RIFT_FIELD_HMAX: src = h->hmax; break;
+            case RIFT_FIELD_QMAX: src = h->qmax; break;
+            case RIFT_FIELD_TPEAK: src = h->tpeak; break;
+            case RIFT_FIELD_TDRY: src = h->tdry; break;
+            case RIFT_FIELD_TWET: src = h->twet; break;
+            default: break;
+        }
+        if (src) {
+            k_export<<<h->numSMs * 8, 256, 0, h->stream>>>(src, h->BrefD, host, ld, h->pitch, nx, ny, mode);
+            CUDA_TRY(h, cudaGetLastError());
+            CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+            return RIFT_OK;
+        }
+    }
     float* const a = stagePlanes(h, 4);
     if (!a) return fail(h, RIFT_ERR_NOMEM, "pinned staging planes");
     float* const b = a + N;
@@ -1190,16 +1319,57 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
     if (!H) return fail(h, RIFT_ERR_NOMEM, "pinned staging planes");
     float* const U = H + N;
     float* const V = H + 2 * N;
-    parallelRows(ny, N, [&](int j0, int j1) {
-        for (int j = j0; j < j1; j++)
-            for (int i = 0; i < nx; i++) {
-                size_t c = hidx(h, j, i);
-                H[c] = depthFromW(h, w[c], j, i);
-                U[c] = (float)hu[c];
-                V[c] = (float)hv[c];
+    const bool direct = h->hostAccess && h->BrefD;
+    if (direct) {
+        // U^n (and F) converted on the device from the caller's arrays; the
+        // ghost cells from the border, computed here as hostGhosts does
+        const size_t pl = h->plane();
+        const bool withF = F && h->FA;
+        k_import<<<h->numSMs * 8, 256, 0, h->stream>>>(w, hu, hv, withF ? F : nullptr, h->BrefD, h->A,
+                                                       h->FA, h->FB, pl, h->pitch, nx, ny);
+        CUDA_TRY(h, cudaGetLastError());
+        auto crit = [](float q, float d) { return std::fmin(std::cbrt(q * q / kG), d); };
+        auto cell = [&](int j, int i, float* v) {
+            const size_t c = hidx(h, j, i);
+            v[0] = depthFromW(h, w[c], j, i);
+            v[1] = (float)hu[c];
+            v[2] = (float)hv[c];
+        };
+        float* gb = H;  // 6 (ny-4) + 6 (nx-4) floats of the pinned staging
+        for (int j = 2; j <= ny - 3; j++)
+            for (int side = 0; side < 2; side++) {
+                float v[3];
+                cell(j, side ? nx - 3 : 2, v);
+                float HL = crit(v[1], v[0]);
+                float* o = gb + 6 * (size_t)(j - 2) + 3 * side;
+                o[0] = (HL > kEps) ? HL : 0.f;
+                o[1] = v[1];
+                o[2] = v[2];
             }
-    });
-    hostGhosts(h, H, U, V);
+        for (int i = 2; i <= nx - 3; i++)
+            for (int side = 0; side < 2; side++) {
+                float v[3];
+                cell(side ? ny - 3 : 2, i, v);
+                float* o = gb + 6 * (size_t)(ny - 4) + 6 * (size_t)(i - 2) + 3 * side;
+                o[0] = crit(v[2], v[0]);
+                o[1] = v[1];
+                o[2] = v[2];
+            }
+        const int nb = (ny - 4) + (nx - 4);
+        k_ghostsFromBorder<<<(nb + 255) / 256, 256, 0, h->stream>>>(gb, h->A, pl, h->pitch, nx, ny);
+        CUDA_TRY(h, cudaGetLastError());
+    } else {
+        parallelRows(ny, N, [&](int j0, int j1) {
+            for (int j = j0; j < j1; j++)
+                for (int i = 0; i < nx; i++) {
+                    size_t c = hidx(h, j, i);
+                    H[c] = depthFromW(h, w[c], j, i);
+                    U[c] = (float)hu[c];
+                    V[c] = (float)hv[c];
+                }
+        });
+        hostGhosts(h, H, U, V);
+    }
     std::vector<uint8_t> wetv(h->gridSize), actf(h->gridSize);
     CUDA_TRY(h, cudaMemcpyAsync(wetv.data(), h->wet, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(actf.data(), h->prevAct, h->gridSize, cudaMemcpyDeviceToHost, h->stream));
@@ -1213,8 +1383,11 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
     std::vector<int> inact;
     for (int b = 1; b < h->gridSize; b++)
         if (!actf[b]) inact.push_back(b);
-    if ((rc = uploadState(h, H, U, V, wetv, actf, inact))) return rc;
-    if (F && h->FA) {
+    if ((rc = uploadState(h, direct ? nullptr : H, U, V, wetv, actf, inact))) return rc;
+    if (direct) {
+        // the caller's arrays stay in use until the import kernel is done
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    } else if (F && h->FA) {
         float* const f = H + 3 * N;
         parallelRows(ny, N, [&](int j0, int j1) {
             for (size_t c = (size_t)j0 * nx; c < (size_t)j1 * nx; c++) f[c] = (float)F[c];
@@ -1572,7 +1745,7 @@ void rift_destroy(rift_handle* h) {
                     (void*)h->strips, (void*)h->stripFlag, (void*)h->wet, (void*)h->prevAct,
                     (void*)h->act, (void*)h->deact,
                     (void*)h->inact, (void*)h->srcIdx, (void*)h->srcTileStart,
-                    (void*)h->srcTileList, (void*)h->st, (void*)h->volPartial})
+                    (void*)h->srcTileList, (void*)h->st, (void*)h->volPartial, (void*)h->BrefD})
         if (p) cudaFree(p);
     if (h->hst) cudaFreeHost(h->hst);
     if (h->stage) cudaFreeHost(h->stage);
