@@ -248,9 +248,10 @@ int rift_get_tile_grid(rift_handle* h, int32_t* nBX, int32_t* nBY);
  * ...UsesHostPageTables both 1), rift_set_state converts the caller's FP64
  * arrays on the device, reading them in place, and rift_get_field writes the
  * FP64 field straight into the caller's array; the results are bit for bit
- * those of the staged host path.  On by default where supported;
- * rift_set_host_access(h, 0) selects the staged path, (h, 1) where the
- * device cannot returns RIFT_ERR_UNSUPPORTED. */
+ * those of the staged host path.  Off by default: on GB300 it measured
+ * slower than the staged copies (config 2: 11 ms against 5 ms for one
+ * upload and one depth readback of 2048^2 cells).  rift_set_host_access(h, 1)
+ * turns it on (RIFT_ERR_UNSUPPORTED where the device cannot), (h, 0) off. */
 int rift_set_host_access(rift_handle* h, int32_t on);
 int rift_get_host_access(rift_handle* h, int32_t* on);
 

@@ -108,7 +108,8 @@ struct rift_handle {
     bool haveStatic = false, inited = false;
     // the device reads and writes pageable host memory through the host's
     // page tables (Grace: NVLink-C2C, address translation services): state
-    // import and field export run as kernels on the caller's arrays
+    // import and field export can run as kernels on the caller's arrays
+    // (off by default: slower than the staged copies, measured)
     bool hostAccessOk = false;  // the device supports it
     bool hostAccess = false;    // and this handle uses it (rift_set_host_access)
     double* BrefD = nullptr;  // [ny][nx] FP64 reference elevations (host-access path)
@@ -538,6 +539,15 @@ bool tileInGrid(const rift_handle* h, int b) {
     return i0 < h->nx && j0 < h->ny;
 }
 
+// FP64 reference elevations on the device, for the host-access path.
+int uploadBref(rift_handle* h) {
+    const size_t n = (size_t)h->nx * h->ny;
+    if (!h->BrefD) CUDA_TRY(h, cudaMalloc(&h->BrefD, n * 8));
+    CUDA_TRY(h, cudaMemcpyAsync(h->BrefD, h->Bref.data(), n * 8, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
 // Upload U (A and B), tile flags and lists.
 int uploadState(rift_handle* h, const float* H, const float* U, const float* V,
                 const std::vector<uint8_t>& wet,
@@ -599,7 +609,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
         int pageable = 0, hostTables = 0;
         cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev);
         cudaDeviceGetAttribute(&hostTables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
-        h->hostAccessOk = h->hostAccess = pageable == 1 && hostTables == 1;
+        h->hostAccessOk = pageable == 1 && hostTables == 1;
     }
     CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     const size_t pl = h->plane() * 4;
@@ -729,13 +739,9 @@ int rift_upload_static(rift_handle* h, const double* BX, const double* BY, const
         if ((rc = upField(h, h->K, tmp))) return rc;
     }
     h->h0_.assign(h0 ? h0 : nullptr, h0 ? h0 + (size_t)nx * ny : nullptr);
-    if (h->hostAccessOk) {
-        if (!h->BrefD) CUDA_TRY(h, cudaMalloc(&h->BrefD, (size_t)nx * ny * 8));
-        CUDA_TRY(h, cudaMemcpyAsync(h->BrefD, h->Bref.data(), (size_t)nx * ny * 8, cudaMemcpyHostToDevice,
-                                    h->stream));
-    }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     h->haveStatic = true;
+    if (h->hostAccess && (rc = uploadBref(h))) return rc;
     return RIFT_OK;
 }
 
@@ -1138,6 +1144,7 @@ int rift_set_host_access(rift_handle* h, int32_t on) {
     if (!h) return RIFT_ERR_ARG;
     if (on && !h->hostAccessOk) return fail(h, RIFT_ERR_UNSUPPORTED, "device cannot access pageable host memory");
     h->hostAccess = on != 0;
+    if (h->hostAccess && h->haveStatic) return uploadBref(h);
     return RIFT_OK;
 }
 
