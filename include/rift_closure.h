@@ -106,12 +106,18 @@ int rift_closure_face_flux(const rift_device_view* view, int32_t ratio, float we
  * |c_mass| dtw / (dx h_donor) exceeds tau falls back to the plain solve
  * (no correction).  src: the six input channels on the handle's grid
  * (plane[0..2] = the view's h, hu, hv); corr: four planes of the view's
- * layout (scratch, left holding the applied corrections); counters[0] +=
- * blocks evaluated, counters[1] += blocks fallen back.  Runs on the view's
+ * layout (scratch, left holding the corrections computed per block);
+ * block_fell: one byte per 16 x 16 block of interior cells, row-major over
+ * ceil((h_nx-4)/16) blocks per row (scratch, left holding 1 for the blocks
+ * that fell back).  A face between a block that fell back and one that did
+ * not is not corrected either, so every cell of a block that fell back keeps
+ * the plain solve exactly.  counters[0] += blocks evaluated, counters[1] +=
+ * blocks fallen back.  lim < 0.25 and hmin (1 - 4 lim) > 1.19e-7 m, so that
+ * no wet cell is dried (RIFT_ERR_ARG otherwise).  Runs on the view's
  * stream. */
 int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src,
                        const float* params, const float* oscale_host, float dtw, float hmin,
-                       float lim, float tau, float* corr, int32_t* counters);
+                       float lim, float tau, float* corr, uint8_t* block_fell, int32_t* counters);
 
 const char* rift_closure_last_error(void);
 

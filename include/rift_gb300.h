@@ -107,6 +107,15 @@ int rift_set_uniform_rates(rift_handle* h, double rain_mps, double drain_mps);
 int rift_set_point_sources(rift_handle* h, const int32_t* idx,
                            const double* rate_mps, int32_t n);
 
+/* New rates (m/s per source cell) for the n cells of the last
+ * rift_set_point_sources call, used from the next step on: the device copy of
+ * Simulator::updateSources (simulator.cu:903-907).  The source cells, the
+ * per-tile source lists and the captured step graph are kept.  A hydrograph
+ * series (rift_set_series which = 2) replaces them at the start of each step,
+ * as UpdateSource does in the reference (simulator.cu:502-518).
+ * RIFT_ERR_ARG when n differs from the source count. */
+int rift_set_point_rates(rift_handle* h, const double* rate_mps, int32_t n);
+
 /* Gridded map for the next step (GridSeries::update, GridSeries.cu:144-403).
  * t1map == NULL: hold t0map.  Otherwise the map is
  * InterpGrid(factor, t0map, t1map) (grid.cu:292-311), evaluated on device. */
@@ -307,7 +316,10 @@ int rift_get_device_view(rift_handle* h, rift_device_view* v);
  * the last call's partial sums (each call rewrites every partial it reads);
  * calls that overlap on the GPU race on it and must be serialised by the
  * caller.  The first call on each device looks up the array's address with
- * that device current; make it before recording any stream capture there. */
+ * that device current; make it before recording any stream capture there.
+ * The address is remembered with the id of the context it was found in: the
+ * first call after a cudaDeviceReset (a new primary context) looks it up
+ * again, so make that call outside stream capture too. */
 #define RIFT_NOALLOC_MAX_ROWS 32768
 #define RIFT_ERR_TOO_LARGE 7
 int rift_volume_noalloc(const float* depth, const float* infil, int32_t h_nx,

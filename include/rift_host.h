@@ -114,6 +114,31 @@ int rift_sim_run(rift_sim* s, double t_end, double* t, int64_t* steps);
 int rift_sim_time(rift_sim* s, double* t, double* dt, double* tf);
 /* the engine handle, for direct field access */
 rift_handle* rift_sim_engine(rift_sim* s);
+
+/* ---- 1D-2D coupling hooks (simulator.h:133-137, simulator.cu:720-735,
+ * 858-907) ------------------------------------------------------------------
+ * OpenSimulation(config, flowrate): rift_sim_open, keeping the flow rate the
+ * caller passes (the reference stores it in flow_rate and reads it nowhere
+ * else; rift_sim_flow_rate returns it). */
+int rift_sim_open_flow(const char* config_path, double flow_rate, rift_sim** out);
+int rift_sim_flow_rate(rift_sim* s, double* flow_rate);
+/* NumSources: cells of the point / rectangular source (InitializeSources) */
+int rift_sim_num_sources(rift_sim* s, int32_t* n);
+/* setSourceValue(value): a discharge in m^3/s spread over the source cells,
+ * value / dx / dy / NumSources m/s each; with check_volume, each cell's rate
+ * times the current dt is added to V_added (rift_sim_source_volume).  Takes
+ * effect on the device at rift_sim_update_sources. */
+int rift_sim_set_source_value(rift_sim* s, double value);
+/* updateSources(): the rates to the device for the next step.  With a
+ * hydrograph CSV in the configuration the next step's UpdateSource replaces
+ * them from the hydrograph, as in the reference (simulator.cu:502-518); a
+ * configuration that gives the source location (source_pt, source_X/Y or
+ * source_rect_X/Y) without a hydrograph keeps them: the coupling's own
+ * source. */
+int rift_sim_update_sources(rift_sim* s);
+/* V_added of setSourceValue (m of depth summed over cells x s; times dx dy
+ * for m^3): the reference's check_volume bookkeeping of the set rates */
+int rift_sim_source_volume(rift_sim* s, double* v_added);
 /* CloseSimulation: summary maps, then frees everything */
 int rift_sim_close(rift_sim* s);
 const char* rift_sim_last_error(rift_sim* s);

@@ -18,7 +18,12 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 BIN = os.path.join(HERE, "_bin")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_TREE = "/root/reference"  # read-only reference sources (build container only)
+# Read-only reference sources, present only where the fatbin is built: the
+# RIFT_REFERENCE_TREE environment variable, else a "reference" directory beside
+# this repository's root.
+REFERENCE_TREE = os.environ.get(
+    "RIFT_REFERENCE_TREE",
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -334,17 +334,34 @@ int main(int argc, char** argv) {
     loadMap(mrain, "rain", rain, rain0, rain1);
     loadMap(mdrain, "drain", drain, drain0, drain1);
     loadMap(msurge, "surge", surge, surge0, surge1);
+    // Interpolated maps: a fixed factor, or (map_times_<name> "t0 t1") the
+    // factor (t - t0) / (t1 - t0) of InterpolatedGridSeries::update
+    // (GridSeries.cu:393-398), evaluated with the time reached after each step
+    // (simulator.cu:819-828) and at the start (simulator.cu:352-370).
+    auto mapTimes = [&](const char* name, double& a, double& b) {
+        std::string k = std::string("map_times_") + name;
+        if (!P.count(k)) return false;
+        std::istringstream ss(P[k]);
+        ss >> a >> b;
+        return b > a;
+    };
+    double trn0 = 0, trn1 = 0, tdr0 = 0, tdr1 = 0, tsg0 = 0, tsg1 = 0;
+    const bool timedRain = mapTimes("rain", trn0, trn1), timedDrain = mapTimes("drain", tdr0, tdr1),
+               timedSurge = mapTimes("surge", tsg0, tsg1);
+    double tNow = getd("t0", 0.0);
     auto interpMaps = [&]() {
         auto one = [&](int m, double f, double* t0, double* t1, double* cur) {
             if (m != 2) return;
             void* a[] = {&f, &pitch, &t0, &t1, &cur};
             CK(cuLaunchKernel(kInterp, GridDim.x, GridDim.y, 1, BC_, BR_, 1, 0, 0, a, 0));
         };
+        if (timedRain) frain = (tNow - trn0) / (trn1 - trn0);
+        if (timedDrain) fdrain = (tNow - tdr0) / (tdr1 - tdr0);
+        if (timedSurge) fsurge = (tNow - tsg0) / (tsg1 - tsg0);
         one(mrain, frain, rain0, rain1, rain);
         one(mdrain, fdrain, drain0, drain1, drain);
         one(msurge, fsurge, surge0, surge1, surge);
     };
-    interpMaps();
 
     // sources
     int nsrc = (int)geti("nsrc", 0);
@@ -412,6 +429,8 @@ int main(int argc, char** argv) {
         CR(cudaMemcpy(my, m2.data(), GridSize * 8, cudaMemcpyHostToDevice));
         applyBC();
     }
+    tNow = t;
+    interpMaps();
     double rainRate = rainRateFixed, drainRate = drainRateFixed;
     long numSources = nsrc;
     if (nsrc > 0) CR(cudaMemcpy(srcIdx, srcIdxH.data(), nsrc * 4, cudaMemcpyHostToDevice));
@@ -433,7 +452,7 @@ int main(int argc, char** argv) {
             dl(q_max, "qmax");
         }
         if (saveArr) dl(t_wet, "twet");
-        dl(BCd, "BC");
+        if (geti("dump_bc", 1)) dl(BCd, "BC");
         std::vector<unsigned char> wb(GridSize);
         CR(cudaMemcpy(wb.data(), wet_blocks, GridSize, cudaMemcpyDeviceToHost));
         writeBin(out + pre + "wet.bin", wb.data(), GridSize);
@@ -453,14 +472,9 @@ int main(int argc, char** argv) {
     if (std::find(dumps.begin(), dumps.end(), 0) != dumps.end()) dump(0);
 
     FILE* log = std::fopen((out + "/steps.txt").c_str(), "w");
-    cudaEvent_t e0, e1;
-    CR(cudaEventCreate(&e0));
-    CR(cudaEventCreate(&e1));
-    CR(cudaDeviceSynchronize());
-    auto wall0 = std::chrono::steady_clock::now();
-    CR(cudaEventRecord(e0));
     long cellsActive = 0;
-    for (int step = 1; step <= nsteps; step++) {
+    // One step in the order of Simulator::RunSimulation (simulator.cu:773-853).
+    auto doStep = [&]() {
         // UpdateSource (simulator.cu:500-538)
         if (dambreak || rainU || drainU) {
             if (nsrc > 0) CR(cudaMemcpy(srcIdx, srcIdxH.data(), nsrc * 4, cudaMemcpyHostToDevice));
@@ -545,7 +559,23 @@ int main(int argc, char** argv) {
             CK(cuLaunchKernel(kInt2, nBlocks, 1, 1, BC_, BR_, 1, 0, 0, a, 0));
             applyBC();
         }
-        interpMaps();  // GridSeries::update (fixed factors here)
+        tNow = t;
+        interpMaps();  // GridSeries::update
+    };
+    // Spin-up / logged part: nsteps steps, or fewer when t reaches t_stop.
+    const double tStop = getd("t_stop", 1e300);
+    const bool dumpFinal = geti("dump_final", 0) != 0;
+    const int timedSteps = (int)geti("timed_steps", 0);
+    cudaEvent_t e0, e1;
+    CR(cudaEventCreate(&e0));
+    CR(cudaEventCreate(&e1));
+    CR(cudaDeviceSynchronize());
+    auto wall0 = std::chrono::steady_clock::now();
+    CR(cudaEventRecord(e0));
+    int step = 0;
+    while (step < nsteps && t < tStop) {
+        step++;
+        doStep();
         if (!timing) {
             std::fprintf(log, "%d %.17g %.17g %d\n", step, t, dt, nBlocks);
             if (std::find(dumps.begin(), dumps.end(), step) != dumps.end()) dump(step);
@@ -558,10 +588,41 @@ int main(int argc, char** argv) {
     CR(cudaEventElapsedTime(&ms, e0, e1));
     double wall = std::chrono::duration<double>(wall1 - wall0).count();
     std::fclose(log);
+    const int stepsRun = step;
+    if (dumpFinal) dump(stepsRun);
+    const double tSpin = t;
+    // Timed part: timed_steps more steps after the spin-up, CUDA events on
+    // the legacy stream around them and the host clock around the loop
+    // (thrust's host synchronisations of every step included, as in the
+    // reference's main loop).
+    float msTimed = 0.f;
+    double wallTimed = 0.0;
+    long cellsTimed = 0;
+    if (timedSteps > 0) {
+        const long c0 = cellsActive;
+        CR(cudaDeviceSynchronize());
+        auto w0 = std::chrono::steady_clock::now();
+        CR(cudaEventRecord(e0));
+        for (int k = 0; k < timedSteps; k++) doStep();
+        CR(cudaEventRecord(e1));
+        CR(cudaEventSynchronize(e1));
+        wallTimed = std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
+        CR(cudaEventElapsedTime(&msTimed, e0, e1));
+        cellsTimed = cellsActive - c0;
+    }
     long interior = (long)(nx - 4) * (ny - 4);
-    std::printf(
-        "{\"steps\": %d, \"t\": %.9g, \"dt\": %.9g, \"gpu_ms\": %.4f, \"wall_s\": %.6f, "
-        "\"domain_cell_updates_per_s\": %.6g, \"active_tile_cells\": %ld, \"n_active_last\": %d}\n",
-        nsteps, t, dt, ms, wall, (double)interior * nsteps / wall, cellsActive, nBlocks);
+    if (timedSteps > 0) {
+        std::printf(
+            "{\"steps\": %d, \"t\": %.9g, \"dt\": %.9g, \"spinup_steps\": %d, \"t_spinup\": %.9g, "
+            "\"spinup_wall_s\": %.3f, \"gpu_ms\": %.4f, \"wall_s\": %.6f, "
+            "\"domain_cell_updates_per_s\": %.6g, \"active_tile_cells\": %ld, \"n_active_last\": %d}\n",
+            timedSteps, t, dt, stepsRun, tSpin, wall, msTimed, wallTimed,
+            (double)interior * timedSteps / wallTimed, cellsTimed, nBlocks);
+    } else {
+        std::printf(
+            "{\"steps\": %d, \"t\": %.9g, \"dt\": %.9g, \"gpu_ms\": %.4f, \"wall_s\": %.6f, "
+            "\"domain_cell_updates_per_s\": %.6g, \"active_tile_cells\": %ld, \"n_active_last\": %d}\n",
+            stepsRun, t, dt, ms, wall, (double)interior * stepsRun / wall, cellsActive, nBlocks);
+    }
     return 0;
 }

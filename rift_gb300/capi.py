@@ -79,6 +79,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
     ns["set_map_factor"] = _sig(lib, p + "set_map_factor", C.c_int, [_P, C.c_int32, C.c_double])
     ns["set_map_times"] = _sig(lib, p + "set_map_times", C.c_int,
                                [_P, C.c_int32, C.c_double, C.c_double])
+    if hasattr(lib, p + "set_point_rates"):
+        ns["set_point_rates"] = _sig(lib, p + "set_point_rates", C.c_int, [_P, _D, C.c_int32])
     if hasattr(lib, p + "set_schedule"):
         ns["set_schedule"] = _sig(lib, p + "set_schedule", C.c_int, [_P, C.c_int32])
     if hasattr(lib, p + "ensemble_create"):

@@ -65,7 +65,7 @@ def load():
             "rift_closure_adam": [P, P, P, P, I, F, F, F, F, F, F, P],
             "rift_closure_face_flux": [C.POINTER(capi.DeviceView), I, F, P, I, I, I, I],
             "rift_closure_apply": [C.POINTER(capi.DeviceView), C.POINTER(Src), P,
-                                   C.POINTER(C.c_float), F, F, F, F, P, P],
+                                   C.POINTER(C.c_float), F, F, F, F, P, P, P],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
@@ -125,11 +125,18 @@ def torch_forward(x, p):
     layer-1 window's centre cell.  Output (S, 4, H-6, W-6)."""
     torch = _torch()
     F = torch.nn.functional
-    W1, b1, W2, b2, W3, b3 = unpack(p.to(x.device))
-    z1 = F.conv2d(x, W1) - x[:, 3:4, 2:-2, 2:-2] * W1[:, 3].sum(dim=(1, 2)).view(1, -1, 1, 1)
-    a1 = torch.relu(z1 + b1.view(1, -1, 1, 1))
-    a2 = torch.relu(F.conv2d(a1, W2) + b2.view(1, -1, 1, 1))
-    return F.conv2d(a2, W3) + b3.view(1, -1, 1, 1)
+    # true FP32: PyTorch's defaults let cuDNN convolutions run on TF32
+    prev = (torch.backends.cudnn.allow_tf32, torch.backends.cuda.matmul.allow_tf32)
+    torch.backends.cudnn.allow_tf32 = False
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        W1, b1, W2, b2, W3, b3 = unpack(p.to(x.device))
+        z1 = F.conv2d(x, W1) - x[:, 3:4, 2:-2, 2:-2] * W1[:, 3].sum(dim=(1, 2)).view(1, -1, 1, 1)
+        a1 = torch.relu(z1 + b1.view(1, -1, 1, 1))
+        a2 = torch.relu(F.conv2d(a1, W2) + b2.view(1, -1, 1, 1))
+        return F.conv2d(a2, W3) + b3.view(1, -1, 1, 1)
+    finally:
+        torch.backends.cudnn.allow_tf32, torch.backends.cuda.matmul.allow_tf32 = prev
 
 
 # ------------------------------------------------------------ device calls
@@ -468,6 +475,8 @@ class ClosureRun:
         self.nman[:ny, :nx] = torch.as_tensor(n[jj][:, ii], dtype=torch.float32)
         self.params = torch.as_tensor(model.params, device="cuda")
         self.corr = torch.zeros((4, rows, pitch), device="cuda", dtype=torch.float32)
+        nb = -(-(v.h_nx - 4) // 16) * -(-(v.h_ny - 4) // 16)
+        self.fell = torch.zeros(nb, device="cuda", dtype=torch.uint8)
         self.counters = torch.zeros(2, device="cuda", dtype=torch.int32)
         # gain: strength of each correction (east mass, east x momentum,
         # north mass, north y momentum), multiplying the output scales
@@ -493,7 +502,8 @@ class ClosureRun:
         src = self._src(uniform_rate(self.sim.case, t))
         _check(load().rift_closure_apply(C.byref(self.view), C.byref(src), self.params.data_ptr(),
                                          self.osc, float(dtw), self.hmin, self.lim, self.tau,
-                                         self.corr.data_ptr(), self.counters.data_ptr()),
+                                         self.corr.data_ptr(), self.fell.data_ptr(),
+                                         self.counters.data_ptr()),
                "rift_closure_apply")
         self.applies += 1
 

@@ -727,6 +727,7 @@ struct ApplyArgs {
     size_t plane;
     int pitch, nx, ny;
     float dtw, inv_dx, inv_dy, hmin, lim, tau;
+    uint8_t* fell;  // per 16 x 16 block: 1 when it fell back to the plain solve
     int* counters;
 };
 
@@ -752,6 +753,7 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
             wet |= S.xs[(ry * RI + rx) * CIN] > hminS;
         }
         if (!__syncthreads_or(wet)) {
+            if (tid == 0) A.fell[tile] = 0;
             for (int i = tid; i < OT * OT; i += NT) {
                 int y = G.Y + i / OT, x = G.X + i % OT;
                 if (y - src.oy0 >= src.OH || x - src.ox0 >= src.OW) continue;
@@ -809,6 +811,7 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
                 }
         }
         if (tid == 0) {
+            A.fell[tile] = fallback ? 1 : 0;
             atomicAdd(&A.counters[0], 1);
             if (fallback) atomicAdd(&A.counters[1], 1);
         }
@@ -816,17 +819,29 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
 }
 
 // U^n -= dtw x divergence of the face corrections (cells one inside the
-// ghost ring and beyond).
+// ghost ring and beyond).  A face is corrected only when neither of the
+// 16 x 16 blocks of its two cells fell back: both cells then see the same
+// correction (mass stays conserved) and every cell of a fallen-back block
+// keeps the plain solve exactly.
 __global__ void k_apply(float* __restrict__ h, float* __restrict__ hu, float* __restrict__ hv,
-                        const float* __restrict__ corr, size_t plane, int pitch, int nx, int ny,
-                        float sx, float sy) {
+                        const float* __restrict__ corr, const uint8_t* __restrict__ fell, size_t plane,
+                        int pitch, int nx, int ny, float sx, float sy) {
     const int i = 3 + blockIdx.x * blockDim.x + threadIdx.x;
     const int j = 3 + blockIdx.y * blockDim.y + threadIdx.y;
     if (i > nx - 4 || j > ny - 4) return;
+    const int tx = (nx - 4 + OT - 1) / OT;
+    const int bx = (i - 2) / OT, by = (j - 2) / OT;
+    const bool own = fell[by * tx + bx] != 0;
+    if (own) return;  // every face of this cell touches its own block
+    const bool westOff = ((i - 2) % OT == 0) && fell[by * tx + bx - 1];
+    const bool eastOff = ((i - 1) % OT == 0) && (i + 1 <= nx - 3) && fell[by * tx + bx + 1];
+    const bool southOff = ((j - 2) % OT == 0) && fell[(by - 1) * tx + bx];
+    const bool northOff = ((j - 1) % OT == 0) && (j + 1 <= ny - 3) && fell[(by + 1) * tx + bx];
     const size_t c = (size_t)j * pitch + i;
-    const float mE = corr[c], mW = corr[c - 1], mN = corr[2 * plane + c], mS = corr[2 * plane + c - pitch];
-    const float uE = corr[plane + c], uW = corr[plane + c - 1];
-    const float vN = corr[3 * plane + c], vS = corr[3 * plane + c - pitch];
+    const float mE = eastOff ? 0.f : corr[c], mW = westOff ? 0.f : corr[c - 1];
+    const float mN = northOff ? 0.f : corr[2 * plane + c], mS = southOff ? 0.f : corr[2 * plane + c - pitch];
+    const float uE = eastOff ? 0.f : corr[plane + c], uW = westOff ? 0.f : corr[plane + c - 1];
+    const float vN = northOff ? 0.f : corr[3 * plane + c], vS = southOff ? 0.f : corr[3 * plane + c - pitch];
     if (mE == 0.f && mW == 0.f && mN == 0.f && mS == 0.f && uE == 0.f && uW == 0.f && vN == 0.f &&
         vS == 0.f)
         return;
@@ -923,10 +938,15 @@ int rift_closure_face_flux(const rift_device_view* view, int32_t ratio, float we
 
 int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src, const float* params,
                        const float* oscale_host, float dtw, float hmin, float lim, float tau, float* corr,
-                       int32_t* counters) {
-    if (!view || !srcOk(src) || !params || !oscale_host || !corr || !counters || !(hmin > 0.f) ||
-        !(lim > 0.f) || !(src->scale[0] > 0.f) || src->samples != 1)
+                       uint8_t* block_fell, int32_t* counters) {
+    if (!view || !srcOk(src) || !params || !oscale_host || !corr || !block_fell || !counters ||
+        !(hmin > 0.f) || !(lim > 0.f) || !(src->scale[0] > 0.f) || src->samples != 1)
         return fail(RIFT_ERR_ARG, "rift_closure_apply: bad argument");
+    // Each of a cell's four faces may carry up to lim x its depth out of it:
+    // a cell deeper than hmin keeps at least hmin (1 - 4 lim), which must stay
+    // above the wet threshold so that no wet cell is dried.
+    if (!(lim < 0.25f) || !(hmin * (1.f - 4.f * lim) > 1.19209e-07f))
+        return fail(RIFT_ERR_ARG, "rift_closure_apply: lim must be < 0.25 and hmin (1 - 4 lim) > 1.19e-7 m");
     if (src->H != view->h_ny || src->W != view->h_nx || src->pitch != view->pitch || src->oy0 != 2 ||
         src->ox0 != 2 || src->OH != view->h_ny - 4 || src->OW != view->h_nx - 4)
         return fail(RIFT_ERR_ARG, "rift_closure_apply: src is not the view's interior");
@@ -947,6 +967,7 @@ int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src
     A.hmin = hmin;
     A.lim = lim;
     A.tau = tau;
+    A.fell = block_fell;
     A.counters = counters;
     const size_t smem = sizeof(rc::NetSmem);
     const int tiles = rc::tileCount(*src);
@@ -955,8 +976,8 @@ int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src
     rc::k_closure<<<grid, rc::NT, smem, st>>>(A);
     if ((rc_ = launched("k_closure"))) return rc_;
     dim3 blk(32, 8), grd((view->h_nx - 6 + 31) / 32, (view->h_ny - 6 + 7) / 8);
-    rc::k_apply<<<grd, blk, 0, st>>>(view->h, view->hu, view->hv, corr, A.plane, view->pitch, view->h_nx,
-                                     view->h_ny, (float)(dtw / view->dx), (float)(dtw / view->dy));
+    rc::k_apply<<<grd, blk, 0, st>>>(view->h, view->hu, view->hv, corr, block_fell, A.plane, view->pitch,
+                                     view->h_nx, view->h_ny, (float)(dtw / view->dx), (float)(dtw / view->dy));
     return launched("k_apply");
 }
 

@@ -830,6 +830,20 @@ int rift_set_uniform_rates(rift_handle* h, double rain_mps, double drain_mps) {
     return pushState(h);
 }
 
+// Simulator::updateSources (simulator.cu:903-907): the per-source rates of
+// the cells rift_set_point_sources placed, copied to the device before the
+// next step; the cells, their tile lists and the captured step graph stay.
+int rift_set_point_rates(rift_handle* h, const double* rate, int32_t n) {
+    if (!h || n < 0 || (n > 0 && !rate)) return RIFT_ERR_ARG;
+    if (n != h->nsrc) return fail(h, RIFT_ERR_ARG, "rate count differs from the source count");
+    if (n == 0) return RIFT_OK;
+    std::vector<float> fr(n);
+    for (int k = 0; k < n; k++) fr[k] = (float)rate[k];
+    CUDA_TRY(h, cudaMemcpyAsync(h->srcRate, fr.data(), (size_t)n * 4, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return RIFT_OK;
+}
+
 int rift_set_point_sources(rift_handle* h, const int32_t* idx, const double* rate, int32_t n) {
     if (!h || n < 0 || (n > 0 && (!idx || !rate))) return RIFT_ERR_ARG;
     cudaFree(h->srcIdx);
@@ -1327,9 +1341,19 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
     float* const U = H + N;
     float* const V = H + 2 * N;
     const bool direct = h->hostAccess && h->BrefD;
+    // Once the import kernel reads the caller's arrays, every exit (the error
+    // returns included) waits for the stream, so the caller may free them.
+    struct SyncOnExit {
+        cudaStream_t s;
+        bool armed;
+        ~SyncOnExit() {
+            if (armed) cudaStreamSynchronize(s);
+        }
+    } guard{h->stream, false};
     if (direct) {
         // U^n (and F) converted on the device from the caller's arrays; the
         // ghost cells from the border, computed here as hostGhosts does
+        guard.armed = true;
         const size_t pl = h->plane();
         const bool withF = F && h->FA;
         k_import<<<h->numSMs * 8, 256, 0, h->stream>>>(w, hu, hv, withF ? F : nullptr, h->BrefD, h->A,
@@ -1785,7 +1809,11 @@ void rift_destroy(rift_handle* h) {
 //    other's partials: the caller serialises them;
 //  - the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current; make that first call
-//    before recording any stream capture on the device.
+//    before recording any stream capture on the device.  The address is kept
+//    per device together with the id of the context it was looked up in; a
+//    call from another context (after cudaDeviceReset the device's primary
+//    context is a new one, and the module may load at a new address) looks
+//    it up again before launching.
 namespace {
 
 constexpr int kNoAllocMaxRows = RIFT_NOALLOC_MAX_ROWS;
@@ -1794,6 +1822,33 @@ static __device__ __align__(256) double g_noallocRowSums[2 * kNoAllocMaxRows];
 constexpr int kMaxDevices = 64;
 std::mutex g_noallocMutex;
 double* g_noallocPtr[kMaxDevices] = {nullptr};
+unsigned long long g_noallocCtx[kMaxDevices] = {0};
+
+// Id of the calling thread's current context (cuCtxGetCurrent + cuCtxGetId,
+// reached through the runtime's driver entry points); 0 when unavailable.
+unsigned long long currentContextId() {
+    using GetCur = CUresult (*)(CUcontext*);
+    using GetId = CUresult (*)(CUcontext, unsigned long long*);
+    static GetCur getCur = nullptr;
+    static GetId getId = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            getCur = reinterpret_cast<GetCur>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            getId = reinterpret_cast<GetId>(p);
+    });
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!getCur || !getId || getCur(&ctx) != CUDA_SUCCESS || !ctx || getId(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
 
 // One warp per interior row: Neumaier sum of (h [+ F]) over the row's
 // interior cells, lanes combined in lane order.
@@ -1825,18 +1880,35 @@ __global__ void k_volume_rows_noalloc(const float* __restrict__ h, const float* 
     }
 }
 
-// Rows combined in row order into the caller's output.
+// Rows combined into the caller's output by one warp: lane l sums the
+// contiguous block of rows [2 + l*chunk, 2 + (l+1)*chunk) in row order, then
+// the 32 lane sums are combined in lane order, so the result does not depend
+// on timing.
 __global__ void k_volume_final_noalloc(const double* rows, int ny, double* out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double S = 0.0, C = 0.0;
-    for (int j = 2; j <= ny - 3; j++) {
-        double v = rows[2 * j];
-        double t = S + v;
-        C += (fabs(S) >= fabs(v)) ? (S - t) + v : (v - t) + S;
-        S = t;
-        C += rows[2 * j + 1];
+    if (blockIdx.x != 0) return;
+    const int lane = threadIdx.x & 31;
+    const int nrows = ny - 4;
+    const int chunk = (nrows + 31) / 32;
+    const int j0 = 2 + lane * chunk;
+    const int j1 = min(j0 + chunk, ny - 2);
+    double s = 0.0, c = 0.0;
+    for (int j = j0; j < j1; j++) {
+        const double v = rows[2 * j];
+        const double t = s + v;
+        c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
+        s = t;
+        c += rows[2 * j + 1];
     }
-    out[0] = S + C;
+    double S = 0.0, C = 0.0;
+    for (int l = 0; l < 32; l++) {
+        const double vs = __shfl_sync(0xffffffffu, s, l);
+        const double vc = __shfl_sync(0xffffffffu, c, l);
+        const double t = S + vs;
+        C += (fabs(S) >= fabs(vs)) ? (S - t) + vs : (vs - t) + S;
+        S = t;
+        C += vc;
+    }
+    if (lane == 0) out[0] = S + C;
 }
 
 }  // namespace
@@ -1849,12 +1921,14 @@ extern "C" int rift_volume_noalloc(const float* depth, const float* infil, int32
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return RIFT_ERR_CUDA;
     double* rows = nullptr;
     {
+        const unsigned long long ctx = currentContextId();
         std::lock_guard<std::mutex> lock(g_noallocMutex);
-        if (!g_noallocPtr[dev]) {
+        if (!g_noallocPtr[dev] || ctx == 0 || g_noallocCtx[dev] != ctx) {
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_noallocRowSums) != cudaSuccess || !p)
                 return RIFT_ERR_CUDA;
             g_noallocPtr[dev] = static_cast<double*>(p);
+            g_noallocCtx[dev] = ctx;
         }
         rows = g_noallocPtr[dev];
     }

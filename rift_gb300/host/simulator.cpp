@@ -41,6 +41,10 @@ struct Simulator {
     bool save_hotstart = false, b_print = false, n_print = false, tile_acceleration = true;
     bool square_cells = true, projected = false;
     double source_X[2] = {0, 0}, source_Y[2] = {0, 0};  // (real, imag) of std::complex
+    bool coupled_source = false;      // source cells whose rate the caller sets
+    double flow_rate = 0.0;           // OpenSimulation's flowrate argument
+    std::vector<double> source_rate;  // m/s per source cell (setSourceValue)
+    double V_added = 0.0;             // setSourceValue's check_volume bookkeeping
     int device = 0, count_print = 0;
     long long count = 0;
     std::vector<float> hyeT, hyeR, drnT, drnR, hydT, hydR;
@@ -66,6 +70,8 @@ struct Simulator {
     int readUserParams(const std::string& path);
     int initSimulation();
     int openSimulation(const std::string& path);
+    void setSourceValue(double value);
+    int updateSources();
     int events();
     int runSimulation();
     int run(double tEnd, long long* steps);
@@ -118,10 +124,16 @@ int Simulator::readUserParams(const std::string& path) {
     h_init = cfg.has("h0");
     if (h_init && (rc = cfg.getString("h0", h_file))) return rc;
     dambreak = cfg.has("hydrograph");
-    if (dambreak) {
-        if ((rc = cfg.getString("hydrograph", hydrograph_file)) ||
-            (rc = readCsv(hydrograph_file, hydT, hydR)))
-            return rc;
+    // A source location without a hydrograph CSV: the source of a 1D-2D
+    // coupling, whose rate the caller sets (setSourceValue / updateSources).
+    // The reference reads the location only with a hydrograph and would leave
+    // such a source without cells.
+    coupled_source = !dambreak && (cfg.has("source_rect_X") || cfg.has("source_pt") ||
+                                   (cfg.has("source_X") && cfg.has("source_Y")));
+    if (dambreak && ((rc = cfg.getString("hydrograph", hydrograph_file)) ||
+                     (rc = readCsv(hydrograph_file, hydT, hydR))))
+        return rc;
+    if (dambreak || coupled_source) {
         if (cfg.has("source_rect_X")) {
             if ((rc = cfg.getComplex("source_rect_X", source_X[0], source_X[1])) ||
                 (rc = cfg.getComplex("source_rect_Y", source_Y[0], source_Y[1])))
@@ -215,7 +227,7 @@ int Simulator::initSimulation() {
     // InitializeSources (simulator.cu:858-885): Coord2Index, whose cell is
     // 2 cells west / south of the coordinate; its ok flag is not checked
     source_idx.clear();
-    if (dambreak) {
+    if (dambreak || coupled_source) {
         int imin, jmin, imax, jmax;
         coord2Index(gc, source_X[0], source_Y[0], imin, jmin);
         coord2Index(gc, source_X[1], source_Y[1], imax, jmax);
@@ -275,7 +287,8 @@ int Simulator::initSimulation() {
               (infiltration ? RIFT_F_INFILTRATION : 0) | (surge_gridded ? RIFT_F_SURGE_GRID : 0) |
               (euler_integration ? RIFT_F_EULER : 0) | (save_max ? RIFT_F_SAVE_MAX : 0) |
               (save_arrival_time ? RIFT_F_SAVE_ARRIVAL : 0) |
-              (tile_acceleration ? RIFT_F_TILE_ACCEL : 0) | (dambreak ? RIFT_F_POINT_SOURCE : 0) |
+              (tile_acceleration ? RIFT_F_TILE_ACCEL : 0) |
+              ((dambreak || coupled_source) ? RIFT_F_POINT_SOURCE : 0) |
               (h_init ? RIFT_F_H_INIT : 0);
     g.device = device;
     if ((rc = rift_create(&g, &R))) return engineFail(rc, "rift_create");
@@ -287,12 +300,12 @@ int Simulator::initSimulation() {
         return engineFail(rc, "hyetograph");
     if (drain_averaged && (rc = rift_set_series(R, 1, drnT.data(), drnR.data(), (int32_t)drnT.size())))
         return engineFail(rc, "drain");
-    if (dambreak) {
-        std::vector<double> zero(source_idx.size(), 0.0);
-        if ((rc = rift_set_point_sources(R, source_idx.data(), zero.data(),
+    source_rate.assign(source_idx.size(), 0.0);
+    if (dambreak || coupled_source) {
+        if ((rc = rift_set_point_sources(R, source_idx.data(), source_rate.data(),
                                          (int32_t)source_idx.size())) ||
-            (rc = rift_set_series(R, 2, hydT.data(), hydR.data(), (int32_t)hydT.size())))
-            return engineFail(rc, "hydrograph");
+            (dambreak && (rc = rift_set_series(R, 2, hydT.data(), hydR.data(), (int32_t)hydT.size()))))
+            return engineFail(rc, "point sources");
     }
     // gridded series at t0 (simulator.cu:329-365)
     const double rainScale = 1.0 / 3600.0 / 1000.0;
@@ -335,6 +348,23 @@ int Simulator::openSimulation(const std::string& path) {
     count = 0;
     start = std::chrono::steady_clock::now();
     return RIFT_OK;
+}
+
+// Simulator::setSourceValue (simulator.cu:891-901): a discharge in m^3/s
+// spread over the source cells, as m/s of depth per cell; with check_volume
+// each cell's rate times the current dt is added to V_added.
+void Simulator::setSourceValue(double value) {
+    const size_t n = source_idx.size();
+    for (size_t k = 0; k < n; k++) {
+        source_rate[k] = value / gc.h_dx / gc.h_dy / (double)n;
+        if (check_volume) V_added += source_rate[k] * dt;
+    }
+}
+
+// Simulator::updateSources (simulator.cu:903-907): the rates to the device.
+int Simulator::updateSources() {
+    int rc = rift_set_point_rates(R, source_rate.data(), (int32_t)source_rate.size());
+    return rc ? engineFail(rc, "updateSources") : RIFT_OK;
 }
 
 // The host part of RunSimulation after a step (simulator.cu:819-849): map
@@ -532,9 +562,14 @@ struct rift_sim {
 extern "C" {
 
 int rift_sim_open(const char* config_path, rift_sim** out) {
+    return rift_sim_open_flow(config_path, 0.0, out);
+}
+
+int rift_sim_open_flow(const char* config_path, double flow_rate, rift_sim** out) {
     if (!config_path || !out) return RIFT_ERR_ARG;
     *out = nullptr;
     rift_sim* s = new rift_sim();
+    s->s.flow_rate = flow_rate;
     int rc = s->s.openSimulation(config_path);
     if (rc) {  // the message stays readable through rift_host_last_error()
         delete s;
@@ -571,6 +606,37 @@ int rift_sim_time(rift_sim* s, double* t, double* dt, double* tf) {
 }
 
 rift_handle* rift_sim_engine(rift_sim* s) { return s ? s->s.R : nullptr; }
+
+int rift_sim_flow_rate(rift_sim* s, double* flow_rate) {
+    if (!s || !flow_rate) return RIFT_ERR_ARG;
+    *flow_rate = s->s.flow_rate;
+    return RIFT_OK;
+}
+
+int rift_sim_num_sources(rift_sim* s, int32_t* n) {
+    if (!s || !n) return RIFT_ERR_ARG;
+    *n = (int32_t)s->s.source_idx.size();
+    return RIFT_OK;
+}
+
+int rift_sim_set_source_value(rift_sim* s, double value) {
+    if (!s || !s->s.R) return RIFT_ERR_STATE;
+    s->s.setSourceValue(value);
+    return RIFT_OK;
+}
+
+int rift_sim_update_sources(rift_sim* s) {
+    if (!s || !s->s.R) return RIFT_ERR_STATE;
+    int rc = s->s.updateSources();
+    if (rc) s->s.err = rift_host::g_err;
+    return rc;
+}
+
+int rift_sim_source_volume(rift_sim* s, double* v_added) {
+    if (!s || !v_added) return RIFT_ERR_ARG;
+    *v_added = s->s.V_added;
+    return RIFT_OK;
+}
 
 int rift_sim_close(rift_sim* s) {
     if (!s) return RIFT_ERR_ARG;

@@ -176,19 +176,27 @@ def config1(N=512, seed=0, cell=10.0, rim=True, tf=3600.0) -> Case:
                 flags=RAIN_UNIFORM | TILE_ACCEL, series={0: (t, r)})
 
 
+def _fft_len(n):
+    """Smallest FFT length >= n with only small prime factors."""
+    import scipy.fft as sf
+    return sf.next_fast_len(int(n))
+
+
 def fractal_surface(N, hurst, relief, rng):
-    """Spectral (1/f^(H+1)) random surface on an (N+1)^2 corner grid."""
+    """Spectral (1/f^(H+1)) random surface on an (N+1)^2 corner grid: the
+    field is synthesised on a periodic grid of a fast FFT length >= N+1 and
+    cropped to the corner grid."""
+    import scipy.fft as sf
     M = N + 1
-    kx = np.fft.fftfreq(M)
-    ky = np.fft.fftfreq(M)
-    KX, KY = np.meshgrid(kx, ky)
-    k = np.sqrt(KX ** 2 + KY ** 2)
+    L = _fft_len(M)
+    kx = np.fft.fftfreq(L)
+    k = np.sqrt(kx[None, :] ** 2 + kx[:, None] ** 2)
     k[0, 0] = 1.0
     amp = k ** (-(hurst + 1.0))
     amp[0, 0] = 0.0
-    phase = rng.uniform(0, 2 * np.pi, size=(M, M))
+    phase = rng.uniform(0, 2 * np.pi, size=(L, L))
     spec = amp * np.exp(1j * phase)
-    z = np.real(np.fft.ifft2(spec))
+    z = np.ascontiguousarray(np.real(sf.ifft2(spec, workers=-1))[:M, :M])
     z -= z.min()
     z *= relief / max(z.max(), 1e-12)
     return z
@@ -298,15 +306,17 @@ def config5(members=128, side=(256, 2048), seed=0, cell=5.0, tf=14400.0) -> list
 
 
 def smooth_field(shape, corr_cells, rng):
-    """Gaussian random field with Gaussian correlation (FFT filter), unit variance."""
+    """Gaussian random field with Gaussian correlation (FFT filter on a
+    periodic grid of fast FFT lengths, cropped to `shape`), unit variance."""
+    import scipy.fft as sf
     ny, nx = shape
-    kx = np.fft.fftfreq(nx)
-    ky = np.fft.fftfreq(ny)
-    KX, KY = np.meshgrid(kx, ky)
-    filt = np.exp(-2.0 * (np.pi ** 2) * (corr_cells ** 2) * (KX ** 2 + KY ** 2))
-    noise = rng.standard_normal(shape)
-    f = np.real(np.fft.ifft2(np.fft.fft2(noise) * filt))
-    f -= f.mean()
+    Ly, Lx = _fft_len(ny), _fft_len(nx)
+    ky = np.fft.fftfreq(Ly)
+    kx = np.fft.rfftfreq(Lx)
+    filt = np.exp(-2.0 * (np.pi ** 2) * (corr_cells ** 2) * (kx[None, :] ** 2 + ky[:, None] ** 2))
+    noise = rng.standard_normal((Ly, Lx))
+    f = sf.irfft2(sf.rfft2(noise, workers=-1) * filt, s=(Ly, Lx), workers=-1)[:ny, :nx]
+    f = f - f.mean()
     s = f.std()
     return f / (s if s > 0 else 1.0)
 

@@ -8,10 +8,14 @@ import os
 import numpy as np
 
 
-def write_case(case, d, nsteps, dump=(), timing=False, maps=None, rates=None, src_rate=None):
+def write_case(case, d, nsteps, dump=(), timing=False, maps=None, rates=None, src_rate=None,
+               map_times=None, extra=None):
     """case: rift_gb300.synth.Case.  maps: {name: (mode, t0, t1, factor)} with
     name in rain/drain/surge and mode 1 = hold, 2 = interpolate.
-    rates: (rain_mps, drain_mps) fixed uniform rates when no series is set."""
+    rates: (rain_mps, drain_mps) fixed uniform rates when no series is set.
+    map_times: {name: (t0, t1)}: the interpolation factor of that map follows
+    the simulated time, (t - t0) / (t1 - t0).  extra: further refrun
+    parameters (t_stop, dump_final, timed_steps, dump_bc)."""
     os.makedirs(d, exist_ok=True)
     BX, BY = case.faces()
     BX.astype(np.float64).tofile(os.path.join(d, "BX.bin"))
@@ -44,6 +48,10 @@ def write_case(case, d, nsteps, dump=(), timing=False, maps=None, rates=None, sr
         np.asarray(t0, np.float64).tofile(os.path.join(d, f"{name}_t0.bin"))
         if t1 is not None:
             np.asarray(t1, np.float64).tofile(os.path.join(d, f"{name}_t1.bin"))
+    for name, (a, b) in (map_times or {}).items():
+        p[f"map_times_{name}"] = f"{float(a)!r} {float(b)!r}"
+    for k, v in (extra or {}).items():
+        p[k] = repr(float(v)) if isinstance(v, float) else v
     with open(os.path.join(d, "params.txt"), "w") as f:
         for k, v in p.items():
             f.write(f"{k} {v}\n")

@@ -316,6 +316,80 @@ def test_closure_fallback_blocks_leave_the_state(torch):
     assert np.array_equal(sim.field("W"), w0)
 
 
+def test_closure_mixed_fallback_isolates_blocks(torch):
+    """Some blocks fall back, others not: every cell of a fallen-back block
+    keeps the plain solve bit for bit, faces shared with a fallen-back block
+    are not corrected from either side, and the other cells change by exactly
+    the divergence of their own blocks' corrections (a numpy FP32 restatement
+    of the apply step with the kernel's per-block flags)."""
+    case = synth.small_case(nx_cells=80, ny_cells=64, seed=9, cell=4.0, rain_mmhr=600.0, rim=True)
+    sim = capi.Sim(case).setup()
+    sim.run(300)
+    rng = np.random.default_rng(8)
+    model = closure.Model(_params(rng), SCALE, np.full(4, 2e-3, np.float32))
+    snap = sim.snapshot()
+    bc = sim.field("BC")
+    dtw = 2.0
+    chosen = None
+    for tau in np.geomspace(1e-5, 1e2, 36):
+        sim.load_snapshot(snap)
+        run = closure.ClosureRun(sim, model, hmin=0.01, lim=0.2, tau=float(tau))
+        run.apply(dtw, sim.time()[0])
+        ev, fb = run.block_counts()
+        if 0 < fb < ev:
+            chosen = run
+            break
+    assert chosen is not None, "no tau splits the blocks"
+    run = chosen
+    torch.cuda.synchronize()
+    h0 = (snap["w"] - bc).astype(np.float64)
+    h1 = sim.field("W") - bc
+    v = run.view
+    ny, nx = v.h_ny, v.h_nx
+    tx = -(-(nx - 4) // 16)
+    fell = run.fell.cpu().numpy().astype(bool)
+    corr = run.corr.cpu().numpy()[:, :ny, :nx]
+    jj, ii = np.mgrid[0:ny, 0:nx]
+    blk = np.full((ny, nx), -1)
+    inner = (jj >= 2) & (jj <= ny - 3) & (ii >= 2) & (ii <= nx - 3)
+    blk[inner] = ((jj[inner] - 2) // 16) * tx + (ii[inner] - 2) // 16
+    fb_cell = np.zeros((ny, nx), bool)
+    fb_cell[inner] = fell[blk[inner]]
+    # fallen-back blocks: bit-identical depths (the FP64 w of an unchanged FP32 h)
+    assert fb_cell.any() and (~fb_cell & inner).any()
+    np.testing.assert_array_equal(sim.field("W")[fb_cell], snap["w"][fb_cell])
+    # restatement of the apply step
+    sx = np.float32(dtw / case.cell)
+    off = fb_cell.copy()
+    exp = h0.astype(np.float32).copy()
+    for j in range(3, ny - 3):
+        for i in range(3, nx - 3):
+            if fb_cell[j, i]:
+                continue
+            mE = 0.0 if off[j, i + 1] else corr[0, j, i]
+            mW = 0.0 if off[j, i - 1] else corr[0, j, i - 1]
+            mN = 0.0 if off[j + 1, i] else corr[2, j, i]
+            mS = 0.0 if off[j - 1, i] else corr[2, j - 1, i]
+            if mE == mW == mN == mS == 0.0:
+                continue
+            exp[j, i] = np.float32(exp[j, i] - (sx * np.float32(mE - mW) + sx * np.float32(mN - mS)))
+    d = np.abs(h1 - exp.astype(np.float64))[inner]
+    assert d.max() <= 1e-6, d.max()
+    assert np.abs(h1 - h0)[inner & ~fb_cell].max() > 0
+    v0 = float(h0[inner].sum())
+    assert abs(float(h1[inner].sum()) - v0) <= 1e-6 * v0
+
+
+def test_closure_rejects_limits_that_could_dry_a_cell(torch):
+    case = synth.small_case(nx_cells=32, ny_cells=32, seed=9, cell=4.0)
+    sim = capi.Sim(case).setup()
+    model = closure.Model(closure.init_params(0), SCALE, np.full(4, 2e-3, np.float32))
+    for kw in (dict(lim=0.25), dict(lim=0.3), dict(hmin=1e-7, lim=0.2)):
+        run = closure.ClosureRun(sim, model, **kw)
+        with pytest.raises(capi.RiftError):
+            run.apply(1.0, 0.0)
+
+
 def test_generate_train_and_run_end_to_end(torch):
     """Small-grid version of the whole closure workflow: training patches
     from the solver, a few Adam steps that lower the loss, a coarse run with

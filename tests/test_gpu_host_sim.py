@@ -303,3 +303,70 @@ def test_dropin_gridded_rain_maps(host, oracle_api, tmp_path, interp):
     case = _oracle_case(z, flags, series={1: synth.csv_series([0, 1], [5, 5])})
     prints, _, _ = _oracle_prints(oracle_api, case, 150.0, 30.0, [hook])
     _compare(tmp, prints)
+
+
+def test_coupling_hooks_drive_the_source(host, oracle_api, tmp_path):
+    """The 1D-2D coupling calls (OpenSimulation with a flow rate,
+    setSourceValue, updateSources): a configuration that places a source
+    without a hydrograph, its discharge set by the caller before every step.
+    The run matches the oracle stepped with the same per-cell rates, and the
+    V_added bookkeeping is the reference's: rate x the dt current at the
+    call, per source cell."""
+    tmp = str(tmp_path)
+    z, _ = _scene(tmp)
+    X0, Y0 = 500.0 + 5.0 + 20 * CELL, 700.0 + 5.0 + 18 * CELL
+    X1, Y1 = X0 + CELL, Y0 + CELL  # a 2 x 2 rectangle of source cells
+    cfg = _config(tmp, {"source_rect_X": f"({X0}, {X1})", "source_rect_Y": f"({Y0}, {Y1})",
+                        "check_volume": "1", "h_print": "0", "tf": "120"})
+
+    def q_of(t):  # the coupled model's discharge, m^3/s
+        return 6.0 * np.sin(np.pi * min(t, 100.0) / 100.0) ** 2
+
+    old = os.getcwd()
+    os.chdir(tmp)
+    try:
+        sim = C.c_void_p()
+        rc = host.rift_sim_open_flow(cfg.encode(), C.c_double(2.5), C.byref(sim))
+        assert rc == 0, host.rift_host_last_error()
+        fr, ns = C.c_double(), C.c_int32()
+        assert host.rift_sim_flow_rate(sim, C.byref(fr)) == 0 and fr.value == 2.5
+        assert host.rift_sim_num_sources(sim, C.byref(ns)) == 0 and ns.value == 4
+        t, dt, tf = C.c_double(), C.c_double(), C.c_double()
+        rates, v_ref = [], 0.0
+        while True:
+            assert host.rift_sim_time(sim, C.byref(t), C.byref(dt), C.byref(tf)) == 0
+            if t.value >= tf.value:
+                break
+            q = q_of(t.value)
+            assert host.rift_sim_set_source_value(sim, C.c_double(q)) == 0
+            assert host.rift_sim_update_sources(sim) == 0
+            r = q / CELL / CELL / 4
+            v_ref += 4 * (r * dt.value)
+            rates.append(r)
+            assert host.rift_sim_step(sim, C.byref(t)) == 0, host.rift_sim_last_error(sim)
+        va = C.c_double()
+        assert host.rift_sim_source_volume(sim, C.byref(va)) == 0
+        assert abs(va.value - v_ref) <= 1e-12 * v_ref
+        eng = C.CDLL(eb.build())
+        h = C.c_void_p(host.rift_sim_engine(sim))
+        W = np.zeros((_NY + 4, _NX + 4))
+        assert eng.rift_get_field(h, 0, W.ctypes.data_as(C.POINTER(C.c_double)),
+                                  C.c_size_t(_NX + 4)) == 0
+        assert host.rift_sim_close(sim) == 0
+    finally:
+        os.chdir(old)
+    h_nx = z.shape[1] + 3
+    i0 = int((X0 - (500.0 + 5.0)) / CELL + 0.5)
+    j0 = int((Y0 - (700.0 + 5.0)) / CELL + 0.5)
+    src = [j * h_nx + i for i in (i0, i0 + 1) for j in (j0, j0 + 1)]
+    case = _oracle_case(z, synth.POINT_SOURCE | synth.TILE_ACCEL, src=src)
+    lib, _ = oracle_api
+    lib.rift_oracle_set_threads(os.cpu_count() or 1)
+    orc = capi.Sim(case, api=oracle_api, create_mode=0).setup()
+    for r in rates:
+        orc.set_point_sources(src, [r] * 4)
+        orc.step()
+    Wo = orc.field("W")
+    dh = np.abs(W - Wo)[2:-2, 2:-2].max()
+    assert dh <= MAX_DH, dh
+    assert (Wo - orc.field("BC"))[2:-2, 2:-2].max() > 0.05  # the source filled cells

@@ -70,6 +70,35 @@ def test_noalloc_volume_matches_engine_volume_twice(engine_api):
     sim.close()
 
 
+@pytest.mark.parametrize("rows", [37, 2101, 32768])
+def test_noalloc_volume_tall_grids(engine_api, rows):
+    """Grids from a few rows (most of the combining warp's lanes get no rows)
+    up to the scratch limit (every lane sums a block of 1,024 rows), with an
+    infiltration field and a leading dimension wider than the grid."""
+    torch = pytest.importorskip("torch")
+    lib, _ = engine_api
+    noalloc = _bind(lib)
+    nx, ld = 21, 32
+    rng = np.random.default_rng(rows)
+    h = np.zeros((rows, ld), dtype=np.float32)
+    F = np.zeros((rows, ld), dtype=np.float32)
+    h[2:-2, 2:nx - 2] = rng.uniform(0.0, 3.0, size=(rows - 4, nx - 4)).astype(np.float32)
+    F[2:-2, 2:nx - 2] = rng.uniform(0.0, 0.1, size=(rows - 4, nx - 4)).astype(np.float32)
+    h[:, nx - 2:] = 1e6  # outside the interior: must not be summed
+    exact = float(np.sum(h[2:-2, 2:nx - 2].astype(np.float64)) +
+                  np.sum(F[2:-2, 2:nx - 2].astype(np.float64)))
+    dh, dF = torch.from_numpy(h).cuda(), torch.from_numpy(F).cuda()
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.cuda.synchronize()
+        rc = noalloc(ctypes.c_void_p(dh.data_ptr()), ctypes.c_void_p(dF.data_ptr()), nx, rows, ld,
+                     ctypes.c_void_p(out.data_ptr()), None)
+        assert rc == 0
+        torch.cuda.synchronize()
+        got = float(out.item())
+        assert abs(got - exact) <= REL_TOL * exact, (rows, got, exact)
+
+
 def test_noalloc_volume_rejects_grids_beyond_its_scratch(engine_api):
     torch = pytest.importorskip("torch")
     lib, _ = engine_api
