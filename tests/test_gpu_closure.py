@@ -14,9 +14,12 @@ from rift_gb300 import capi, closure, synth
 
 pytestmark = pytest.mark.gpu
 
-# BF16 operands (8-bit mantissa) in every contraction, FP32 accumulation
-FWD_TOL = 3e-2      # max |out - ref| / max |ref|
-GRAD_TOL = 6e-2     # |g - g_ref| / |g_ref| per parameter block
+# BF16 operands (8-bit mantissa) in every contraction, FP32 accumulation,
+# against true FP32 PyTorch (TF32 off).  Measured on GB300: forward 5.1e-3,
+# loss 2.5e-4, gradient blocks 1.6e-3 .. 2.5e-3; the bars keep 3-4x margin.
+FWD_TOL = 1.5e-2    # max |out - ref| / max |ref|
+LOSS_TOL = 2e-3     # relative loss difference
+GRAD_TOL = 1e-2     # |g - g_ref| / |g_ref| per parameter block
 
 
 @pytest.fixture(scope="module")
@@ -99,7 +102,7 @@ def test_gradient_matches_autograd(torch):
     lref = ls * (w * (ref - tgt) ** 2).sum()
     lref.backward()
     g = pr.grad
-    assert abs(loss.item() - lref.item()) / lref.item() < FWD_TOL
+    assert abs(loss.item() - lref.item()) / lref.item() < LOSS_TOL
     blocks = {"W1": (closure.OFF_W1, closure.OFF_B1), "b1": (closure.OFF_B1, closure.OFF_W2),
               "W2": (closure.OFF_W2, closure.OFF_B2), "b2": (closure.OFF_B2, closure.OFF_W3),
               "W3": (closure.OFF_W3, closure.OFF_W3 + 128), "b3": (closure.OFF_B3, closure.OFF_B3 + 4)}
