@@ -52,6 +52,7 @@ extern "C" {
 #define RIFT_F_TILE_ACCEL    (1u << 9)  /* tile_acceleration: skip dry tiles */
 #define RIFT_F_POINT_SOURCE  (1u << 10) /* dambreak: hydrograph point/rect source */
 #define RIFT_F_H_INIT        (1u << 11) /* h_init: initial depth map */
+#define RIFT_F_CHECK_VOLUME  (1u << 12) /* check_volume: keep the full volume ledger */
 
 /* ---- map slots for rift_set_map ---------------------------------------- */
 #define RIFT_MAP_RAIN  0  /* m/s, hyetograph_gridded_rate */
@@ -188,6 +189,33 @@ int rift_volume(rift_handle* h, double* volume);
  * drain, infiltration or clamping, volume - volume(init) = added up to the
  * FP32 rounding of the state. */
 int rift_mass_ledger(rift_handle* h, double* volume, double* added);
+
+/* The full FP64 volume ledger (the check_volume accounting of
+ * simulator.cu:524-530, 609-637, 819-820, 892-897, completed with every way
+ * the step adds or removes water: the clamps of grid.cu:748-749, 914-915,
+ * 1083-1084, the drain and infiltration caps of grid.cu:776-805, the surge
+ * condition of grid.cu:894-904 and the critical-depth ghosts of
+ * grid.cu:1325-1406).  Depths summed over interior cells (times dx*dy for
+ * m^3), since the ledger's start (rift_init or rift_set_state):
+ *   volume - volume0 = added - drained - infiltrated - clamped + surge + boundary
+ * and, with infiltration, soil - soil0 = infiltrated.  Each term is the
+ * state change it caused: an RK2 step applies half of each stage's rates for
+ * dt (Euler: the single stage's), and the clamps' removals as applied.  The
+ * terms after `added`, and volume0 / soil0, are kept only when the handle
+ * was created with RIFT_F_CHECK_VOLUME (a few operations per cell and
+ * stage); otherwise they read 0 (volume0, soil0: NaN).  The ensemble kernel
+ * does not keep them (rift_ensemble_create rejects such members). */
+typedef struct rift_ledger {
+    double volume, soil;       /* sums of h and of F (Green-Ampt) now */
+    double volume0, soil0;     /* the same at the ledger's start */
+    double added;              /* uniform rain, gridded rain and point sources */
+    double drained;            /* uniform and gridded drain, after the h/dt cap */
+    double infiltrated;        /* Green-Ampt rates, after the h/dt cap */
+    double clamped;            /* depth the epsilon clamps removed (net) */
+    double surge;              /* depth the surge condition added (net) */
+    double boundary;           /* net inflow through the domain edge */
+} rift_ledger;
+int rift_mass_ledger_terms(rift_handle* h, rift_ledger* out);
 
 /* Measurement entry point (no reference counterpart; the reference only
  * prints a wall-clock Mcells/s line, simulator.cu:836-841): nsteps step-graph

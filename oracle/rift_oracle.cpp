@@ -210,6 +210,13 @@ struct rift_oracle {
     double t = 0.0, dt = 0.0;
     double rain_rate = 0.0, drain_rate = 0.0;
     double v_added = 0.0;  // volume ledger, see rift_oracle_mass_ledger
+    // full ledger (rift_oracle_mass_ledger_terms): terms since its start,
+    // LED order drained, infiltrated, clamped, surge, boundary inflow; the
+    // rates of the last flux pass (edge inflow, drain, infiltration) wait
+    // for the dt the integrator applies them with
+    double led[5] = {0, 0, 0, 0, 0};
+    double pendRate[3] = {0, 0, 0};
+    double vol0 = 0.0, soil0 = 0.0, added0 = 0.0;
     std::vector<int32_t> src_idx;
     std::vector<double> src_rate;
     Map maps[3];
@@ -364,7 +371,9 @@ void grow(rift_oracle* o) {
 // ComputeFluxes_k (grid.cu:564-839) over the active tiles.  Fluxes read the
 // unclamped w of every cell; the w = BC clamp of grid.cu:748-749 is applied
 // after all tiles are done (in the reference neighbours may read either value).
-void computeFluxes(rift_oracle* o, double dtArg) {
+// clampWeight: the share of the step's result that the state entering this
+// flux pass carries (1 for U^n, whose clamp both RK stages see; 1/2 for U*).
+void computeFluxes(rift_oracle* o, double dtArg, double clampWeight) {
     const FM& m = o->m;
     const int nx = o->nx, ny = o->ny, nBX = o->nBX;
     const double kappa = o->g.kappa, dx = o->g.dx, dy = o->g.dy;
@@ -373,6 +382,9 @@ void computeFluxes(rift_oracle* o, double dtArg) {
         if (o->active[b]) tiles.push_back(b);
     std::vector<uint8_t> clampMask(o->w.size(), 0);
     const int ntiles = (int)tiles.size();
+    // ledger partials per tile (summed in tile order afterwards): edge
+    // inflow rate, drain rate, infiltration rate
+    std::vector<double> part(3 * (size_t)ntiles, 0.0);
 
 #pragma omp parallel for schedule(dynamic, 4)
     for (int k = 0; k < ntiles; k++) {
@@ -450,12 +462,22 @@ void computeFluxes(rift_oracle* o, double dtArg) {
                 double S0 = 0.0;
                 if (o->has(RIFT_F_RAIN_UNIFORM)) S0 += o->rain_rate;
                 if (o->has(RIFT_F_RAIN_GRID)) S0 += mapValue(o, RIFT_MAP_RAIN, id);
-                if (o->has(RIFT_F_DRAIN_UNIFORM))
-                    S0 -= (o->drain_rate > hC / dtArg) ? hC / dtArg : o->drain_rate;
+                if (o->has(RIFT_F_DRAIN_UNIFORM)) {
+                    double d = (o->drain_rate > hC / dtArg) ? hC / dtArg : o->drain_rate;
+                    S0 -= d;
+                    part[3 * k + 1] += d;
+                }
                 if (o->has(RIFT_F_DRAIN_GRID)) {
                     double d = mapValue(o, RIFT_MAP_DRAIN, id);
-                    S0 -= (d > hC / dtArg) ? hC / dtArg : d;
+                    d = (d > hC / dtArg) ? hC / dtArg : d;
+                    S0 -= d;
+                    part[3 * k + 1] += d;
                 }
+                // flow through the domain edge (the critical-depth ghosts)
+                if (i == 2) part[3 * k] += FX[ty][tx][0] / dx;
+                if (i == nx - 3) part[3 * k] -= FX[ty][tx + 1][0] / dx;
+                if (j == 2) part[3 * k] += FY[ty][tx][0] / dy;
+                if (j == ny - 3) part[3 * k] -= FY[ty + 1][tx][0] / dy;
                 if (o->has(RIFT_F_POINT_SOURCE) || !o->src_idx.empty()) {
                     for (size_t s = 0; s < o->src_idx.size(); s++)
                         S0 = ((long)j * nx + i == (long)o->src_idx[s]) ? S0 + o->src_rate[s] : S0;
@@ -469,6 +491,7 @@ void computeFluxes(rift_oracle* o, double dtArg) {
                     f = (f > 0.0) ? f : 0.0;
                     o->dF[id] = f;
                     S0 -= f;
+                    part[3 * k + 2] += f;
                 }
                 o->dw[id] = dwv + S0;
                 o->dhu[id] = dhuv + S1;
@@ -480,8 +503,24 @@ void computeFluxes(rift_oracle* o, double dtArg) {
         o->mx[b] = mxt;
         o->my[b] = myt;
     }
+    double clamped = 0.0;
     for (size_t id = 0; id < clampMask.size(); id++)
-        if (clampMask[id]) o->w[id] = o->BC[id];
+        if (clampMask[id]) {
+            clamped += o->w[id] - o->BC[id];
+            o->w[id] = o->BC[id];
+        }
+    o->led[2] += clampWeight * clamped;
+    for (int q = 0; q < 3; q++) o->pendRate[q] = 0.0;
+    for (int k = 0; k < ntiles; k++)
+        for (int q = 0; q < 3; q++) o->pendRate[q] += part[3 * (size_t)k + q];
+}
+
+// The rates of the last flux pass applied for weight x dt: edge inflow,
+// drain and infiltration into the ledger.
+void ledgerRates(rift_oracle* o, double wdt) {
+    o->led[4] += wdt * o->pendRate[0];
+    o->led[0] += wdt * o->pendRate[1];
+    o->led[1] += wdt * o->pendRate[2];
 }
 
 // Simulator::ComputeTimestep (simulator.cu:540-566): max over ALL tiles,
@@ -505,10 +544,12 @@ void integrate1(rift_oracle* o) {
     const int nx = o->nx, nBX = o->nBX;
     const double t = o->t, dt = o->dt, kappa = o->g.kappa;
     const bool euler = o->has(RIFT_F_EULER);
+    const double wHalf = euler ? 1.0 : 0.5;
     std::vector<int> tiles;
     for (int b = 0; b < o->gridSize; b++)
         if (o->active[b]) tiles.push_back(b);
     const int ntiles = (int)tiles.size();
+    std::vector<double> part(2 * (size_t)ntiles, 0.0);  // clamp, surge
 #pragma omp parallel for schedule(dynamic, 4)
     for (int k = 0; k < ntiles; k++) {
         const int b = tiles[k];
@@ -526,7 +567,9 @@ void integrate1(rift_oracle* o) {
                     double s = mapValue(o, RIFT_MAP_SURGE, id);
                     if (s != o->g.nodata && s > 0.0) {
                         double next_h = o->w[id] + o->dw[id] * dt - o->BC[id];
+                        double d0 = o->dw[id];
                         o->dw[id] = (s - next_h) / dt;
+                        part[2 * k + 1] += (o->dw[id] - d0) * dt;
                     }
                 }
                 o->w[id] += o->dw[id] * dt;
@@ -535,6 +578,7 @@ void integrate1(rift_oracle* o) {
                 o->hv[id] += o->dhv[id] * dt;
                 o->hv[id] /= (1.0 - dt * o->G[id]);
                 double hC = (o->w[id] - o->BC[id] > kEps) ? o->w[id] - o->BC[id] : 0.0;
+                if (!(hC > kEps)) part[2 * k] += o->w[id] - o->BC[id];
                 o->w[id] = (hC > kEps) ? o->w[id] : o->BC[id];
                 if (o->has(RIFT_F_INFILTRATION)) {
                     o->F_old[id] = o->F[id];
@@ -572,6 +616,11 @@ void integrate1(rift_oracle* o) {
             }
         if (euler && o->tileHead(b)) o->wet[b] = (!o->has(RIFT_F_TILE_ACCEL)) || anyWet;
     }
+    ledgerRates(o, wHalf * dt);
+    for (int k = 0; k < ntiles; k++) {
+        o->led[2] += wHalf * part[2 * (size_t)k];
+        o->led[3] += wHalf * part[2 * (size_t)k + 1];
+    }
 }
 
 // Integrate_2_k (grid.cu:1043-1171)
@@ -583,6 +632,7 @@ void integrate2(rift_oracle* o) {
     for (int b = 0; b < o->gridSize; b++)
         if (o->active[b]) tiles.push_back(b);
     const int ntiles = (int)tiles.size();
+    std::vector<double> part((size_t)ntiles, 0.0);  // clamp
 #pragma omp parallel for schedule(dynamic, 4)
     for (int k = 0; k < ntiles; k++) {
         const int b = tiles[k];
@@ -597,6 +647,7 @@ void integrate2(rift_oracle* o) {
                 o->hu[id] = 0.5 * (o->hu_old[id] + o->hu[id] + o->dhu[id] * dt);
                 o->hv[id] = 0.5 * (o->hv_old[id] + o->hv[id] + o->dhv[id] * dt);
                 double hC = (o->w[id] - o->BC[id] > kEps) ? o->w[id] - o->BC[id] : 0.0;
+                if (!(hC > kEps)) part[k] += o->w[id] - o->BC[id];
                 o->w[id] = (hC > kEps) ? o->w[id] : o->BC[id];
                 if (o->has(RIFT_F_INFILTRATION))
                     o->F[id] = 0.5 * (o->F_old[id] + o->F[id] + o->dF[id] * dt);
@@ -620,6 +671,8 @@ void integrate2(rift_oracle* o) {
             }
         if (o->tileHead(b)) o->wet[b] = (!o->has(RIFT_F_TILE_ACCEL)) || anyWet;
     }
+    ledgerRates(o, 0.5 * dt);
+    for (int k = 0; k < ntiles; k++) o->led[2] += part[(size_t)k];
 }
 
 // Simulator::UpdateSource (simulator.cu:500-538) for device-style series:
@@ -659,7 +712,7 @@ void oneStep(rift_oracle* o) {
             refreshMap(o, w);
         }
     grow(o);
-    computeFluxes(o, o->dt);
+    computeFluxes(o, o->dt, 1.0);
     computeTimestep(o);
     // volume the sources add over this step (each rate applies for dt)
     double add = 0.0;
@@ -672,12 +725,42 @@ void oneStep(rift_oracle* o) {
     integrate1(o);
     applyBoundaries(o);
     if (!o->has(RIFT_F_EULER)) {
-        computeFluxes(o, o->dt);
+        computeFluxes(o, o->dt, 0.5);
         integrate2(o);
         applyBoundaries(o);
     }
 }
 
+}  // namespace
+
+namespace {
+// Interior sums of h = w - BC (as the state holds it) and of F, Kahan.
+void stateSums(const rift_oracle* o, double* vol, double* soil) {
+    double s = 0.0, cs = 0.0, f = 0.0, cf = 0.0;
+    for (int j = 2; j <= o->ny - 3; j++)
+        for (int i = 2; i <= o->nx - 3; i++) {
+            size_t id = o->c(j, i);
+            double y = (o->w[id] - o->BC[id]) - cs;
+            double tt = s + y;
+            cs = (tt - s) - y;
+            s = tt;
+            if (o->has(RIFT_F_INFILTRATION)) {
+                double yf = o->F[id] - cf;
+                double tf = f + yf;
+                cf = (tf - f) - yf;
+                f = tf;
+            }
+        }
+    *vol = s;
+    *soil = f;
+}
+
+void ledgerStart(rift_oracle* o) {
+    for (double& x : o->led) x = 0.0;
+    for (double& x : o->pendRate) x = 0.0;
+    o->added0 = o->v_added;
+    stateSums(o, &o->vol0, &o->soil0);
+}
 }  // namespace
 
 extern "C" {
@@ -772,6 +855,7 @@ int rift_oracle_init(rift_oracle* o, double t0) {
     o->dt = (double)0.0000001f;  // simulator.cu:35
     applyBoundaries(o);
     o->inited = true;
+    ledgerStart(o);
     return RIFT_OK;
 }
 
@@ -919,6 +1003,7 @@ int rift_oracle_set_state(rift_oracle* o, double t, double dt_prev, const double
     // (no -1 fills), so the first-Grow special case no longer applies
     o->first_grow = false;
     for (int b = 0; b < o->gridSize; b++) o->prev_active[b] = o->active[b];
+    ledgerStart(o);
     return RIFT_OK;
 }
 
@@ -945,6 +1030,23 @@ int rift_oracle_volume(rift_oracle* o, double* volume) {
             s = tt;
         }
     *volume = s;
+    return RIFT_OK;
+}
+
+
+int rift_oracle_mass_ledger_terms(rift_oracle* o, rift_ledger* out) {
+    if (!o || !out || !o->inited) return RIFT_ERR_ARG;
+    rift_ledger L{};
+    stateSums(o, &L.volume, &L.soil);
+    L.volume0 = o->vol0;
+    L.soil0 = o->soil0;
+    L.added = o->v_added - o->added0;
+    L.drained = o->led[0];
+    L.infiltrated = o->led[1];
+    L.clamped = o->led[2];
+    L.surge = o->led[3];
+    L.boundary = o->led[4];
+    *out = L;
     return RIFT_OK;
 }
 

@@ -62,6 +62,9 @@ int rift_oracle_set_state(rift_oracle* o, double t, double dt_prev, const double
 int rift_oracle_get_time(rift_oracle* o, double* t, double* dt);
 int rift_oracle_volume(rift_oracle* o, double* volume);
 int rift_oracle_mass_ledger(rift_oracle* o, double* volume, double* added);
+/* The full FP64 ledger (rift_ledger of include/rift_gb300.h), since
+ * rift_oracle_init / rift_oracle_set_state; always kept. */
+int rift_oracle_mass_ledger_terms(rift_oracle* o, rift_ledger* out);
 int rift_oracle_get_tile_grid(rift_oracle* o, int32_t* nBX, int32_t* nBY);
 int rift_oracle_set_threads(int32_t n);
 const char* rift_oracle_last_error(rift_oracle* o);

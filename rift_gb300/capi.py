@@ -37,6 +37,12 @@ class DeviceView(C.Structure):
                 ("dx", C.c_double), ("dy", C.c_double), ("kappa", C.c_double)]
 
 
+class Ledger(C.Structure):
+    """rift_ledger (include/rift_gb300.h)."""
+    _fields_ = [(n, C.c_double) for n in ("volume", "soil", "volume0", "soil0", "added", "drained",
+                                          "infiltrated", "clamped", "surge", "boundary")]
+
+
 class RiftError(RuntimeError):
     pass
 
@@ -79,6 +85,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
     ns["set_map_factor"] = _sig(lib, p + "set_map_factor", C.c_int, [_P, C.c_int32, C.c_double])
     ns["set_map_times"] = _sig(lib, p + "set_map_times", C.c_int,
                                [_P, C.c_int32, C.c_double, C.c_double])
+    if hasattr(lib, p + "mass_ledger_terms"):
+        ns["mass_ledger_terms"] = _sig(lib, p + "mass_ledger_terms", C.c_int, [_P, C.POINTER(Ledger)])
     if hasattr(lib, p + "set_point_rates"):
         ns["set_point_rates"] = _sig(lib, p + "set_point_rates", C.c_int, [_P, _D, C.c_int32])
     if hasattr(lib, p + "set_schedule"):
@@ -340,6 +348,17 @@ class Sim:
         v, a = C.c_double(), C.c_double()
         self._check(self.f["mass_ledger"](self.h, C.byref(v), C.byref(a)), "mass_ledger")
         return v.value, a.value
+
+    def ledger(self):
+        """The full volume ledger (rift_mass_ledger_terms) as a dict, with
+        `residual` = (volume - volume0) - (added - drained - infiltrated -
+        clamped + surge + boundary)."""
+        L = Ledger()
+        self._check(self.f["mass_ledger_terms"](self.h, C.byref(L)), "mass_ledger_terms")
+        d = {n: getattr(L, n) for n, _ in Ledger._fields_}
+        d["residual"] = (d["volume"] - d["volume0"]) - (d["added"] - d["drained"] - d["infiltrated"]
+                                                        - d["clamped"] + d["surge"] + d["boundary"])
+        return d
 
     def set_state(self, t, dt_prev, w, hu, hv, F=None, wet=None, active=None, mx=None, my=None):
         arrs = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None

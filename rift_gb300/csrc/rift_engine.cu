@@ -91,6 +91,9 @@ struct rift_handle {
     int serN[3] = {0, 0, 0};
     DevState* st = nullptr;
     DevState* hst = nullptr;  // pinned mirror
+    // start of the volume ledger (rift_init, rift_set_state): interior sums
+    // of h and F, and the source total at that moment
+    double ledVol0 = 0.0, ledSoil0 = 0.0, ledAdded0 = 0.0;
     float* stage = nullptr;   // pinned host planes for field uploads / readbacks
     size_t stageFloats = 0;
     double* volPartial = nullptr;
@@ -387,6 +390,9 @@ const char* deviceErrorText(int err) {
     if (err & ERR_BARRIER_TIMEOUT) return "device wait timed out (grid barrier)";
     return "device wait timed out (TMA barrier)";
 }
+
+int volumeSum(rift_handle* h, int what, double* out);
+int ledgerStart(rift_handle* h);
 
 int pullState(rift_handle* h) {
     CUDA_TRY(h, cudaMemcpyAsync(h->hst, h->st, sizeof(DevState), cudaMemcpyDeviceToHost, h->stream));
@@ -813,7 +819,7 @@ int rift_init(rift_handle* h, double t0) {
     s.t_stop = INFINITY;
     s.nInact = (int)inact.size();
     h->inited = true;
-    return pushState(h);
+    return ledgerStart(h);
 }
 
 int rift_set_uniform_rates(rift_handle* h, double rain_mps, double drain_mps) {
@@ -1437,7 +1443,7 @@ int rift_set_state(rift_handle* h, double t, double dt_prev, const double* w, co
     h->hst->t = t;
     h->hst->dt = dt_prev;
     h->hst->dt_old = dt_prev;
-    return pushState(h);
+    return ledgerStart(h);
 }
 
 int rift_mass_ledger(rift_handle* h, double* volume, double* added) {
@@ -1448,11 +1454,39 @@ int rift_mass_ledger(rift_handle* h, double* volume, double* added) {
     return RIFT_OK;
 }
 
+int rift_mass_ledger_terms(rift_handle* h, rift_ledger* out) {
+    if (!h || !out) return RIFT_ERR_ARG;
+    if (!h->inited) return fail(h, RIFT_ERR_STATE, "init first");
+    rift_ledger L{};
+    int rc;
+    if ((rc = volumeSum(h, 1, &L.volume)) || (rc = volumeSum(h, 2, &L.soil)) || (rc = pullState(h)))
+        return rc;
+    const DevState& s = *h->hst;
+    L.volume0 = h->ledVol0;
+    L.soil0 = h->ledSoil0;
+    L.added = s.v_added - h->ledAdded0;
+    L.drained = s.led[LED_DRAIN];
+    L.infiltrated = s.led[LED_INFIL];
+    L.clamped = s.led[LED_CLAMP];
+    L.surge = s.led[LED_SURGE];
+    L.boundary = s.led[LED_BOUND];
+    *out = L;
+    return RIFT_OK;
+}
+
 int rift_volume(rift_handle* h, double* volume) {
     if (!h || !volume) return RIFT_ERR_ARG;
+    return volumeSum(h, 0, volume);
+}
+
+}  // extern "C"
+
+namespace {
+// Compensated volume sum (k_volume's `what`) into *out.
+int volumeSum(rift_handle* h, int what, double* out) {
     Params P = makeParams(h);
     const int blocks = 1024;
-    k_volume<<<blocks, 256, 0, h->stream>>>(P, h->volPartial);
+    k_volume<<<blocks, 256, 0, h->stream>>>(P, h->volPartial, what);
     std::vector<double> part(2 * blocks);
     CUDA_TRY(h, cudaMemcpyAsync(part.data(), h->volPartial, part.size() * 8, cudaMemcpyDeviceToHost,
                                 h->stream));
@@ -1465,9 +1499,26 @@ int rift_volume(rift_handle* h, double* volume) {
         S = t;
         C += part[2 * b + 1];
     }
-    *volume = S + C;
+    *out = S + C;
     return RIFT_OK;
 }
+
+// Start of the check_volume ledger: its terms zeroed, the volumes and the
+// source total of this moment kept (the device state is synchronised).
+int ledgerStart(rift_handle* h) {
+    int rc;
+    for (int k = 0; k < LED_N; k++) h->hst->led[k] = 0.0;
+    h->hst->ledPend = 0.0;
+    if ((rc = pushState(h))) return rc;
+    h->ledAdded0 = h->hst->v_added;
+    h->ledVol0 = h->ledSoil0 = NAN;  // kept only for check_volume runs
+    if (!h->has(RIFT_F_CHECK_VOLUME)) return RIFT_OK;
+    if ((rc = volumeSum(h, 1, &h->ledVol0)) || (rc = volumeSum(h, 2, &h->ledSoil0))) return rc;
+    return RIFT_OK;
+}
+}  // namespace
+
+extern "C" {
 
 // Timed run for measurement: nsteps graph replays bracketed by CUDA events on
 // the handle's stream (ms_total), then up to 20 more steps launched one by
@@ -1678,6 +1729,8 @@ int rift_ensemble_create(rift_handle* const* members, int32_t n, rift_ensemble**
         if (!members[k]) return RIFT_ERR_ARG;
         if (!members[k]->inited) return RIFT_ERR_STATE;
         if (members[k]->g.device != members[0]->g.device) return RIFT_ERR_ARG;
+        // the ensemble kernel keeps the source ledger only
+        if (members[k]->has(RIFT_F_CHECK_VOLUME)) return RIFT_ERR_UNSUPPORTED;
         for (int q = 0; q < k; q++)
             if (members[q] == members[k]) return RIFT_ERR_ARG;
     }

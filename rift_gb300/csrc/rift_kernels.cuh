@@ -48,14 +48,16 @@ constexpr int MAX_SERIES = 4096;
 constexpr uint32_t F_RAIN_U = 1u << 0, F_RAIN_G = 1u << 1, F_DRAIN_U = 1u << 2,
                    F_DRAIN_G = 1u << 3, F_INFIL = 1u << 4, F_SURGE = 1u << 5,
                    F_EULER = 1u << 6, F_SAVE_MAX = 1u << 7, F_SAVE_ARR = 1u << 8,
-                   F_TILE_ACC = 1u << 9, F_POINT = 1u << 10, F_H_INIT = 1u << 11;
+                   F_TILE_ACC = 1u << 9, F_POINT = 1u << 10, F_H_INIT = 1u << 11,
+                   F_CHECKVOL = 1u << 12;
 
 // Flags that change the per-cell update; a kernel instantiated with a fixed
 // set FIX (!= 0) reads its flags from FIX instead of the run's flags: the
 // engine picks such an instantiation only when the run's flags, masked with
 // CELL_FLAGS, equal FIX (and point sources are present iff FIX has F_POINT).
 constexpr uint32_t CELL_FLAGS = F_RAIN_U | F_RAIN_G | F_DRAIN_U | F_DRAIN_G | F_INFIL | F_SURGE |
-                                F_EULER | F_SAVE_MAX | F_SAVE_ARR | F_TILE_ACC | F_POINT;
+                                F_EULER | F_SAVE_MAX | F_SAVE_ARR | F_TILE_ACC | F_POINT |
+                                F_CHECKVOL;
 // the fixed sets with march instantiations: uniform rain; infiltration with
 // a point hydrograph; gridded rain with a uniform drain (all with tile
 // acceleration)
@@ -100,6 +102,10 @@ struct DevState {
     unsigned staleBits[2];           // ensemble: stale speed maxima of inactive tiles
     double v_added;    // volume (depth x cells) the sources added since init
     double rain_sum[2];  // interior sums of the two rain maps (volume ledger)
+    // check_volume ledger since init (depth x cells), LED_* order; ledPend:
+    // stage-1 edge inflow rates summed before the step's dt is known
+    double led[5];
+    double ledPend;
     int error;
     int err_info;
 };
@@ -316,6 +322,49 @@ __device__ __forceinline__ float blockMax(float v, float* red) {
 }
 
 
+// ---------------------------------------------------------------- ledger
+// Volume ledger terms of a check_volume run (the reference's check_volume
+// switch, grid.cu:23), each already weighted by its share of the step: an
+// RK2 step moves the cell by half of each stage's rates times dt (Euler: all
+// of the single stage), plus the clamps applied to the state.  With V the
+// interior sum of h:
+//   V(t) - V(0) = added - drained - infiltrated - clamped + surge + boundary
+enum { LED_DRAIN = 0, LED_INFIL = 1, LED_CLAMP = 2, LED_SURGE = 3, LED_BOUND = 4, LED_N = 5 };
+
+struct Led {
+    float v[LED_N];
+};
+
+__device__ __forceinline__ void ledZero(Led& L) {
+#pragma unroll
+    for (int k = 0; k < LED_N; k++) L.v[k] = 0.f;
+}
+
+// Warp sums of the threads' terms into dst[0..LED_N) (FP64, one atomic per
+// non-zero term and warp); every lane of the warp calls it.  Zeroes L.
+__device__ __forceinline__ void flushLed(Led& L, double* dst) {
+#pragma unroll
+    for (int k = 0; k < LED_N; k++) {
+        float v = L.v[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(&dst[k], (double)v);
+        L.v[k] = 0.f;
+    }
+}
+
+// Inflow rate through the domain edge of interior cell (j, i) (m/s of
+// depth): the mass flux of its west / south face at the first interior
+// column / row, minus that of its east / north face at the last.
+__device__ __forceinline__ float edgeInflow(const Params& P, int j, int i, float fW, float fE,
+                                            float fS, float fN) {
+    float r = 0.f;
+    if (i == 2) r += fW * P.inv_dx;
+    if (i == P.nx - 3) r -= fE * P.inv_dx;
+    if (j == 2) r += fS * P.inv_dy;
+    if (j == P.ny - 3) r -= fN * P.inv_dy;
+    return r;
+}
+
 // ComputeTimestep's arithmetic (simulator.cu:540-566) from the maxima of
 // the tile speeds: dt with the reference's rounding points (fmaxf on the
 // scaled maxima, FP64 division), t += dt, and the step's entry in the
@@ -378,6 +427,10 @@ __device__ __forceinline__ void publishDt(const Params& P, DevState* st, double 
         if (P.mapMode[0] == 2) add += (double)st->factor[0] * (st->rain_sum[1] - st->rain_sum[0]);
     }
     st->v_added += add * dt;
+    if (P.flags & F_CHECKVOL) {  // stage-1 edge inflow of a flux pass that ran before dt
+        st->led[LED_BOUND] += ((P.flags & F_EULER) ? 1.0 : 0.5) * dt * st->ledPend;
+        st->ledPend = 0.0;
+    }
 }
 
 __device__ __forceinline__ void computeDt(const Params& P, DevState* st, double maxx, double maxy) {
@@ -837,6 +890,8 @@ __device__ __forceinline__ void writeGhosts(const Params& P, float* U, int j, in
 // Step-wide constants of a stage kernel.
 struct StageConsts {
     float kappa, dtNew, dtSrc, invDtSrc, rainU, drainU, fac0, fac1, fac2;
+    float wRate;   // ledger weight of this stage's rates: dt/2 (RK2) or dt (Euler)
+    float wHalf;   // 1/2 (RK2) or 1 (Euler)
     float srcR;  // the hydrograph's rate per source cell (every source holds it)
     double tNew;
     uint32_t fl;
@@ -868,6 +923,8 @@ __device__ __forceinline__ StageConsts stageConsts(const Params& P) {
     C.Uout = (STAGE == 1) ? P.B : P.A;
     C.Fin = (STAGE == 1) ? P.FA : P.FB;
     C.Fout = (STAGE == 1) ? P.FB : P.FA;
+    C.wHalf = C.euler ? 1.f : 0.5f;
+    C.wRate = C.wHalf * C.dtNew;
     return C;
 }
 
@@ -891,6 +948,7 @@ __device__ __forceinline__ StageConsts stageConstsAt(const Params& P, double dtN
     C.dtSrc = (STAGE == 1) ? (float)dtOld : C.dtNew;
     C.invDtSrc = 1.f / C.dtSrc;
     C.tNew = tNew;
+    C.wRate = C.wHalf * C.dtNew;
     return C;
 }
 
@@ -919,6 +977,7 @@ struct CellSrc {
     float Fc, dF;        // infiltration: F entering the stage, rate
     float rainG;         // gridded rain at the cell
     float G;             // stage 1: semi-implicit Manning coefficient
+    float drained;       // drain rate withdrawn (uniform + gridded, after the cap)
     bool srcCell;        // the cell holds a point source
 };
 
@@ -941,10 +1000,17 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
         S0 += rainG;
     }
     const float cap = hC * C.invDtSrc;
-    if (fl & F_DRAIN_U) S0 -= (C.drainU > cap) ? cap : C.drainU;
+    float drained = 0.f;
+    if (fl & F_DRAIN_U) {
+        const float d = (C.drainU > cap) ? cap : C.drainU;
+        S0 -= d;
+        drained += d;
+    }
     if (fl & F_DRAIN_G) {
         float d = mapValue(P, 1, c, C.fac1);
-        S0 -= (d > cap) ? cap : d;
+        d = (d > cap) ? cap : d;
+        S0 -= d;
+        drained += d;
     }
     bool srcCell = false;
     if ((FIX == 0 || (FIX & F_POINT)) && P.nsrc > 0) {
@@ -976,6 +1042,7 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
     r.Fc = Fc;
     r.dF = dF;
     r.rainG = rainG;
+    r.drained = drained;
     r.srcCell = srcCell;
     r.G = STAGE == 1 ? manningG(pre[0], hu0, hv0, hC, C.kappa) : 0.f;
     return r;
@@ -983,10 +1050,11 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
 
 // edge: the work item holds a cell next to the ghost band (i or j at 2 or
 // at n - 3); false skips the ghost tests for the items inside.
+// L (check_volume runs, else null): the cell's ledger terms are added to it.
 template <int STAGE, bool PREF = false, uint32_t FIX = 0>
 __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C, int j, int i,
                                            const CellSrc& src, float hC, float hu0, float hv0,
-                                           const float* pre, bool edge) {
+                                           const float* pre, bool edge, Led* L = nullptr) {
     const uint32_t fl = cellFlags<FIX>(C.fl);
     const bool euler = FIX ? (FIX & F_EULER) != 0 : C.euler;
     const size_t c = cidx(P, 0, j, i);
@@ -1002,12 +1070,17 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
         const float G = src.G;
         if (fl & F_SURGE) {
             float sg = mapValue(P, 2, c, C.fac2);
-            if (sg != P.nodata && sg > 0.f) dh = (sg - (hc + dh * dtNew)) / dtNew;
+            if (sg != P.nodata && sg > 0.f) {
+                const float d0 = dh;
+                dh = (sg - (hc + dh * dtNew)) / dtNew;
+                if (L) L->v[LED_SURGE] += C.wRate * (dh - d0);
+            }
         }
         hN = hc + dh * dtNew;
         const float den = 1.f / (1.f - dtNew * G);
         huN = (hu0 + dhu * dtNew) * den;
         hvN = (hv0 + dhv * dtNew) * den;
+        if (L) L->v[LED_CLAMP] += C.wHalf * ((hC - hc) + ((hN > kEps) ? 0.f : hN));
         hN = (hN > kEps) ? hN : 0.f;
         if (fl & F_INFIL) C.Fout[c] = Fc + dF * dtNew;
         if (euler) {
@@ -1037,6 +1110,7 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
         hN = 0.5f * (hOc + hc + dh * dtNew);
         huN = 0.5f * (pre[1] + hu0 + dhu * dtNew);
         hvN = 0.5f * (pre[2] + hv0 + dhv * dtNew);
+        if (L) L->v[LED_CLAMP] += 0.5f * ((hOld - hOc) + (hC - hc)) + ((hN > kEps) ? 0.f : hN);
         hN = (hN > kEps) ? hN : 0.f;
         if (fl & F_INFIL) C.Fout[c] = 0.5f * ((PREF ? pre[5] : P.FA[c]) + Fc + dF * dtNew);
         if (fl & F_SAVE_MAX) {
@@ -1051,6 +1125,10 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
         wetCell = (hN > kEps) || srcCell || ((fl & F_RAIN_U) && C.rainU > 0.f) ||
                   ((fl & F_RAIN_G) && rainG > 0.f);
     }
+    if (L) {
+        L->v[LED_DRAIN] += C.wRate * src.drained;
+        L->v[LED_INFIL] += C.wRate * dF;
+    }
     C.Uout[cidx(P, 0, j, i)] = hN;
     C.Uout[cidx(P, 1, j, i)] = huN;
     C.Uout[cidx(P, 2, j, i)] = hvN;
@@ -1062,10 +1140,11 @@ template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0>
 __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
                                            int i, float dh, float dhu, float dhv, float hC,
                                            float hu0, float hv0, float eW, float eE, float eS,
-                                           float eN, const float* pre, bool edge = true) {
+                                           float eN, const float* pre, bool edge = true,
+                                           Led* L = nullptr) {
     const CellSrc src = cellSources<STAGE, PREF, BED, FIX>(P, C, tile, j, i, dh, dhu, dhv, hC, hu0,
                                                            hv0, eW, eE, eS, eN, pre);
-    return cellFinish<STAGE, PREF, FIX>(P, C, j, i, src, hC, hu0, hv0, pre, edge);
+    return cellFinish<STAGE, PREF, FIX>(P, C, j, i, src, hC, hu0, hv0, pre, edge, L);
 }
 
 
@@ -1075,10 +1154,12 @@ __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C
 // j0-1 .. j0+14 and the 15 y faces.  Thread tid < 224 gets the divergence of
 // cell (tid / 16, tid % 16); with SPEEDS, spx / spy get the local speed of
 // the east / north face of that cell (0 outside the interior).
+// bin (check_volume runs, else null): the cell's inflow rate through the
+// domain edge (edgeInflow), 0 away from it.
 template <bool SPEEDS>
 __device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, const Params& P, int i0,
                                             int j0, float& dh, float& dhu, float& dhv, float& spx,
-                                            float& spy) {
+                                            float& spy, float* bin = nullptr) {
     // Two phases of the whole CTA: every thread builds one x and one y
     // reconstruction, then one x and one y face flux (the two directions are
     // independent until the divergence, so each thread has two chains in
@@ -1152,6 +1233,13 @@ __device__ __forceinline__ void tileFluxDiv(StageSmem& S, const TileBuf& T, cons
         dhu += -(S.FY[1][ty + 1][tx] - S.FY[1][ty][tx]) * P.inv_dy;
         dhv += -(S.FY[2][ty + 1][tx] - S.FY[2][ty][tx]) * P.inv_dy;
     }
+    if (bin) {
+        *bin = 0.f;
+        const int i = i0 + tx, j = j0 + ty;
+        if (tid < TH * TW && i <= P.nx - 3 && j <= P.ny - 3)
+            *bin = edgeInflow(P, j, i, S.FX[0][ty][tx], S.FX[0][ty][tx + 1], S.FY[0][ty][tx],
+                              S.FY[0][ty + 1][tx]);
+    }
 }
 
 // The cell's own global inputs for cellUpdate<STAGE, true> (pre[0..5]),
@@ -1184,7 +1272,8 @@ __device__ __forceinline__ void tilePrefetch(const Params& P, const StageConsts&
 template <int STAGE, uint32_t FIX = 0>
 __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConsts& C,
                                                const TileBuf& T, int tile, int i0, int j0, float dh,
-                                               float dhu, float dhv, const float (&pre)[6]) {
+                                               float dhu, float dhv, const float (&pre)[6],
+                                               Led* L = nullptr) {
     const int tid = threadIdx.x;
     const int tx = tid % TW, ty = tid / TW;
     const int i = i0 + tx, j = j0 + ty;
@@ -1194,7 +1283,7 @@ __device__ __forceinline__ bool tileCellUpdate(const Params& P, const StageConst
     const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
     return cellUpdate<STAGE, true, true, FIX>(P, C, tile, j, i, dh, dhu, dhv, T.in[0][r][c], T.in[1][r][c],
                                    T.in[2][r][c], T.e[0][r][c], T.e[1][r][c], T.e[2][r][c],
-                                   T.e[3][r][c], pre, edge);
+                                   T.e[3][r][c], pre, edge, L);
 }
 
 // tileCellUpdate in its two halves (see cellSources / cellFinish).
@@ -1217,7 +1306,8 @@ __device__ __forceinline__ CellSrc tileCellSources(const Params& P, const StageC
 template <int STAGE, uint32_t FIX = 0>
 __device__ __forceinline__ bool tileCellFinish(const Params& P, const StageConsts& C,
                                                const TileBuf& T, int i0, int j0,
-                                               const CellSrc& src, const float (&pre)[6]) {
+                                               const CellSrc& src, const float (&pre)[6],
+                                               Led* L = nullptr) {
     const int tid = threadIdx.x;
     const int tx = tid % TW, ty = tid / TW;
     const int i = i0 + tx, j = j0 + ty;
@@ -1225,7 +1315,7 @@ __device__ __forceinline__ bool tileCellFinish(const Params& P, const StageConst
     const int rr = ty + 2, cc = tx + 2;
     const bool edge = i0 == 2 || j0 == 2 || i0 + TW - 1 >= P.nx - 3 || j0 + TH - 1 >= P.ny - 3;
     return cellFinish<STAGE, true, FIX>(P, C, j, i, src, T.in[0][rr][cc], T.in[1][rr][cc],
-                                   T.in[2][rr][cc], pre, edge);
+                                   T.in[2][rr][cc], pre, edge, L);
 }
 
 // Tile flags (stage 2, or stage 1 in Euler mode) and stage-2 tile speeds.
@@ -1262,6 +1352,9 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
     const int tid = threadIdx.x;
     tileFirst(S, tmIn, tmE, P, nAct);
     const StageConsts C = given ? *given : blockConsts<STAGE>(P);
+    const bool led = (cellFlags<FIX>(C.fl) & F_CHECKVOL) != 0;
+    Led L;
+    ledZero(L);
     int bsel = 0;
     for (int k = blockIdx.x; k < nAct; k += gridDim.x, bsel ^= 1) {
         const int tile = P.act[k];
@@ -1274,12 +1367,15 @@ __device__ bool stageTiles(StageSmem& S, const CUtensorMap* tmIn, const CUtensor
             return false;
         }
         const TileBuf& T = S.buf[bsel];
-        float dh, dhu, dhv, spx, spy;
-        tileFluxDiv<STAGE == 2>(S, T, P, i0, j0, dh, dhu, dhv, spx, spy);
-        const bool wetCell = tileCellUpdate<STAGE, FIX>(P, C, T, tile, i0, j0, dh, dhu, dhv, pre);
+        float dh, dhu, dhv, spx, spy, bin = 0.f;
+        tileFluxDiv<STAGE == 2>(S, T, P, i0, j0, dh, dhu, dhv, spx, spy, led ? &bin : nullptr);
+        L.v[LED_BOUND] += C.wRate * bin;
+        const bool wetCell =
+            tileCellUpdate<STAGE, FIX>(P, C, T, tile, i0, j0, dh, dhu, dhv, pre, led ? &L : nullptr);
         tileFlags<STAGE>(P, C, S, tile, wetCell, spx, spy);
         __syncthreads();
     }
+    if (led) flushLed(L, P.st->led);
     return true;
 }
 
@@ -1337,15 +1433,17 @@ __global__ void __launch_bounds__(NT) k_commit(Params P) {
 }
 
 // ---------------------------------------------------------------- volume
-// FP64 compensated (Neumaier) sum of (h [+ F]) over interior cells; one
-// partial per block, combined on the host with the same summation.
-__global__ void k_volume(Params P, double* partial) {
+// FP64 compensated (Neumaier) sum over interior cells of h + F (what = 0;
+// F only with infiltration), h (what = 1) or F (what = 2); one partial per
+// block, combined on the host with the same summation.
+__global__ void k_volume(Params P, double* partial, int what) {
     double s = 0.0, c = 0.0;
     const int nInt = (P.nx - 4) * (P.ny - 4);
+    const bool withH = what != 2, withF = what != 1 && (P.flags & F_INFIL) && P.FA;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nInt; q += gridDim.x * blockDim.x) {
         int i = q % (P.nx - 4) + 2, j = q / (P.nx - 4) + 2;
-        double v = (double)P.A[cidx(P, 0, j, i)];
-        if (P.flags & F_INFIL) v += (double)P.FA[cidx(P, 0, j, i)];
+        double v = withH ? (double)P.A[cidx(P, 0, j, i)] : 0.0;
+        if (withF) v += (double)P.FA[cidx(P, 0, j, i)];
         double t = s + v;
         c += (fabs(s) >= fabs(v)) ? (s - t) + v : (v - t) + s;
         s = t;

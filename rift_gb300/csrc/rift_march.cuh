@@ -127,6 +127,11 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
     const bool owned = lane >= 2 && lane <= 29;
     const int tcol = owned ? lc / TW : 0;       // tile column inside the strip
     const float kappa = C.kappa;
+    // check_volume ledger: stage 1 sums the edge inflow rates (dt is not
+    // known yet), stage 2 the weighted terms of its cells
+    const bool led = (cellFlags<FIX>(C.fl) & F_CHECKVOL) != 0;
+    Led L;
+    ledZero(L);
 
     for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
         const int strip = P.strips[item];
@@ -241,6 +246,10 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                 const float fW1 = __shfl_up_sync(FULL, fE[1], 1);
                 const float fW2 = __shfl_up_sync(FULL, fE[2], 1);
                 if (cellOn) {
+                    if (led && edgeStrip) {
+                        const float r = edgeInflow(P, j, i, fW0, fE[0], fS0, fN[0]);
+                        L.v[LED_BOUND] += STAGE == 1 ? r : C.wRate * r;
+                    }
                     const float dh = -(fE[0] - fW0) * P.inv_dx - (fN[0] - fS0) * P.inv_dy;
                     const float dhu = -(fE[1] - fW1) * P.inv_dx - (fN[1] - fS1) * P.inv_dy;
                     const float dhv = -(fE[2] - fW2) * P.inv_dx - (fN[2] - fS2) * P.inv_dy;
@@ -254,7 +263,7 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                         const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
                         accWet |= cellUpdate<STAGE, false, true, FIX>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
                                                     cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre,
-                                                    edgeStrip);
+                                                    edgeStrip, led ? &L : nullptr);
                     }
                 }
                 fS0 = fN[0];
@@ -302,6 +311,16 @@ __global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtenso
                     }
         }
     }
+    if (led) {
+        if (STAGE == 1) {
+            float r = L.v[LED_BOUND];
+            for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(FULL, r, o);
+            if (lane == 0 && r != 0.f) atomicAdd(&P.st->ledPend, (double)r);
+            __threadfence();  // before the dt ticket: the last CTA folds ledPend
+        } else {
+            flushLed(L, P.st->led);
+        }
+    }
     if (STAGE == 1) {
         __syncthreads();
         finishDt(P, tmxAll, tmyAll, &last);
@@ -324,6 +343,9 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
     const int nItems = 2 * P.st->nStrips;
     const StageConsts C = blockConsts<1>(P);
     const size_t pl = (size_t)P.planeSize;
+    const bool led = (cellFlags<FIX>(C.fl) & F_CHECKVOL) != 0;
+    Led L;
+    ledZero(L);
     for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
         const int strip = P.strips[item >> 1];
         const int half = item & 1;
@@ -373,7 +395,7 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
                     wetAny |= cellUpdate<1, false, false, FIX>(P, C, tile, Y0 + r0 + q, i, v[q][0],
                                                           v[q][1], v[q][2], v[q][3], v[q][4],
                                                           v[q][5], 0.f, 0.f, 0.f, 0.f, pre,
-                                                          edgeStrip);
+                                                          edgeStrip, led ? &L : nullptr);
                 }
             }
             if (C.euler && wetAny) atomicOr(&twet[slot], 1);
@@ -384,6 +406,7 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
                 P.wet[by * P.nBX + STRIP_TX * sx + tid] = (uint8_t)((!(C.fl & F_TILE_ACC)) || twet[tid]);
         }
     }
+    if (led) flushLed(L, P.st->led);
 }
 
 }  // namespace rift

@@ -338,6 +338,9 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
     const bool euler = (fl & F_EULER) != 0;
     const bool tableOk = !track && !euler && P.owner != nullptr;
     const bool spare = blockIdx.x == gridDim.x - 1;
+    const bool led = (cellFlags<FIX>(fl) & F_CHECKVOL) != 0;  // check_volume ledger
+    Led L;
+    ledZero(L);
     tileInit(S, &tmA, &tmE);
     if (tid == 0) {
         prefetch_tmap(&tmB);
@@ -421,7 +424,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             // publishes it during stage 2, when no CTA reads the old value.
             bool mine = tile >= 0;
             int bX, bY, i0 = 0, j0 = 0;
-            float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f;
+            float pre[6], dh = 0.f, dhu = 0.f, dhv = 0.f, spx = 0.f, spy = 0.f, bin1 = 0.f;
             if (tid == 0 && mine) issueTile(S.buf[0], &S.bar[0], &tmA, &tmE, P, tile);
             bool wetOld = false, live = true;
             if (mine) {
@@ -445,7 +448,8 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                 }
                 ph[0] ^= 1u;
                 if (live) {
-                    tileFluxDiv<true>(S, S.buf[0], P, i0, j0, dh, dhu, dhv, spx, spy);
+                    tileFluxDiv<true>(S, S.buf[0], P, i0, j0, dh, dhu, dhv, spx, spy,
+                                      led ? &bin1 : nullptr);
                     const float mxv = blockMax(spx, S.red[0]);
                     const float myv = blockMax(spy, S.red[1]);
                     if (tid == 0) {
@@ -532,7 +536,9 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
             nActPrev = sSched;
             if (mine) {  // the rest of the stage-1 update with this step's dt (Integrate_1_k)
                 const StageConsts C1 = sC[0];
-                const bool wetCell = tileCellFinish<1, FIX>(P, C1, S.buf[0], i0, j0, sSrc[tid], pre);
+                L.v[LED_BOUND] += C1.wRate * bin1;
+                const bool wetCell = tileCellFinish<1, FIX>(P, C1, S.buf[0], i0, j0, sSrc[tid], pre,
+                                                            led ? &L : nullptr);
                 tileFlags<1>(P, C1, S, tile, wetCell, 0.f, 0.f);
                 __syncthreads();
             }
@@ -559,10 +565,12 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                         return;
                     }
                     ph[1] ^= 1u;
-                    float sx2, sy2;
-                    tileFluxDiv<true>(S, S.buf[1], P, i0, j0, dh, dhu, dhv, sx2, sy2);
-                    const bool wetCell =
-                        tileCellUpdate<2, FIX>(P, C2, S.buf[1], tile, i0, j0, dh, dhu, dhv, pre);
+                    float sx2, sy2, bin2 = 0.f;
+                    tileFluxDiv<true>(S, S.buf[1], P, i0, j0, dh, dhu, dhv, sx2, sy2,
+                                      led ? &bin2 : nullptr);
+                    L.v[LED_BOUND] += C2.wRate * bin2;
+                    const bool wetCell = tileCellUpdate<2, FIX>(P, C2, S.buf[1], tile, i0, j0, dh, dhu,
+                                                                dhv, pre, led ? &L : nullptr);
                     const bool wetNew = tileFlags<2>(P, C2, S, tile, wetCell, sx2, sy2);
                     if ((table || built) && wetNew && !wetOld && tid < 4)
                         tableClaim(P, tile, &sOverflow);
@@ -602,6 +610,7 @@ __global__ void __launch_bounds__(NT, 4) k_persist(const __grid_constant__ CUten
                     publishGrow(st);
                 }
             }
+            if (led) flushLed(L, st->led);
             int voided = 0;
             if (!gridSync(P.gbar, barTarget, st, sOverflow != 0, &voided)) return;
             if (tid == 0) sOverflow = 0;

@@ -289,7 +289,7 @@ int Simulator::initSimulation() {
               (save_arrival_time ? RIFT_F_SAVE_ARRIVAL : 0) |
               (tile_acceleration ? RIFT_F_TILE_ACCEL : 0) |
               ((dambreak || coupled_source) ? RIFT_F_POINT_SOURCE : 0) |
-              (h_init ? RIFT_F_H_INIT : 0);
+              (h_init ? RIFT_F_H_INIT : 0) | (check_volume ? RIFT_F_CHECK_VOLUME : 0);
     g.device = device;
     if ((rc = rift_create(&g, &R))) return engineFail(rc, "rift_create");
     if ((rc = rift_upload_static(R, BX.data(), BY.data(), h_n.data(),

@@ -122,6 +122,7 @@ class Case:
 RAIN_UNIFORM, RAIN_GRID, DRAIN_UNIFORM, DRAIN_GRID = 1, 2, 4, 8
 INFILTRATION, SURGE_GRID, EULER, SAVE_MAX = 16, 32, 64, 128
 SAVE_ARRIVAL, TILE_ACCEL, POINT_SOURCE, H_INIT = 256, 512, 1024, 2048
+CHECK_VOLUME = 4096
 
 
 def csv_series(hours, rates):

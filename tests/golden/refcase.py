@@ -85,3 +85,41 @@ def read_dump(out, step, nx, ny, grid_size, names=("w", "hu", "hv")):
     t = np.fromfile(pre + "t.bin", dtype=np.float64)
     r["t"], r["dt"] = float(t[0]), float(t[1])
     return r
+
+
+def run(case, nsteps, dump=(), maps=None, map_times=None, extra=None, state=None, workdir=None):
+    """Run the reference's own kernels (oracle/refkit/refrun with the prebuilt
+    fatbin) on `case`; returns (the runner's JSON record, {step: dump},
+    steps.txt rows).  `state`: a snapshot (reference representation) to start
+    from.  Raises RuntimeError when the runner or the fatbin is missing."""
+    import json
+    import shutil
+    import subprocess
+    import tempfile
+
+    from oracle import build as ob
+    fat = ob.fatbin_path()
+    if not os.path.exists(fat):
+        raise RuntimeError("reference fatbin missing")
+    exe = ob.build_refrun()
+    if exe is None:
+        raise RuntimeError("no nvcc to build the runner")
+    d = tempfile.mkdtemp(prefix="rift_ref_", dir=workdir)
+    try:
+        write_case(case, d, nsteps, dump=dump, maps=maps, map_times=map_times, extra=extra)
+        if state is not None:
+            write_state(d, state)
+        out = os.path.join(d, "out")
+        os.makedirs(out)
+        r = subprocess.run([exe, fat, d, out], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"refrun rc={r.returncode}: {r.stderr[-500:]}")
+        rec = json.loads(r.stdout.strip().splitlines()[-1])
+        nbx, nby = -(-case.h_nx // 16), -(-case.h_ny // 14)
+        steps = sorted(set(dump) | ({rec["steps"]} if (extra or {}).get("dump_final") else set()))
+        dumps = {s: read_dump(out, s, case.h_nx, case.h_ny, nbx * nby,
+                              names=("w", "hu", "hv", "F", "hmax", "twet")) for s in steps}
+        log = np.loadtxt(os.path.join(out, "steps.txt"), ndmin=2)
+        return rec, dumps, log
+    finally:
+        shutil.rmtree(d, ignore_errors=True)

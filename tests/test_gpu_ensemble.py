@@ -82,3 +82,37 @@ def test_ensemble_rejects_bad_members(engine_api):
     b = FX.start(capi.Sim(case, api=engine_api), fx)
     with pytest.raises(capi.RiftError):
         capi.Ensemble([b, b])
+
+
+def test_ensemble_members_match_the_reference_kernels(engine_api):
+    """Every golden case stepped inside the ensemble kernel, all together,
+    checked at its dump steps against the reference's own kernels (the
+    golden dumps): tile sets bit-exact, t within 1e-5 relative, depths within
+    the golden bars (1e-6 m on 99% of the cells, 5e-5 m everywhere)."""
+    names = list(FX.CASES)
+    fxs = [FX.load(n)[0] for n in names]
+    members = _members(engine_api, names)
+    ens = capi.Ensemble(members)
+    done = [0] * len(names)
+    targets = sorted({s for fx in fxs for s in FX.dumps(fx)})
+    for s in targets:
+        live = [m for m, fx in enumerate(fxs) if max(FX.dumps(fx)) >= s]
+        # members past their last dump stay in the kernel; advance everyone to s
+        steps = s - min(done[m] for m in live)
+        t, k = ens.run(max_steps=steps)
+        for m in range(len(names)):
+            done[m] += int(k[m])
+        for m in live:
+            fx = fxs[m]
+            if s not in FX.dumps(fx):
+                continue
+            assert done[m] == s, (names[m], done[m], s)
+            ref = FX.ref_state(fx, s)
+            wet, act = members[m].tiles()
+            assert np.array_equal(wet, ref["wet"]), f"{names[m]}: wet tiles at step {s}"
+            assert np.array_equal(act, ref["active"]), f"{names[m]}: active tiles at step {s}"
+            tm = members[m].time()[0]
+            assert abs(tm - ref["t"]) <= 1e-5 * max(1.0, abs(ref["t"])), (names[m], tm, ref["t"])
+            d = np.abs(FX.interior(members[m].field("W") - ref["w"]))
+            assert np.quantile(d, 0.99) <= Q99 and d.max() <= MAX, f"{names[m]} step {s}: {d.max()}"
+    ens.close()

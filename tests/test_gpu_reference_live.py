@@ -1,0 +1,97 @@
+"""Parity with the reference's own step on the benchmark workloads, run live
+on this GPU: the reference's unmodified grid.cu kernels (the prebuilt
+sm_103a fatbin, driven in RunSimulation order by oracle/refkit/refrun) and
+the engine on identical inputs.
+
+- The small plain workload (512 x 512 cells at 10 m, bumpy plane, 50 mm/hr
+  for 30 minutes, rimmed), run for one simulated hour from t0: tile wet flags
+  and active lists bit-exact at the checked steps and at the end, simulated
+  time within 1e-5 relative, max |dh| <= 1e-4 m over the interior after the
+  hour (the spec bar).
+- A 200-step window of the mostly dry channel flood (2048 x 2048 at 5 m,
+  point hydrograph and Green-Ampt), both codes starting from the state the
+  reference reached at 3600 s: tile sets bit-exact at every checked step,
+  depths within the golden bars (1e-6 m on 99% of the cells, 5e-5 m
+  everywhere), infiltrated depth F likewise.
+
+The FP64 oracle's distance from the reference over the same hour is printed
+beside the engine's, so each error is stated against an FP64 restatement of
+the same scheme."""
+import numpy as np
+import pytest
+
+import refcase
+from rift_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+HOUR = 3600.0
+
+
+def _ref(case, nsteps, **kw):
+    try:
+        return refcase.run(case, nsteps, **kw)
+    except RuntimeError as e:
+        pytest.skip(f"reference kernels unavailable: {e}")
+
+
+def _interior_h(w, bc):
+    return (w - bc)[2:-2, 2:-2]
+
+
+def test_config1_one_hour_against_the_reference_step(engine_api, oracle_api):
+    case = synth.config1(N=512, tf=HOUR)
+    checks = (1, 200)
+    rec, dumps, log = _ref(case, 2 ** 31 - 1, dump=checks, extra={"t_stop": HOUR, "dump_final": 1})
+    n = rec["steps"]
+    assert rec["t"] >= HOUR and n > checks[-1]
+    eng = capi.Sim(case, api=engine_api).setup()
+    bc = eng.field("BC")
+    done = 0
+    for s in sorted(dumps):
+        t, _, k = eng.run(s - done)
+        done += k
+        assert done == s
+        ref = dumps[s]
+        wet, act = eng.tiles()
+        assert np.array_equal(wet, ref["wet"]), f"wet tiles at step {s}: {np.sum(wet != ref['wet'])} differ"
+        assert np.array_equal(act, ref["active"]), f"active tiles at step {s}"
+        assert abs(t - ref["t"]) <= 1e-5 * ref["t"], (s, t, ref["t"])
+    dh = np.abs(_interior_h(eng.field("W"), bc) - _interior_h(dumps[n]["w"], bc))
+    # the FP64 restatement of the same scheme over the same steps
+    lib, _ = oracle_api
+    import os
+    lib.rift_oracle_set_threads(os.cpu_count() or 1)
+    orc = capi.Sim(case, api=oracle_api, create_mode=0).setup()
+    orc.run(n)
+    do = np.abs(_interior_h(orc.field("W"), bc) - _interior_h(dumps[n]["w"], bc))
+    print(f"config1 512^2, {n} steps to t = {rec['t']:.3f} s: max |dh| engine {dh.max():.2e} m, "
+          f"FP64 oracle {do.max():.2e} m, q99 engine {np.quantile(dh, 0.99):.2e} m")
+    assert dh.max() <= 1e-4, dh.max()
+    eng.close()
+    orc.close()
+
+
+def test_config2_window_against_the_reference_step(engine_api):
+    case = synth.config2(N=2048)
+    _, spun, _ = _ref(case, 2 ** 31 - 1, extra={"t_stop": HOUR, "dump_final": 1, "dump_bc": 0})
+    (n0, st), = spun.items()
+    snap = dict(t=st["t"], dt=st["dt"], w=st["w"], hu=st["hu"], hv=st["hv"], F=st["F"],
+                wet=st["wet"], active=st["active"], mx=st["mx"], my=st["my"])
+    checks = (1, 50, 200)
+    _, dumps, log = _ref(case, checks[-1], dump=checks, state=snap)
+    eng = capi.Sim(case, api=engine_api).setup()
+    eng.load_snapshot(snap)
+    done = 0
+    for s in checks:
+        t, _, k = eng.run(s - done)
+        done += k
+        ref = dumps[s]
+        wet, act = eng.tiles()
+        assert np.array_equal(wet, ref["wet"]), f"wet tiles at window step {s}"
+        assert np.array_equal(act, ref["active"]), f"active tiles at window step {s}"
+        assert abs(t - ref["t"]) <= 1e-5 * ref["t"], (s, t, ref["t"])
+        for field, key in (("W", "w"), ("F", "F")):
+            d = np.abs((eng.field(field) - ref[key])[2:-2, 2:-2])
+            assert np.quantile(d, 0.99) <= 1e-6 and d.max() <= 5e-5, (s, field, d.max())
+    eng.close()
