@@ -265,6 +265,11 @@ typedef struct rift_ensemble rift_ensemble;
 int rift_ensemble_create(rift_handle* const* members, int32_t n, rift_ensemble** out);
 int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double* t_out,
                       int32_t* steps_out);
+/* Per member (n entries): the device time, in seconds, from the start of the
+ * last rift_ensemble_run's kernel to the end of the member's last step in it
+ * (the GPU's global timer, read when the member's final iteration ends); 0
+ * for a member that ran no step. */
+int rift_ensemble_member_times(rift_ensemble* e, double* seconds);
 const char* rift_ensemble_last_error(rift_ensemble* e);
 void rift_ensemble_destroy(rift_ensemble* e);
 

@@ -98,6 +98,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                   [_P, C.c_double, C.c_int32, _D, C.POINTER(C.c_int32)])
         ns["ensemble_last_error"] = _sig(lib, p + "ensemble_last_error", C.c_char_p, [_P])
         ns["ensemble_destroy"] = _sig(lib, p + "ensemble_destroy", None, [_P])
+        if hasattr(lib, p + "ensemble_member_times"):
+            ns["ensemble_member_times"] = _sig(lib, p + "ensemble_member_times", C.c_int, [_P, _D])
     if hasattr(lib, p + "autotune"):
         ns["autotune"] = _sig(lib, p + "autotune", C.c_int, [_P, C.c_int32, _I, _D])
     if hasattr(lib, p + "set_persistent"):
@@ -413,6 +415,14 @@ class Ensemble:
             raise RiftError(f"ensemble_run failed: {ERRORS.get(rc, rc)} "
                             f"{self.f['ensemble_last_error'](self.h).decode()}")
         return t, k
+
+    def member_times(self):
+        """Device seconds from the last run's start to each member's end."""
+        out = np.zeros(len(self.sims))
+        rc = self.f["ensemble_member_times"](self.h, _dp(out))
+        if rc != RIFT_OK:
+            raise RiftError(f"ensemble_member_times failed: {ERRORS.get(rc, rc)}")
+        return out
 
     def close(self):
         if getattr(self, "h", None):

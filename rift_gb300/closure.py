@@ -536,9 +536,15 @@ class EnsembleClosure:
         self.chunks = 0  # ensemble launches (one kernel each)
 
     def run(self, t_stop):
+        """Run every member to t_stop; finish_wall[m] is the host time from
+        the call's start to the end of the chunk in which member m reached
+        t_stop (its closure step included)."""
+        import time
         torch = _torch()
         t_prev = np.array([s.time()[0] for s in self.sims])
         steps = np.zeros(len(self.sims), dtype=np.int64)
+        self.finish_wall = np.zeros(len(self.sims))
+        t0 = time.perf_counter()
         while True:
             t, k = self.ens.run(t_stop=t_stop, max_steps=self.every)
             self.chunks += 1
@@ -550,6 +556,9 @@ class EnsembleClosure:
             # the closure kernels run on the members' streams, the ensemble
             # kernel on its own: finish them before the next launch
             torch.cuda.synchronize()
+            now = time.perf_counter() - t0
+            for m in np.nonzero((t >= t_stop) & (t_prev < t_stop))[0]:
+                self.finish_wall[m] = now
             t_prev = t
             if (t >= t_stop).all():
                 break

@@ -1699,6 +1699,7 @@ int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* 
 // ---------------------------------------------------------------- ensembles
 struct rift_ensemble {
     std::vector<rift_handle*> m;
+    std::vector<double> memberSec;  // last run: device time from its start to each member's end
     cudaStream_t stream = nullptr;
     Params* dP = nullptr;
     CUtensorMap* dMaps = nullptr;
@@ -1786,6 +1787,16 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
     ENS_TRY(e, cudaLaunchCooperativeKernel((const void*)k_ensemble, dim3(e->grid), dim3(NT), args, 0,
                                            e->stream));
     ENS_TRY(e, cudaStreamSynchronize(e->stream));
+    {  // each member's completion on the device clock
+        std::vector<unsigned long long> done(n, 0ull);
+        unsigned long long t0 = 0ull;
+        ENS_TRY(e, cudaMemcpy(done.data(), e->dE->tDone, sizeof(unsigned long long) * n,
+                              cudaMemcpyDeviceToHost));
+        ENS_TRY(e, cudaMemcpy(&t0, &e->dE->t0, sizeof(t0), cudaMemcpyDeviceToHost));
+        e->memberSec.assign(n, 0.0);
+        for (int k = 0; k < n; k++)
+            if (live[k] && done[k] >= t0) e->memberSec[k] = 1e-9 * (double)(done[k] - t0);
+    }
     int rc = RIFT_OK;
     for (int k = 0; k < n; k++) {
         rift_handle* h = e->m[k];
@@ -1799,6 +1810,13 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
         e->steps += h->hst->steps_done;
     }
     return rc;
+}
+
+int rift_ensemble_member_times(rift_ensemble* e, double* seconds) {
+    if (!e || !seconds) return RIFT_ERR_ARG;
+    for (size_t k = 0; k < e->m.size(); k++)
+        seconds[k] = k < e->memberSec.size() ? e->memberSec[k] : 0.0;
+    return RIFT_OK;
 }
 
 const char* rift_ensemble_last_error(rift_ensemble* e) { return e ? e->err.c_str() : "null ensemble"; }

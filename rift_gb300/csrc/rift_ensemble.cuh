@@ -35,7 +35,15 @@ struct EnsDev {
     int live[2][ENS_MAX];  // liveness per step parity
     int nAlive[2];
     StageConsts consts[ENS_MAX][2];  // each member's stage constants of the step (phase D)
+    unsigned long long t0;                // globaltimer at the kernel's start (ns)
+    unsigned long long tDone[ENS_MAX];    // globaltimer when each member finished its last step
 };
+
+__device__ __forceinline__ unsigned long long globalTimerNs() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 struct EnsArgs {
     const Params* Ps;        // [n] member parameters
@@ -241,6 +249,7 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
     uint32_t ph[2] = {0u, 0u};
     unsigned barTarget = 0u;
     DevState* st0 = E.Ps[0].st;  // barrier timeouts are recorded in member 0
+    if (blockIdx.x == 0 && tid == 0) D->t0 = globalTimerNs();  // before any member can finish
 #define ENS_SYNC()                               \
     if (!gridSync(&D->bar, barTarget, st0)) return; \
     (void)0
@@ -407,6 +416,9 @@ __global__ void __launch_bounds__(NT, 4) k_ensemble(EnsArgs E) {
             commitTile(E.Ps[m], E.Ps[m].act[g - Q.offs2[m]]);
         }
         ENS_SYNC();
+        // members whose last step this iteration was: its end on the device clock
+        for (int m = blockIdx.x * NT + tid; m < n; m += gridDim.x * NT)
+            if (live[m] && !D->live[cur ^ 1][m]) D->tDone[m] = globalTimerNs();
     }
 #undef ENS_SYNC
 }

@@ -104,8 +104,15 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
 //          ComputeTimestep), re-sync of U* on tiles that went inactive.
 // STAGE 2: reads U* (B) and U^n (A) at the cell -> writes U^{n+1} (A),
 //          F^{n+1} (FA), outputs, tile wet flags and tile speeds.
+#ifndef RIFT_MARCH1_MINB
+#define RIFT_MARCH1_MINB 6
+#endif
+#ifndef RIFT_MARCH2_MINB
+#define RIFT_MARCH2_MINB 6
+#endif
 template <int STAGE, uint32_t FIX = 0>
-__global__ void __launch_bounds__(MT, 6) k_march(const __grid_constant__ CUtensorMap tmIn,
+__global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH2_MINB)
+    k_march(const __grid_constant__ CUtensorMap tmIn,
                                               const __grid_constant__ CUtensorMap tmE, Params P) {
     __shared__ MarchSmem S;
     __shared__ bool last;

@@ -116,3 +116,23 @@ def test_ensemble_members_match_the_reference_kernels(engine_api):
             d = np.abs(FX.interior(members[m].field("W") - ref["w"]))
             assert np.quantile(d, 0.99) <= Q99 and d.max() <= MAX, f"{names[m]} step {s}: {d.max()}"
     ens.close()
+
+
+def test_ensemble_member_times_follow_completion(engine_api):
+    """Members of different dt reach t_stop after different step counts: the
+    device clock has each one finish no later than a member that ran more
+    iterations of the shared loop, and every member that ran has a positive
+    completion time inside the call's wall time."""
+    import time
+    names = ["rain", "front", "euler"]
+    members = _members(engine_api, names)
+    ens = capi.Ensemble(members)
+    w0 = time.perf_counter()
+    t, k = ens.run(t_stop=40.0)
+    wall = time.perf_counter() - w0
+    sec = ens.member_times()
+    assert (sec > 0).all() and (sec <= wall).all(), (sec, wall)
+    order = np.argsort(k)
+    assert k[order[0]] < k[order[-1]]
+    assert sec[order[0]] <= sec[order[-1]]
+    ens.close()
