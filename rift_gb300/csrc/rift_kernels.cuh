@@ -145,6 +145,7 @@ struct Params {
     uint8_t* stripFlag;
     int nSX, nSY;      // strip grid (strips of 7 x 2 tiles)
     int marchMin;      // active strips from which the march kernels run
+    int fuse;          // march, RK2: stage 2 rebuilds U* (k_march2f) on the strips that qualify
     int persistMax;    // the persistent step kernel runs while active tiles <= this
     struct GridBar* gbar;            // grid barrier of the persistent kernel
     int* owner;        // [gridSize] tile -> CTA of the persistent loop's tile table, or -1
@@ -1048,6 +1049,34 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
     return r;
 }
 
+// The RK stage-1 combination of Integrate_1_k (grid.cu:856-922) from a
+// cell's sources: the surge condition, the explicit depth update, the
+// semi-implicit Manning division of the momenta and the epsilon clamp.
+// Shared by the stage-1 pass and by the stage-2 march that rebuilds U* from
+// U^n and the stored divergence, so both give the same bits.
+template <uint32_t FIX = 0>
+__device__ __forceinline__ void rk1Core(const Params& P, const StageConsts& C, size_t c,
+                                        const CellSrc& src, float hC, float hu0, float hv0, Led* L,
+                                        float& hN, float& huN, float& hvN) {
+    const uint32_t fl = cellFlags<FIX>(C.fl);
+    const float dtNew = C.dtNew, hc = src.hc;
+    float dh = src.dh;
+    if (fl & F_SURGE) {
+        float sg = mapValue(P, 2, c, C.fac2);
+        if (sg != P.nodata && sg > 0.f) {
+            const float d0 = dh;
+            dh = (sg - (hc + dh * dtNew)) / dtNew;
+            if (L) L->v[LED_SURGE] += C.wRate * (dh - d0);
+        }
+    }
+    hN = hc + dh * dtNew;
+    const float den = 1.f / (1.f - dtNew * src.G);
+    huN = (hu0 + src.dhu * dtNew) * den;
+    hvN = (hv0 + src.dhv * dtNew) * den;
+    if (L) L->v[LED_CLAMP] += C.wHalf * ((hC - hc) + ((hN > kEps) ? 0.f : hN));
+    hN = (hN > kEps) ? hN : 0.f;
+}
+
 // edge: the work item holds a cell next to the ghost band (i or j at 2 or
 // at n - 3); false skips the ghost tests for the items inside.
 // L (check_volume runs, else null): the cell's ledger terms are added to it.
@@ -1067,21 +1096,7 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
     bool wetCell = false;
     if (STAGE == 1) {
         // Integrate_1_k (grid.cu:856-922)
-        const float G = src.G;
-        if (fl & F_SURGE) {
-            float sg = mapValue(P, 2, c, C.fac2);
-            if (sg != P.nodata && sg > 0.f) {
-                const float d0 = dh;
-                dh = (sg - (hc + dh * dtNew)) / dtNew;
-                if (L) L->v[LED_SURGE] += C.wRate * (dh - d0);
-            }
-        }
-        hN = hc + dh * dtNew;
-        const float den = 1.f / (1.f - dtNew * G);
-        huN = (hu0 + dhu * dtNew) * den;
-        hvN = (hv0 + dhv * dtNew) * den;
-        if (L) L->v[LED_CLAMP] += C.wHalf * ((hC - hc) + ((hN > kEps) ? 0.f : hN));
-        hN = (hN > kEps) ? hN : 0.f;
+        rk1Core<FIX>(P, C, c, src, hC, hu0, hv0, L, hN, huN, hvN);
         if (fl & F_INFIL) C.Fout[c] = Fc + dF * dtNew;
         if (euler) {
             // Euler-mode outputs and wet flags (grid.cu:926-1023)

@@ -16,7 +16,7 @@ from rift_gb300 import capi, synth
 pytestmark = pytest.mark.gpu
 
 TERM_TOL = 1e-4   # |engine term - oracle term| / water moved
-CLOSE_TOL = 1e-5  # |engine residual| / water moved
+CLOSE_TOL = 1e-7  # |engine residual| / water moved (measured on GB300: at most 2.5e-8)
 TERMS = ("added", "drained", "infiltrated", "clamped", "surge", "boundary")
 
 SCHEDULES = {
@@ -44,6 +44,8 @@ def test_engine_ledger_matches_oracle(engine_api, oracle_api, name, steps, sched
         orc.step()
     Le, Lo = eng.ledger(), orc.ledger()
     scale = _scale(Lo)
+    worst = max(abs(Le[k] - Lo[k]) for k in TERMS + ("volume", "volume0")) / scale
+    print(f"{name}/{schedule}: largest term difference {worst:.2e} of the water moved")
     for k in TERMS + ("volume", "volume0"):
         assert abs(Le[k] - Lo[k]) <= TERM_TOL * scale, (name, schedule, k, Le[k], Lo[k])
     print(f"{name}/{schedule}: engine residual {Le['residual'] / scale:.2e}, "

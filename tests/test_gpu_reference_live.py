@@ -45,6 +45,8 @@ def test_config1_one_hour_against_the_reference_step(engine_api, oracle_api):
     rec, dumps, log = _ref(case, 2 ** 31 - 1, dump=checks, extra={"t_stop": HOUR, "dump_final": 1})
     n = rec["steps"]
     assert rec["t"] >= HOUR and n > checks[-1]
+    # the engine keeps its full volume ledger over the hour (check_volume)
+    case.flags |= synth.CHECK_VOLUME
     eng = capi.Sim(case, api=engine_api).setup()
     bc = eng.field("BC")
     done = 0
@@ -68,6 +70,15 @@ def test_config1_one_hour_against_the_reference_step(engine_api, oracle_api):
     print(f"config1 512^2, {n} steps to t = {rec['t']:.3f} s: max |dh| engine {dh.max():.2e} m, "
           f"FP64 oracle {do.max():.2e} m, q99 engine {np.quantile(dh, 0.99):.2e} m")
     assert dh.max() <= 1e-4, dh.max()
+    # volume drift against the integrated sources over the hour: the FP64
+    # oracle's ledger (the scheme itself) and the engine's (FP32 state)
+    Le, Lo = eng.ledger(), orc.ledger()
+    drift_e, drift_o = Le["residual"] / Le["added"], Lo["residual"] / Lo["added"]
+    print(f"config1 512^2, one hour: volume drift / integrated sources: engine {drift_e:.2e}, "
+          f"FP64 oracle {drift_o:.2e}; edge outflow {Le['boundary'] / Le['added']:.2e}, "
+          f"clamps {Le['clamped'] / Le['added']:.2e} of the sources")
+    assert abs(drift_o) <= 1e-9
+    assert abs(drift_e) <= 1e-6
     eng.close()
     orc.close()
 
