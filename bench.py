@@ -212,7 +212,6 @@ def run_ours(args, device=0, sync=None):
     # ---- e2e through the C ABI with host buffers ----------------------------
     t0 = time.perf_counter()
     sim = capi.Sim(case, device=device).set_schedule(args.schedule).set_persistent(args.persistent)
-    sim.set_stage_fusion(args.fusion)
     sim.setup()
     t_setup = time.perf_counter() - t0
     spin_up(sim, spin)
@@ -273,10 +272,10 @@ def run_ours(args, device=0, sync=None):
         achieved = active_cells * bytes_per / (ms * 1e-3) / 1e9
         launches = 1
     else:
-        kernel = ("RK stages 1+2 (k_march<1>, k_update1, k_march<2>, k_march2f or k_stage<1>, "
-                  "k_stage<2>; one schedule runs, the other exits at entry)")
+        kernel = ("RK stages 1+2 (k_march<1>, k_update1, k_march<2> or k_stage<1>, k_stage<2>; one "
+                  "schedule runs, the other exits at entry)")
         achieved = stage_cells * bytes_per / (stage_ms * 1e-3) / 1e9 if stage_ms > 0 else None
-        launches = graph_steps * launches_per_step(case.flags, args.fusion) + (1 if persist_steps else 0)
+        launches = graph_steps * launches_per_step(case.flags) + (1 if persist_steps else 0)
     # DRAM bytes (read + write) of the reported kernel per launch, from the
     # ncu capture summarised under profiles/ (per step there)
     traffic = None
@@ -317,7 +316,7 @@ def run_ours(args, device=0, sync=None):
         "clocks": clk,
         "gpu_launches": launches,
         "path": {"persistent_steps": persist_steps, "graph_steps": graph_steps,
-                 "autotune": tuned, "stage_fusion": bool(args.fusion)},
+                 "autotune": tuned},
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, snap, args)
@@ -325,14 +324,12 @@ def run_ours(args, device=0, sync=None):
     return line
 
 
-def launches_per_step(flags, fusion=True):
+def launches_per_step(flags):
     """Kernels one step's graph launches: k_track (gridded rain or surge),
     k_grow, the speed/dt kernel and the stage kernels of both schedules (the
-    schedule not chosen for the step exits at entry), k_march2f with stage
-    fusion, k_commit in Euler mode."""
+    schedule not chosen for the step exits at entry), k_commit in Euler
+    mode."""
     n = 1 + 2 + 2 + (1 if flags & synth.EULER else 2)
-    if fusion and not flags & synth.EULER:
-        n += 1
     if flags & (synth.RAIN_GRID | synth.SURGE_GRID):
         n += 1
     return n
@@ -724,8 +721,6 @@ def main():
     ap.add_argument("--autotune", type=int, default=0,
                     help="before the timed region, time each schedule for this many steps "
                          "from the spun-up state and keep the fastest (0: off)")
-    ap.add_argument("--no-fusion", dest="fusion", action="store_false",
-                    help="column march: stage 2 reads U* from memory instead of rebuilding it")
     ap.add_argument("--persistent", type=int, default=-1,
                     help="persistent step loop while at most this many tiles are active "
                          "(-1: engine default, 0: off)")

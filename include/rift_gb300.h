@@ -235,15 +235,6 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total,
  * per resident march CTA); 0 forces the march, a huge value the tiles. */
 int rift_set_schedule(rift_handle* h, int32_t march_min_strips);
 
-/* Stage fusion of the column march (no reference counterpart): on (the
- * default), RK stage 2 rebuilds U* from U^n and the stored stage-1
- * divergence for every strip whose staged block holds no ghost cell
- * (k_march2f), and the separate stage-1 update pass runs only on the strips
- * near the domain edge; off, every strip runs the stage-1 update pass and
- * stage 2 reads U* from memory.  Both give the same results; Euler runs
- * always run the separate pass. */
-int rift_set_stage_fusion(rift_handle* h, int32_t on);
-
 /* Persistent step loop (no reference counterpart): while at most
  * max_active_tiles tiles are active, rift_run / rift_step run their steps
  * in one cooperative launch whose phases are separated by grid barriers,

@@ -89,8 +89,6 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
         ns["mass_ledger_terms"] = _sig(lib, p + "mass_ledger_terms", C.c_int, [_P, C.POINTER(Ledger)])
     if hasattr(lib, p + "set_point_rates"):
         ns["set_point_rates"] = _sig(lib, p + "set_point_rates", C.c_int, [_P, _D, C.c_int32])
-    if hasattr(lib, p + "set_stage_fusion"):
-        ns["set_stage_fusion"] = _sig(lib, p + "set_stage_fusion", C.c_int, [_P, C.c_int32])
     if hasattr(lib, p + "set_schedule"):
         ns["set_schedule"] = _sig(lib, p + "set_schedule", C.c_int, [_P, C.c_int32])
     if hasattr(lib, p + "ensemble_create"):
@@ -260,12 +258,6 @@ class Sim:
         (-1 default, 0 always march, a huge value always per-tile)."""
         if "set_schedule" in self.f:
             self._check(self.f["set_schedule"](self.h, march_min_strips), "set_schedule")
-        return self
-
-    def set_stage_fusion(self, on):
-        """Stage 2 of the column march rebuilds U* (on, default) or reads it."""
-        if "set_stage_fusion" in self.f:
-            self._check(self.f["set_stage_fusion"](self.h, int(on)), "set_stage_fusion")
         return self
 
     def set_persistent(self, max_active_tiles):

@@ -28,7 +28,6 @@
 #include "rift_grow.cuh"
 #include "rift_kernels.cuh"
 #include "rift_march.cuh"
-#include "rift_march2f.cuh"
 #include "rift_persist.cuh"
 #include "rift_ensemble.cuh"
 
@@ -74,9 +73,6 @@ struct rift_handle {
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
     CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
-    CUtensorMap tmDm{};                  // the same box over the stored divergence
-    bool fusion = true;                  // k_march2f rebuilds U* in stage 2 (rift_set_stage_fusion)
-    int gridFused = 0;                   // k_march2f: resident CTAs
     cudaStream_t stream = nullptr;
     float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
     float* D = nullptr;  // [3] planes: the march's stage-1 divergence
@@ -273,7 +269,6 @@ Params makeParams(rift_handle* h) {
     P.nSX = h->nSX;
     P.nSY = h->nSY;
     P.marchMin = h->marchMin;
-    P.fuse = (h->fusion && !h->has(RIFT_F_EULER)) ? 1 : 0;
     P.persistMax = h->persistMax;
     P.gbar = h->gbar;
     P.owner = h->owner;
@@ -351,22 +346,6 @@ const void* persistKernel(const rift_handle* h) {
     }
 }
 
-// RK stage 2 of the march strips whose U* it rebuilds (k_march2f); the
-// kernel returns at once when the step runs the per-tile kernels or no fusion.
-void launchFused(const rift_handle* h, const Params& P, cudaStream_t s) {
-    if (!P.fuse) return;
-    switch (marchFix(h)) {
-        case FIX_RAIN: k_march2f<FIX_RAIN><<<h->gridFused, MT, 0, s>>>(h->tmAm, h->tmDm, h->tmEm, P); break;
-        case FIX_INFIL_SRC:
-            k_march2f<FIX_INFIL_SRC><<<h->gridFused, MT, 0, s>>>(h->tmAm, h->tmDm, h->tmEm, P);
-            break;
-        case FIX_RAINMAP_DRAIN:
-            k_march2f<FIX_RAINMAP_DRAIN><<<h->gridFused, MT, 0, s>>>(h->tmAm, h->tmDm, h->tmEm, P);
-            break;
-        default: k_march2f<><<<h->gridFused, MT, 0, s>>>(h->tmAm, h->tmDm, h->tmEm, P);
-    }
-}
-
 void launchUpdate1(const rift_handle* h, const Params& P, cudaStream_t s) {
     switch (marchFix(h)) {
         case FIX_RAIN: k_update1<FIX_RAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
@@ -391,7 +370,6 @@ void enqueueStep(rift_handle* h) {
     if (!h->has(RIFT_F_EULER)) {
         k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
         launchMarch<2>(h, h->tmBm, P, s, h->gridMarch);
-        launchFused(h, P, s);
     } else {
         k_commit<<<h->gridStage, NT, 0, s>>>(P);
     }
@@ -687,8 +665,7 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
         (r = encodeMap(h, &h->tmE, h->E, 4)) ||
         (r = encodeMap(h, &h->tmAm, h->A, 3, MBOXW, MRC)) ||
         (r = encodeMap(h, &h->tmBm, h->B, 3, MBOXW, MRC)) ||
-        (r = encodeMap(h, &h->tmEm, h->E, 4, MBOXW, MRC)) ||
-        (r = encodeMap(h, &h->tmDm, h->D, 3, MBOXW, MRC)))
+        (r = encodeMap(h, &h->tmEm, h->E, 4, MBOXW, MRC)))
         return r;
     h->nSX = (h->nBX + STRIP_TX - 1) / STRIP_TX;
     h->nSY = (h->nBY + STRIP_TY - 1) / STRIP_TY;
@@ -706,9 +683,6 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     int occ1 = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_march<1>, MT, 0);
     h->gridMarch1 = std::max(1, std::min(NS, h->numSMs * std::max(occ1, 1)));
-    int occF = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occF, k_march2f<>, MT, 0);
-    h->gridFused = std::max(1, std::min(NS, h->numSMs * std::max(occF, 1)));
     int occU = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1<>, MT, 0);
     h->gridUpdate = std::max(1, std::min(2 * NS, h->numSMs * std::max(occU, 1)));
@@ -1599,8 +1573,7 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
         if (!h->has(RIFT_F_EULER)) {
             k_stage<2><<<h->gridStage, NT, 0, s>>>(h->tmB, h->tmE, P);
             launchMarch<2>(h, h->tmBm, P, s, h->gridMarch);
-            launchFused(h, P, s);
-        } else {
+            } else {
             k_commit<<<h->gridStage, NT, 0, s>>>(P);
         }
         CUDA_TRY(h, cudaEventRecord(e1, s));
@@ -1616,13 +1589,6 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     if (active_total) *active_total = graphCells;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    return RIFT_OK;
-}
-
-int rift_set_stage_fusion(rift_handle* h, int32_t on) {
-    if (!h) return RIFT_ERR_ARG;
-    h->fusion = on != 0;
-    destroyGraph(h);
     return RIFT_OK;
 }
 

@@ -145,7 +145,6 @@ struct Params {
     uint8_t* stripFlag;
     int nSX, nSY;      // strip grid (strips of 7 x 2 tiles)
     int marchMin;      // active strips from which the march kernels run
-    int fuse;          // march, RK2: stage 2 rebuilds U* (k_march2f) on the strips that qualify
     int persistMax;    // the persistent step kernel runs while active tiles <= this
     struct GridBar* gbar;            // grid barrier of the persistent kernel
     int* owner;        // [gridSize] tile -> CTA of the persistent loop's tile table, or -1
@@ -428,8 +427,11 @@ __device__ __forceinline__ void publishDt(const Params& P, DevState* st, double 
         if (P.mapMode[0] == 2) add += (double)st->factor[0] * (st->rain_sum[1] - st->rain_sum[0]);
     }
     st->v_added += add * dt;
-    if (P.flags & F_CHECKVOL) {  // stage-1 edge inflow of a flux pass that ran before dt
-        st->led[LED_BOUND] += ((P.flags & F_EULER) ? 1.0 : 0.5) * dt * st->ledPend;
+    // stage-1 edge inflow of a flux pass that ran before dt (the column
+    // march).  Atomic: in the persistent loop other CTAs add their terms to
+    // the same total while this runs.
+    if ((P.flags & F_CHECKVOL) && st->ledPend != 0.0) {
+        atomicAdd(&st->led[LED_BOUND], ((P.flags & F_EULER) ? 1.0 : 0.5) * dt * st->ledPend);
         st->ledPend = 0.0;
     }
 }

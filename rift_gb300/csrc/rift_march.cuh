@@ -104,28 +104,11 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
 //          ComputeTimestep), re-sync of U* on tiles that went inactive.
 // STAGE 2: reads U* (B) and U^n (A) at the cell -> writes U^{n+1} (A),
 //          F^{n+1} (FA), outputs, tile wet flags and tile speeds.
-// The staged block of strip (sx, sy) -- its 112 x 28 cells and two more on
-// every side -- lies inside the interior: stage 2 can rebuild its U* from U^n
-// and the stored divergence (k_march2f).
-__device__ __forceinline__ bool stripFusableM(const Params& P, int sx, int sy) {
-    const int X0 = MCOLS * sx + 2, Y0 = MHR * sy + 2;
-    return X0 - 2 >= 2 && Y0 - 2 >= 2 && X0 + MCOLS + 1 <= P.nx - 3 && Y0 + MHR + 1 <= P.ny - 3;
-}
-
-// A strip that does not qualify, or one next to such a strip: k_march<2>
-// reads its U* from memory, so k_update1 writes it.
-__device__ __forceinline__ bool stripBandM(const Params& P, int sx, int sy) {
-    for (int dy = -1; dy <= 1; dy++)
-        for (int dx = -1; dx <= 1; dx++) {
-            const int x = sx + dx, y = sy + dy;
-            if (x < 0 || y < 0 || x >= P.nSX || y >= P.nSY) continue;
-            if (!stripFusableM(P, x, y)) return true;
-        }
-    return false;
-}
-
+// Resident CTAs per SM the march kernels are compiled for: the stage-1 flux
+// pass fits 8 (64 registers, 27 KB shared memory; measured 1% faster on the
+// 8192^2 step than 6), stage 2 needs its 80 registers at 6.
 #ifndef RIFT_MARCH1_MINB
-#define RIFT_MARCH1_MINB 6
+#define RIFT_MARCH1_MINB 8
 #endif
 #ifndef RIFT_MARCH2_MINB
 #define RIFT_MARCH2_MINB 6
@@ -163,7 +146,6 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
     for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
         const int strip = P.strips[item];
         const int sx = strip % P.nSX, sy = strip / P.nSX;
-        if (STAGE == 2 && P.fuse && stripFusableM(P, sx, sy)) continue;  // k_march2f's strip
         const int X0 = MCOLS * sx + 2, Y0 = MHR * sy + 2;
         // strip-uniform: does the strip reach the first or last interior row/column?
         const bool edgeStrip =
@@ -378,10 +360,6 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
         const int strip = P.strips[item >> 1];
         const int half = item & 1;
         const int sx = strip % P.nSX, sy = strip / P.nSX;
-        // with stage fusion only the strips whose U* k_march<2> reads; the
-        // ledger counts the cells that k_march2f does not update itself
-        if (P.fuse && !stripBandM(P, sx, sy)) continue;
-        Led* const Lc = (led && !(P.fuse && stripFusableM(P, sx, sy))) ? &L : nullptr;
         const int by = STRIP_TY * sy + half;  // the tile row of this item
         const int X0 = MCOLS * sx + 2, Y0 = by * TH + 2;
         const bool edgeStrip =
@@ -427,7 +405,7 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
                     wetAny |= cellUpdate<1, false, false, FIX>(P, C, tile, Y0 + r0 + q, i, v[q][0],
                                                           v[q][1], v[q][2], v[q][3], v[q][4],
                                                           v[q][5], 0.f, 0.f, 0.f, 0.f, pre,
-                                                          edgeStrip, Lc);
+                                                          edgeStrip, led ? &L : nullptr);
                 }
             }
             if (C.euler && wetAny) atomicOr(&twet[slot], 1);

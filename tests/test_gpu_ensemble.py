@@ -128,11 +128,11 @@ def test_ensemble_member_times_follow_completion(engine_api):
     members = _members(engine_api, names)
     ens = capi.Ensemble(members)
     w0 = time.perf_counter()
-    t, k = ens.run(t_stop=40.0)
+    t, k = ens.run(t_stop=600.0)
     wall = time.perf_counter() - w0
     sec = ens.member_times()
     assert (sec > 0).all() and (sec <= wall).all(), (sec, wall)
-    order = np.argsort(k)
-    assert k[order[0]] < k[order[-1]]
+    order = np.argsort(k, kind="stable")
+    assert k[order[0]] < k[order[-1]], k  # the wet cases take smaller steps than the dry front
     assert sec[order[0]] <= sec[order[-1]]
     ens.close()
