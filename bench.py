@@ -212,6 +212,7 @@ def run_ours(args, device=0, sync=None):
     # ---- e2e through the C ABI with host buffers ----------------------------
     t0 = time.perf_counter()
     sim = capi.Sim(case, device=device).set_schedule(args.schedule).set_persistent(args.persistent)
+    sim.set_march_rows(args.march_rows)
     sim.setup()
     t_setup = time.perf_counter() - t0
     spin_up(sim, spin)
@@ -246,8 +247,9 @@ def run_ours(args, device=0, sync=None):
     tuned = None
     if args.autotune > 0:
         choice, ms = sim.autotune(args.autotune)
-        tuned = {"choice": ["persistent", "graph+tiles", "graph+march"][choice],
-                 "ms_per_step": [None if np.isnan(x) else float(x) for x in ms]}
+        tuned = {"choice": capi.Sim.AUTOTUNE_CANDIDATES[choice],
+                 "ms_per_step": {n: (None if np.isnan(x) else float(x))
+                                 for n, x in zip(capi.Sim.AUTOTUNE_CANDIDATES, ms)}}
     for _ in range(args.warmup):
         sim.step()
     clocks = ClockSampler().start()
@@ -316,7 +318,7 @@ def run_ours(args, device=0, sync=None):
         "clocks": clk,
         "gpu_launches": launches,
         "path": {"persistent_steps": persist_steps, "graph_steps": graph_steps,
-                 "autotune": tuned},
+                 "autotune": tuned, "march_rows": sim.march_rows()},
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(case, snap, args)
@@ -721,6 +723,8 @@ def main():
     ap.add_argument("--autotune", type=int, default=0,
                     help="before the timed region, time each schedule for this many steps "
                          "from the spun-up state and keep the fastest (0: off)")
+    ap.add_argument("--march-rows", type=int, default=2, choices=(1, 2, 4),
+                    help="column march work items of this many 16 x 14 tile rows")
     ap.add_argument("--persistent", type=int, default=-1,
                     help="persistent step loop while at most this many tiles are active "
                          "(-1: engine default, 0: off)")

@@ -243,13 +243,26 @@ int rift_set_schedule(rift_handle* h, int32_t march_min_strips);
  * RIFT_ERR_UNSUPPORTED when the device has no cooperative launch. */
 int rift_set_persistent(rift_handle* h, int32_t max_active_tiles);
 
-/* Schedule autotuner (no reference counterpart): from the current state,
- * runs probe_steps steps on each schedule -- the persistent loop, the
- * per-step graph with the per-tile kernels, the graph with the column-march
- * kernels -- timing each with CUDA events, restores the state exactly, and
- * keeps the fastest (as rift_set_persistent / rift_set_schedule would set
- * it).  choice: 0, 1 or 2 in that order; ms_per_step[3] (may be NULL): the
- * measured times (NaN for a schedule not available). */
+/* Height of the column march's work items (no reference counterpart): 1, 2
+ * (default) or 4 reference tile rows, i.e. CTA items of 112 x 14, 112 x 28
+ * or 112 x 56 cells.  Each item stages its rows with a 2-row halo, so taller
+ * items stage fewer rows twice and shorter ones balance a ragged active set
+ * better.  The activity tiles stay 16 x 14: every height gives the same
+ * results. */
+int rift_set_march_rows(rift_handle* h, int32_t tile_rows);
+int rift_get_march_rows(rift_handle* h, int32_t* tile_rows);
+
+/* Autotuner of the schedule and the march's work-item shape (no reference
+ * counterpart): from the current state, runs probe_steps steps on each
+ * candidate -- 0 the persistent loop, 1 the per-step graph with the per-tile
+ * kernels (one 16 x 14 tile per CTA of 256 threads), 2, 3, 4 the graph with
+ * the column-march kernels on items of 2, 1 and 4 tile rows (128 threads per
+ * 7-tile-wide item) -- timing each with CUDA events, restores the state
+ * exactly, and keeps the fastest (as rift_set_persistent / rift_set_schedule
+ * / rift_set_march_rows would set it).  choice: the candidate's index;
+ * ms_per_step[RIFT_AUTOTUNE_CANDIDATES] (may be NULL): the measured times
+ * (NaN for a candidate not available). */
+#define RIFT_AUTOTUNE_CANDIDATES 5
 int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* ms_per_step);
 
 /* Ensembles (no reference counterpart; the reference runs one scenario per

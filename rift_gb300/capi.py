@@ -89,6 +89,9 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
         ns["mass_ledger_terms"] = _sig(lib, p + "mass_ledger_terms", C.c_int, [_P, C.POINTER(Ledger)])
     if hasattr(lib, p + "set_point_rates"):
         ns["set_point_rates"] = _sig(lib, p + "set_point_rates", C.c_int, [_P, _D, C.c_int32])
+    if hasattr(lib, p + "set_march_rows"):
+        ns["set_march_rows"] = _sig(lib, p + "set_march_rows", C.c_int, [_P, C.c_int32])
+        ns["get_march_rows"] = _sig(lib, p + "get_march_rows", C.c_int, [_P, _I])
     if hasattr(lib, p + "set_schedule"):
         ns["set_schedule"] = _sig(lib, p + "set_schedule", C.c_int, [_P, C.c_int32])
     if hasattr(lib, p + "ensemble_create"):
@@ -260,6 +263,17 @@ class Sim:
             self._check(self.f["set_schedule"](self.h, march_min_strips), "set_schedule")
         return self
 
+    def set_march_rows(self, tile_rows):
+        """Column march work items of 1, 2 or 4 tile rows."""
+        if "set_march_rows" in self.f:
+            self._check(self.f["set_march_rows"](self.h, tile_rows), "set_march_rows")
+        return self
+
+    def march_rows(self):
+        r = C.c_int32()
+        self._check(self.f["get_march_rows"](self.h, C.byref(r)), "get_march_rows")
+        return r.value
+
     def set_persistent(self, max_active_tiles):
         """Persistent cooperative step loop while at most this many tiles are
         active (-1 default, 0 off)."""
@@ -267,11 +281,15 @@ class Sim:
             self._check(self.f["set_persistent"](self.h, max_active_tiles), "set_persistent")
         return self
 
+    AUTOTUNE_CANDIDATES = ("persistent", "graph+tiles", "graph+march 2 rows", "graph+march 1 row",
+                           "graph+march 4 rows")
+
     def autotune(self, probe_steps=10):
-        """Time each kernel schedule from the current state, restore the
-        state, keep the fastest; returns (choice, ms per step of each)."""
+        """Time each kernel schedule and march work-item height from the
+        current state, restore the state, keep the fastest; returns (choice,
+        ms per step of each candidate, AUTOTUNE_CANDIDATES order)."""
         choice = C.c_int32()
-        ms = np.zeros(3)
+        ms = np.zeros(len(self.AUTOTUNE_CANDIDATES))
         self._check(self.f["autotune"](self.h, probe_steps, C.byref(choice), _dp(ms)), "autotune")
         return choice.value, ms
 

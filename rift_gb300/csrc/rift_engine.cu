@@ -72,6 +72,7 @@ struct rift_handle {
     long long persistSteps = 0, graphSteps = 0;  // steps run by each path (diagnostics)
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
+    int marchRows = STRIP_TY;  // tile rows per march work item (1, 2 or 4)
     CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
     cudaStream_t stream = nullptr;
     float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
@@ -324,16 +325,29 @@ uint32_t marchFix(const rift_handle* h) {
     return 0u;
 }
 
+template <int STAGE, int STY>
+void launchMarchRows(const rift_handle* h, const CUtensorMap& tmIn, const Params& P, cudaStream_t s,
+                     int grid) {
+    switch (marchFix(h)) {
+        case FIX_RAIN: k_march<STAGE, FIX_RAIN, STY><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P); break;
+        case FIX_INFIL_SRC:
+            k_march<STAGE, FIX_INFIL_SRC, STY><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
+            break;
+        case FIX_RAINMAP_DRAIN:
+            k_march<STAGE, FIX_RAINMAP_DRAIN, STY><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
+            break;
+        default: k_march<STAGE, 0, STY><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
+    }
+}
+
+// The march pass of STAGE with the handle's work-item height.
 template <int STAGE>
 void launchMarch(const rift_handle* h, const CUtensorMap& tmIn, const Params& P, cudaStream_t s,
                  int grid) {
-    switch (marchFix(h)) {
-        case FIX_RAIN: k_march<STAGE, FIX_RAIN><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P); break;
-        case FIX_INFIL_SRC: k_march<STAGE, FIX_INFIL_SRC><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P); break;
-        case FIX_RAINMAP_DRAIN:
-            k_march<STAGE, FIX_RAINMAP_DRAIN><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
-            break;
-        default: k_march<STAGE><<<grid, MT, 0, s>>>(tmIn, h->tmEm, P);
+    switch (h->marchRows) {
+        case 1: launchMarchRows<STAGE, 1>(h, tmIn, P, s, grid); break;
+        case 4: launchMarchRows<STAGE, 4>(h, tmIn, P, s, grid); break;
+        default: launchMarchRows<STAGE, 2>(h, tmIn, P, s, grid);
     }
 }
 
@@ -1592,6 +1606,21 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     return RIFT_OK;
 }
 
+int rift_set_march_rows(rift_handle* h, int32_t tile_rows) {
+    if (!h) return RIFT_ERR_ARG;
+    if (tile_rows != 1 && tile_rows != 2 && tile_rows != 4)
+        return fail(h, RIFT_ERR_ARG, "march work items are 1, 2 or 4 tile rows high");
+    h->marchRows = tile_rows;
+    destroyGraph(h);
+    return RIFT_OK;
+}
+
+int rift_get_march_rows(rift_handle* h, int32_t* tile_rows) {
+    if (!h || !tile_rows) return RIFT_ERR_ARG;
+    *tile_rows = h->marchRows;
+    return RIFT_OK;
+}
+
 int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_steps) {
     if (!h) return RIFT_ERR_ARG;
     if (persist_steps) *persist_steps = h->persistSteps;
@@ -1642,21 +1671,25 @@ int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* 
         }
         return RIFT_OK;
     };
-    const int keepPersist = h->persistMax, keepMarch = h->marchMin;
-    // candidates: persistent loop, per-step graph with tile kernels, with march kernels
-    const int persistOf[3] = {h->gridPersist > 0 ? INT32_MAX : -1, 0, 0};
-    const int marchOf[3] = {INT32_MAX, INT32_MAX, 0};
+    const int keepPersist = h->persistMax, keepMarch = h->marchMin, keepRows = h->marchRows;
+    // candidates: persistent loop; per-step graph with the tile kernels; with
+    // the march kernels on work items of 2, 1 and 4 tile rows
+    constexpr int NC = RIFT_AUTOTUNE_CANDIDATES;
+    const int persistOf[NC] = {h->gridPersist > 0 ? INT32_MAX : -1, 0, 0, 0, 0};
+    const int marchOf[NC] = {INT32_MAX, INT32_MAX, 0, 0, 0};
+    const int rowsOf[NC] = {keepRows, keepRows, 2, 1, 4};
     double best = INFINITY;
     int pick = 1;
-    double ms3[3] = {NAN, NAN, NAN};
+    double ms3[NC] = {NAN, NAN, NAN, NAN, NAN};
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     rc = copyAll(true);
     if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
         rc = fail(h, RIFT_ERR_CUDA, "cudaEventCreate");
-    for (int c = 0; c < 3 && !rc; c++) {
+    for (int c = 0; c < NC && !rc; c++) {
         if (persistOf[c] < 0) continue;
         h->persistMax = persistOf[c];
         h->marchMin = marchOf[c];
+        h->marchRows = rowsOf[c];
         destroyGraph(h);
         *h->hst = saved;
         h->hst->t_stop = INFINITY;
@@ -1685,6 +1718,7 @@ int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* 
     }
     h->persistMax = rc ? keepPersist : (pick == 0 ? INT32_MAX : 0);
     h->marchMin = rc ? keepMarch : marchOf[pick];
+    h->marchRows = rc ? keepRows : rowsOf[pick];
     destroyGraph(h);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
@@ -1692,7 +1726,7 @@ int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* 
     if (rc) return rc;
     if (choice) *choice = pick;
     if (ms_per_step)
-        for (int c = 0; c < 3; c++) ms_per_step[c] = ms3[c];
+        for (int c = 0; c < NC; c++) ms_per_step[c] = ms3[c];
     return RIFT_OK;
 }
 

@@ -256,18 +256,33 @@ __device__ __forceinline__ void tileOrigin(const Params& P, int tile, int& bX, i
 }
 
 // Gridded map value at a cell (hold or InterpGrid_k semantics, grid.cu:292-311).
-__device__ __forceinline__ float mapValue(const Params& P, int which, size_t c, float factor) {
+// Map value from the cell's entries x0, x1 of the two maps (InterpGrid_k,
+// grid.cu:292-311): hold mode reads x0; interpolation skips nodata entries.
+__device__ __forceinline__ float mapFrom(const Params& P, int which, float x0, float x1,
+                                         float factor) {
     // a series that was never set reads as its GridSeries fill value:
     // nodata for surge (allow_no_data), 0 otherwise
     if (P.mapMode[which] == 0) return which == 2 ? P.nodata : 0.f;
-    float x0 = P.map0[which][c];
     if (P.mapMode[which] != 2) return x0;
-    float x1 = P.map1[which][c];
     float nd = P.nodata;
     if (x1 == nd && x0 == nd) return nd;
     if (x1 == nd) return x0;
     if (x0 == nd) return x1;
     return factor * (x1 - x0) + x0;
+}
+
+__device__ __forceinline__ float mapValue(const Params& P, int which, size_t c, float factor) {
+    if (P.mapMode[which] == 0) return which == 2 ? P.nodata : 0.f;
+    const float x0 = P.map0[which][c];
+    const float x1 = P.mapMode[which] == 2 ? P.map1[which][c] : 0.f;
+    return mapFrom(P, which, x0, x1, factor);
+}
+
+// The cell's two rain-map entries, for a caller that loads them ahead of the
+// update (cellSources with RAINPRE reads them from pre[6], pre[7]).
+__device__ __forceinline__ void loadRainMaps(const Params& P, size_t c, float* q) {
+    q[0] = P.mapMode[0] != 0 ? P.map0[0][c] : 0.f;
+    q[1] = P.mapMode[0] == 2 ? P.map1[0][c] : 0.f;
 }
 
 // L1 prefetch of the gridded maps a cell update will read (rain, drain,
@@ -985,7 +1000,8 @@ struct CellSrc {
 };
 
 // BED: add the bed-slope source here (false: the caller's dhu, dhv hold it).
-template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0>
+// RAINPRE: the cell's rain-map entries were loaded ahead into pre[6], pre[7].
+template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0, bool RAINPRE = false>
 __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConsts& C, int tile,
                                                int j, int i, float dh, float dhu, float dhv,
                                                float hC, float hu0, float hv0, float eW, float eE,
@@ -999,7 +1015,7 @@ __device__ __forceinline__ CellSrc cellSources(const Params& P, const StageConst
     if (fl & F_RAIN_U) S0 += C.rainU;
     float rainG = 0.f;
     if (fl & F_RAIN_G) {
-        rainG = mapValue(P, 0, c, C.fac0);
+        rainG = RAINPRE ? mapFrom(P, 0, pre[6], pre[7], C.fac0) : mapValue(P, 0, c, C.fac0);
         S0 += rainG;
     }
     const float cap = hC * C.invDtSrc;
@@ -1153,14 +1169,15 @@ __device__ __forceinline__ bool cellFinish(const Params& P, const StageConsts& C
     return wetCell;
 }
 
-template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0>
+template <int STAGE, bool PREF = false, bool BED = true, uint32_t FIX = 0, bool RAINPRE = false>
 __device__ __forceinline__ bool cellUpdate(const Params& P, const StageConsts& C, int tile, int j,
                                            int i, float dh, float dhu, float dhv, float hC,
                                            float hu0, float hv0, float eW, float eE, float eS,
                                            float eN, const float* pre, bool edge = true,
                                            Led* L = nullptr) {
-    const CellSrc src = cellSources<STAGE, PREF, BED, FIX>(P, C, tile, j, i, dh, dhu, dhv, hC, hu0,
-                                                           hv0, eW, eE, eS, eN, pre);
+    const CellSrc src = cellSources<STAGE, PREF, BED, FIX, RAINPRE>(P, C, tile, j, i, dh, dhu, dhv,
+                                                                    hC, hu0, hv0, eW, eE, eS, eN,
+                                                                    pre);
     return cellFinish<STAGE, PREF, FIX>(P, C, j, i, src, hC, hu0, hv0, pre, edge, L);
 }
 

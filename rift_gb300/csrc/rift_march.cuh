@@ -52,14 +52,65 @@ static_assert(offsetof(MarchSlot, e) % 128 == 0, "TMA destination alignment");
 constexpr uint32_t MBYTES_S = 3 * MRC * MBOXW * 4;
 constexpr uint32_t MBYTES_E = 4 * MRC * MBOXW * 4;
 
+// Work items of the march are 112 columns wide and STY reference tile rows
+// high (STY = 1, 2 or 4: 14, 28 or 56 cells), chosen per handle
+// (rift_set_march_rows, the autotuner).  The grow lists strips of 7 x 2
+// tiles; an item of one tile row is half such a strip, one of four rows a
+// pair of vertically adjacent strips.
+constexpr int STY_MAX = 4;
+
 struct __align__(128) MarchSmem {
     MarchSlot slot[MNSLOT];
     uint64_t bar[MNSLOT];
-    unsigned tmx[STRIP_TX * STRIP_TY];
-    unsigned tmy[STRIP_TX * STRIP_TY];
-    int twet[STRIP_TX * STRIP_TY];
-    int tact[STRIP_TX * STRIP_TY];
+    unsigned tmx[STRIP_TX * STY_MAX];
+    unsigned tmy[STRIP_TX * STY_MAX];
+    int twet[STRIP_TX * STY_MAX];
+    int tact[STRIP_TX * STY_MAX];
 };
+
+// Does strip (sx, sy) of the grow's 7 x 2 strips hold an active tile?
+__device__ __forceinline__ bool stripHasActive(const Params& P, int sx, int sy) {
+    for (int q = 0; q < STRIP_TX * STRIP_TY; q++) {
+        const int bx = STRIP_TX * sx + q % STRIP_TX, by = STRIP_TY * sy + q / STRIP_TX;
+        if (bx < P.nBX && by < P.nBY && P.prevAct[by * P.nBX + bx] && bx * TW + 2 <= P.nx - 3 &&
+            by * TH + 2 <= P.ny - 3)
+            return true;
+    }
+    return false;
+}
+
+// Work item `item` of an STY-row march: its strip column and first tile row;
+// false when the item is covered by another one (STY = 4: the upper strip of
+// a pair whose lower strip is listed).  Items: 2 x the listed strips for
+// STY = 1, the listed strips otherwise.
+template <int STY>
+__device__ __forceinline__ bool marchItem(const Params& P, int item, int& sx, int& by0) {
+    if (STY == 1) {
+        const int st = P.strips[item >> 1];
+        sx = st % P.nSX;
+        by0 = STRIP_TY * (st / P.nSX) + (item & 1);
+        return true;
+    }
+    const int st = P.strips[item];
+    sx = st % P.nSX;
+    const int sy = st / P.nSX;
+    if (STY == 2) {
+        by0 = STRIP_TY * sy;
+        return true;
+    }
+    if (sy & 1) {  // pairs (2p, 2p + 1): the upper one alone only without its partner
+        if (stripHasActive(P, sx, sy - 1)) return false;
+        by0 = STRIP_TY * (sy - 1);
+    } else {
+        by0 = STRIP_TY * sy;
+    }
+    return true;
+}
+
+template <int STY>
+__host__ __device__ constexpr int marchItems(int nStrips) {
+    return STY == 1 ? 2 * nStrips : nStrips;
+}
 
 struct Row {  // one staged row at this lane's column
     float h, u, v, eW, eE, eS, eN;
@@ -94,8 +145,8 @@ __device__ __forceinline__ void issueChunk(MarchSmem& S, int slot, const CUtenso
 // Error path of a timed-out ring wait on chunk c: wait, bounded, for the
 // chunks still in flight (c .. c+MNSLOT-1), so that no TMA write lands after
 // the CTA has left.  `par` holds the slots' parities before chunk c's wait.
-__device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
-    for (int k = c; k < c + MNSLOT && k < MNCHUNK; k++)
+__device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c, int nchunk = MNCHUNK) {
+    for (int k = c; k < c + MNSLOT && k < nchunk; k++)
         mbar_wait_bounded(&S.bar[k % MNSLOT], (par >> (k % MNSLOT)) & 1u);
 }
 
@@ -113,15 +164,20 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c) {
 #ifndef RIFT_MARCH2_MINB
 #define RIFT_MARCH2_MINB 6
 #endif
-template <int STAGE, uint32_t FIX = 0>
+template <int STAGE, uint32_t FIX = 0, int STY = STRIP_TY>
 __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH2_MINB)
     k_march(const __grid_constant__ CUtensorMap tmIn,
                                               const __grid_constant__ CUtensorMap tmE, Params P) {
     __shared__ MarchSmem S;
     __shared__ bool last;
     if (P.st->stop || !useMarch(P)) return;
+    // rain maps read ahead with U^n when the instantiation has gridded rain
+    constexpr bool RAINPRE = STAGE == 2 && (FIX & F_RAIN_G) != 0;
+    constexpr int HR = STY * TH;                      // output rows per item
+    constexpr int NCHUNK = (HR + 4 + MRC - 1) / MRC;  // staged chunks (2-row halo each side)
+    constexpr int NT_ = STRIP_TX * STY;                // tiles per item
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nItems = P.st->nStrips;
+    const int nItems = marchItems<STY>(P.st->nStrips);
     const StageConsts C = blockConsts<STAGE>(P);
     float tmxAll = 0.f, tmyAll = 0.f;
     if (tid == 0) {
@@ -144,17 +200,17 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
     ledZero(L);
 
     for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
-        const int strip = P.strips[item];
-        const int sx = strip % P.nSX, sy = strip / P.nSX;
-        const int X0 = MCOLS * sx + 2, Y0 = MHR * sy + 2;
-        // strip-uniform: does the strip reach the first or last interior row/column?
+        int sx, by0;
+        if (!marchItem<STY>(P, item, sx, by0)) continue;  // item-uniform
+        const int X0 = MCOLS * sx + 2, Y0 = TH * by0 + 2;
+        // item-uniform: does the item reach the first or last interior row/column?
         const bool edgeStrip =
-            X0 == 2 || Y0 == 2 || X0 + MCOLS - 1 >= P.nx - 3 || Y0 + MHR - 1 >= P.ny - 3;
+            X0 == 2 || Y0 == 2 || X0 + MCOLS - 1 >= P.nx - 3 || Y0 + HR - 1 >= P.ny - 3;
         const int xs = MCOLS * sx - 4, ys = Y0 - 2;
         const int i = X0 + lc;
         __syncthreads();  // the previous item no longer reads the ring or the tile tables
-        if (tid < STRIP_TX * STRIP_TY) {
-            const int bx = STRIP_TX * sx + tid % STRIP_TX, by = STRIP_TY * sy + tid / STRIP_TX;
+        if (tid < NT_) {
+            const int bx = STRIP_TX * sx + tid % STRIP_TX, by = by0 + tid / STRIP_TX;
             int a = 0;
             if (bx < P.nBX && by < P.nBY)
                 a = P.prevAct[by * P.nBX + bx] && (bx * TW + 2 <= P.nx - 3) &&
@@ -168,7 +224,7 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             for (int c = 0; c < MNSLOT; c++) issueChunk(S, c, &tmIn, &tmE, xs, ys + c * MRC);
         bool ok = mbar_wait_bounded(&S.bar[0], par & 1u);
         if (!__syncthreads_and(ok)) {
-            marchDrain(S, par, 0);
+            marchDrain(S, par, 0, NCHUNK);
             if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
             return;
         }
@@ -192,30 +248,34 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             yPu = y2.uP;
             yPv = y2.vP;
         }
-        // centre values of the first output row (stage 2: U^n), loaded ahead of use
+        // centre values of the first output row (stage 2: U^n, and the rain
+        // maps when the instantiation reads them ahead), loaded ahead of use
         const bool colIn = owned && i <= P.nx - 3;
-        float pre[3] = {0.f, 0.f, 0.f}, nextPre[3] = {0.f, 0.f, 0.f};
+        float pre[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nextPre[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) nextPre[q] = 0.f;
         if (STAGE == 2 && colIn && Y0 <= P.ny - 3) {
             pre[0] = P.A[cidx(P, 0, Y0, i)];
             pre[1] = P.A[cidx(P, 1, Y0, i)];
             pre[2] = P.A[cidx(P, 2, Y0, i)];
+            if (RAINPRE) loadRainMaps(P, cidx(P, 0, Y0, i), pre + 6);
         }
         float accMx = 0.f, accMy = 0.f;
         bool accWet = false;
         // two rows per iteration: the compiler interleaves their independent
         // work (7% faster than one row at the same 80 registers)
 #pragma unroll 2
-        for (int R = 2; R <= MHR + 1; R++) {
+        for (int R = 2; R <= HR + 1; R++) {
             const int lead = R + 2;
             if (lead % MRC == 0) {  // entering chunk c: refill the slot chunk c-1 used
                 const int c = lead / MRC;
                 __syncthreads();
-                if (tid == 0 && c - 1 + MNSLOT < MNCHUNK)
+                if (tid == 0 && c - 1 + MNSLOT < NCHUNK)
                     issueChunk(S, (c - 1) % MNSLOT, &tmIn, &tmE, xs, ys + (c - 1 + MNSLOT) * MRC);
                 const int sl = c % MNSLOT;
                 bool ok2 = mbar_wait_bounded(&S.bar[sl], (par >> sl) & 1u);
                 if (!__syncthreads_and(ok2)) {
-                    marchDrain(S, par, c);
+                    marchDrain(S, par, c, NCHUNK);
                     if (tid == 0) atomicOr(&P.st->error, ERR_TMA_TIMEOUT);
                     return;
                 }
@@ -229,7 +289,10 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
                 nextPre[0] = P.A[cn];
                 nextPre[1] = P.A[cn + P.planeSize];
                 nextPre[2] = P.A[cn + 2 * (size_t)P.planeSize];
-                prefetchMaps(P, cellFlags<FIX>(C.fl), cn);
+                if (RAINPRE)
+                    loadRainMaps(P, cn, nextPre + 6);
+                else
+                    prefetchMaps(P, cellFlags<FIX>(C.fl), cn);
             }
             const int tslot = ((R - 2) / TH) * STRIP_TX + tcol;
             const bool cellOn = colIn && S.tact[tslot] && j <= P.ny - 3;
@@ -270,8 +333,8 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
                         P.D[c + P.planeSize] = dhu + bedSourceX(P, cur.h, cur.eW, cur.eE);
                         P.D[c + 2 * (size_t)P.planeSize] = dhv + bedSourceY(P, cur.h, cur.eS, cur.eN);
                     } else {
-                        const int tile = (STRIP_TY * sy + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
-                        accWet |= cellUpdate<STAGE, false, true, FIX>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
+                        const int tile = (by0 + (R - 2) / TH) * P.nBX + STRIP_TX * sx + tcol;
+                        accWet |= cellUpdate<STAGE, false, true, FIX, RAINPRE>(P, C, tile, j, i, dh, dhu, dhv, cur.h, cur.u,
                                                     cur.v, cur.eW, cur.eE, cur.eS, cur.eN, pre,
                                                     edgeStrip, led ? &L : nullptr);
                     }
@@ -300,12 +363,14 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             pre[0] = nextPre[0];
             pre[1] = nextPre[1];
             pre[2] = nextPre[2];
+            pre[6] = nextPre[6];
+            pre[7] = nextPre[7];
             cur = nxt;
             nxt = ld;
         }
         __syncthreads();
-        if (tid < STRIP_TX * STRIP_TY && S.tact[tid]) {
-            const int bx = STRIP_TX * sx + tid % STRIP_TX, by = STRIP_TY * sy + tid / STRIP_TX;
+        if (tid < NT_ && S.tact[tid]) {
+            const int bx = STRIP_TX * sx + tid % STRIP_TX, by = by0 + tid / STRIP_TX;
             const int b = by * P.nBX + bx;
             if (STAGE == 2) P.wet[b] = (uint8_t)((!(C.fl & F_TILE_ACC)) || S.twet[tid]);
             P.mx[b] = __uint_as_float(S.tmx[tid]);
@@ -314,7 +379,7 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
         if (STAGE == 1) {  // thread 0 keeps this CTA's maximum of new tile speeds
             __syncthreads();
             if (tid == 0)
-                for (int k = 0; k < STRIP_TX * STRIP_TY; k++)
+                for (int k = 0; k < NT_; k++)
                     if (S.tact[k]) {
                         tmxAll = fmaxf(tmxAll, __uint_as_float(S.tmx[k]));
                         tmyAll = fmaxf(tmyAll, __uint_as_float(S.tmy[k]));
@@ -379,8 +444,9 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
             const int tile = by * P.nBX + STRIP_TX * sx + slot;
             constexpr int G = 2;
             bool wetAny = false;
+            constexpr bool RAINPRE = (FIX & F_RAIN_G) != 0;
             for (int r0 = 0; r0 < TH; r0 += G) {
-                float v[G][7];
+                float v[G][9];
                 bool on[G];
 #pragma unroll
                 for (int q = 0; q < G; q++) {
@@ -395,14 +461,17 @@ __global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
                         v[q][4] = P.A[c + pl];
                         v[q][5] = P.A[c + 2 * pl];
                         v[q][6] = P.nman[c];
-                        prefetchMaps(P, cellFlags<FIX>(C.fl), c);
+                        if (RAINPRE)
+                            loadRainMaps(P, c, &v[q][7]);
+                        else
+                            prefetchMaps(P, cellFlags<FIX>(C.fl), c);
                     }
                 }
 #pragma unroll
                 for (int q = 0; q < G; q++) {
                     if (!on[q]) continue;
-                    const float pre[1] = {v[q][6]};
-                    wetAny |= cellUpdate<1, false, false, FIX>(P, C, tile, Y0 + r0 + q, i, v[q][0],
+                    const float pre[8] = {v[q][6], 0.f, 0.f, 0.f, 0.f, 0.f, v[q][7], v[q][8]};
+                    wetAny |= cellUpdate<1, false, false, FIX, RAINPRE>(P, C, tile, Y0 + r0 + q, i, v[q][0],
                                                           v[q][1], v[q][2], v[q][3], v[q][4],
                                                           v[q][5], 0.f, 0.f, 0.f, 0.f, pre,
                                                           edgeStrip, led ? &L : nullptr);

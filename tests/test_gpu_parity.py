@@ -26,14 +26,15 @@ def _close(a, b, what):
     assert d.max() <= MAX_TOL, f"{what}: max {d.max()}"
 
 
-# (march threshold in strips, persistent-loop threshold in tiles)
-SCHEDULES = {"auto": (-1, -1), "tiles": (1 << 30, 0), "march": (0, 0),
-             "persist": (1 << 30, 1 << 30)}
+# (march threshold in strips, persistent-loop threshold in tiles, march
+# work-item height in tile rows)
+SCHEDULES = {"auto": (-1, -1, 2), "tiles": (1 << 30, 0, 2), "march": (0, 0, 2),
+             "march1": (0, 0, 1), "march4": (0, 0, 4), "persist": (1 << 30, 1 << 30, 2)}
 
 
 def _scheduled(sim, schedule):
-    march, persist = SCHEDULES[schedule]
-    return sim.set_schedule(march).set_persistent(persist)
+    march, persist, rows = SCHEDULES[schedule]
+    return sim.set_schedule(march).set_persistent(persist).set_march_rows(rows)
 
 
 def _run_against_golden(engine_api, name, schedule="auto"):
@@ -94,11 +95,12 @@ def name_run(request):
     return request.param
 
 
-@pytest.mark.parametrize("schedule", ["tiles", "march", "persist"])
+@pytest.mark.parametrize("schedule", ["tiles", "march", "march1", "march4", "persist"])
 @pytest.mark.parametrize("name", FX.CASES)
 def test_engine_matches_reference_kernels(engine_api, name, schedule):
-    """Every kernel schedule (per-tile kernels, column march, persistent
-    cooperative loop) against the reference kernels."""
+    """Every kernel schedule (per-tile kernels, column march on work items of
+    2, 1 and 4 tile rows, persistent cooperative loop) against the reference
+    kernels."""
     eng = _run_against_golden(engine_api, name, schedule)
     persist_steps, graph_steps = eng.path_stats()
     if schedule == "persist":
@@ -186,16 +188,19 @@ def test_one_step_from_identical_snapshot(engine_api, oracle_api, name, schedule
 
 
 def test_autotune_restores_state(engine_api):
-    """The autotuner times the three schedules from the current state, puts
-    the state back exactly and keeps the fastest; the run then goes on as
-    if nothing had happened."""
+    """The autotuner times the schedules and march item heights from the
+    current state, puts the state back exactly and keeps the fastest; the run
+    then goes on as if nothing had happened."""
     fx, case = FX.load("rain")
     a = FX.start(capi.Sim(case, api=engine_api), fx)
     b = FX.start(capi.Sim(case, api=engine_api), fx)
     a.run(6)
     b.run(6)
     choice, ms = b.autotune(8)
-    assert choice in (0, 1, 2)
+    assert choice in range(len(capi.Sim.AUTOTUNE_CANDIDATES))
+    assert np.isfinite(ms).sum() >= 4
+    if choice >= 2:
+        assert b.march_rows() == (2, 1, 4)[choice - 2]
     assert np.isfinite(ms[choice]) and ms[choice] == np.nanmin(ms)
     assert np.array_equal(a.field("W"), b.field("W"))
     assert a.time() == b.time()
@@ -206,3 +211,25 @@ def test_autotune_restores_state(engine_api):
     (wa, aa), (wb, ab) = a.tiles(), b.tiles()
     assert np.array_equal(wa, wb) and np.array_equal(aa, ab)
     _close(b.field("W"), a.field("W"), "after autotune")
+
+
+@pytest.mark.parametrize("rows", [1, 4])
+def test_march_item_heights_match_on_a_dense_grid(engine_api, rows):
+    """On a 1024^2 grid under uniform rain (every tile active, 74 x 37 strips
+    of 7 x 2 tiles), march items of 1 and 4 tile rows give the results of the
+    default 2-row items: the same tile sets and times, and the same state to
+    the bit (the per-cell arithmetic does not depend on the item shape).  The
+    golden runs above cover partial activity on every height."""
+    from rift_gb300 import synth
+    case = synth.config1(N=1024)
+    runs = []
+    for r in (2, rows):
+        sim = capi.Sim(case, api=engine_api).set_schedule(0).set_persistent(0).set_march_rows(r).setup()
+        sim.run(40)
+        runs.append((sim.tiles(), sim.time(), sim.field("W"), sim.field("HU")))
+        sim.close()
+    (w0, a0), t0, W0, U0 = runs[0]
+    (w1, a1), t1, W1, U1 = runs[1]
+    assert np.array_equal(w0, w1) and np.array_equal(a0, a1)
+    assert t0 == t1
+    assert np.array_equal(W0, W1) and np.array_equal(U0, U1)
