@@ -468,6 +468,7 @@ def run_ensemble(args):
         args.sequential = False  # the one-after-another comparison runs members without it
     members = setup()
     ens = capi.Ensemble(members)
+    ens.set_solo_cells(args.solo_cells)
     ens.run(max_steps=args.warmup)  # warm-up steps (counted in t, not timed)
     runner = None
     if model is not None:
@@ -512,6 +513,8 @@ def run_ensemble(args):
             "config": {"workload": "config5", "members": len(cases),
                        "side_cells": [args.side_min, args.side_max], "tf_s": args.tf,
                        "total_cells": int(cells.sum()), "iterations": iters,
+                       "solo_cells": args.solo_cells,
+                       "solo_members": int(np.sum(cells >= args.solo_cells)) if args.solo_cells else 0,
                        "member_steps_min_max": [int(k.min()), int(k.max())]},
             "per_member_s": {"p50": float(np.percentile(per_member, 50)),
                              "p99": float(np.percentile(per_member, 99)),
@@ -708,6 +711,9 @@ def main():
     ap.add_argument("--closure-gain", type=float, default=0.25,
                     help="config 4: strength of the applied corrections (chosen on scenario 100000)")
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")
+    ap.add_argument("--solo-cells", type=int, default=1 << 20,
+                    help="config 5: members of at least this many cells run on their own per-step "
+                         "graphs (the march) after the ensemble kernel; 0 puts all in the kernel")
     ap.add_argument("--side-min", type=int, default=128, help="config 5: smallest side (cells)")
     ap.add_argument("--side-max", type=int, default=512, help="config 5: largest side (cells)")
     ap.add_argument("--tf", type=float, default=3600.0, help="config 5: end time (s)")

@@ -278,10 +278,17 @@ typedef struct rift_ensemble rift_ensemble;
 int rift_ensemble_create(rift_handle* const* members, int32_t n, rift_ensemble** out);
 int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double* t_out,
                       int32_t* steps_out);
+/* Members with at least min_cells interior cells (0, the default: none) are
+ * not stepped by the persistent ensemble kernel: after it, each of them runs
+ * on its own per-step graph, smallest first, with the whole GPU (the column
+ * march on dense grids, about 2.5x the cell rate of the kernel's per-tile
+ * code).  Their results are those of a run of their own, as every member's. */
+int rift_ensemble_set_solo_cells(rift_ensemble* e, int64_t min_cells);
 /* Per member (n entries): the device time, in seconds, from the start of the
  * last rift_ensemble_run's kernel to the end of the member's last step in it
- * (the GPU's global timer, read when the member's final iteration ends); 0
- * for a member that ran no step. */
+ * (the GPU's global timer, read when the member's final iteration ends; for
+ * members run on their own, CUDA events, counted after the kernel and the
+ * members run before them); 0 for a member that ran no step. */
 int rift_ensemble_member_times(rift_ensemble* e, double* seconds);
 const char* rift_ensemble_last_error(rift_ensemble* e);
 void rift_ensemble_destroy(rift_ensemble* e);

@@ -103,6 +103,9 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
         ns["ensemble_destroy"] = _sig(lib, p + "ensemble_destroy", None, [_P])
         if hasattr(lib, p + "ensemble_member_times"):
             ns["ensemble_member_times"] = _sig(lib, p + "ensemble_member_times", C.c_int, [_P, _D])
+        if hasattr(lib, p + "ensemble_set_solo_cells"):
+            ns["ensemble_set_solo_cells"] = _sig(lib, p + "ensemble_set_solo_cells", C.c_int,
+                                                 [_P, C.c_int64])
     if hasattr(lib, p + "autotune"):
         ns["autotune"] = _sig(lib, p + "autotune", C.c_int, [_P, C.c_int32, _I, _D])
     if hasattr(lib, p + "set_persistent"):
@@ -433,6 +436,14 @@ class Ensemble:
             raise RiftError(f"ensemble_run failed: {ERRORS.get(rc, rc)} "
                             f"{self.f['ensemble_last_error'](self.h).decode()}")
         return t, k
+
+    def set_solo_cells(self, min_cells):
+        """Members with at least min_cells interior cells run on their own
+        per-step graphs after the ensemble kernel (0: none)."""
+        rc = self.f["ensemble_set_solo_cells"](self.h, int(min_cells))
+        if rc != RIFT_OK:
+            raise RiftError(f"ensemble_set_solo_cells failed: {ERRORS.get(rc, rc)}")
+        return self
 
     def member_times(self):
         """Device seconds from the last run's start to each member's end."""

@@ -1734,6 +1734,7 @@ int rift_autotune(rift_handle* h, int32_t probe_steps, int32_t* choice, double* 
 struct rift_ensemble {
     std::vector<rift_handle*> m;
     std::vector<double> memberSec;  // last run: device time from its start to each member's end
+    int64_t soloCells = 0;          // members with at least this many interior cells run on their own
     cudaStream_t stream = nullptr;
     Params* dP = nullptr;
     CUtensorMap* dMaps = nullptr;
@@ -1747,6 +1748,11 @@ namespace {
 int efail(rift_ensemble* e, int code, const std::string& msg) {
     if (e) e->err = msg;
     return code;
+}
+
+// A member large enough to run on its own per-step graph (rift_ensemble_set_solo_cells).
+bool isSolo(const rift_ensemble* e, const rift_handle* h) {
+    return e->soloCells > 0 && (int64_t)(h->nx - 4) * (h->ny - 4) >= e->soloCells;
 }
 #define ENS_TRY(e, call)                                                                        \
     do {                                                                                        \
@@ -1805,7 +1811,7 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
         maps[3 * k] = h->tmA;
         maps[3 * k + 1] = h->tmB;
         maps[3 * k + 2] = h->tmE;
-        live[k] = (h->hst->t < t_stop && max_steps > 0) ? 1 : 0;
+        live[k] = (h->hst->t < t_stop && max_steps > 0 && !isSolo(e, h)) ? 1 : 0;
         nAlive += live[k];
     }
     ENS_TRY(e, cudaMemcpyAsync(e->dP, P.data(), sizeof(Params) * n, cudaMemcpyHostToDevice, e->stream));
@@ -1818,8 +1824,14 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
                                e->stream));
     EnsArgs A{e->dP, e->dMaps, e->dE, n, max_steps};
     void* args[] = {(void*)&A};
-    ENS_TRY(e, cudaLaunchCooperativeKernel((const void*)k_ensemble, dim3(e->grid), dim3(NT), args, 0,
-                                           e->stream));
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    ENS_TRY(e, cudaEventCreate(&ev0));
+    ENS_TRY(e, cudaEventCreate(&ev1));
+    ENS_TRY(e, cudaEventRecord(ev0, e->stream));
+    if (nAlive > 0)
+        ENS_TRY(e, cudaLaunchCooperativeKernel((const void*)k_ensemble, dim3(e->grid), dim3(NT), args, 0,
+                                               e->stream));
+    ENS_TRY(e, cudaEventRecord(ev1, e->stream));
     ENS_TRY(e, cudaStreamSynchronize(e->stream));
     {  // each member's completion on the device clock
         std::vector<unsigned long long> done(n, 0ull);
@@ -1831,6 +1843,40 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
         for (int k = 0; k < n; k++)
             if (live[k] && done[k] >= t0) e->memberSec[k] = 1e-9 * (double)(done[k] - t0);
     }
+    // The large members, one after another on their own per-step graphs (the
+    // column march on dense grids), smallest first; each one's completion is
+    // the CUDA-event time since the ensemble kernel's start.
+    {
+        float kernelMs = 0.f;
+        ENS_TRY(e, cudaEventElapsedTime(&kernelMs, ev0, ev1));
+        double offset = 1e-3 * kernelMs;
+        std::vector<int> solo;
+        for (int k = 0; k < n; k++)
+            if (isSolo(e, e->m[k]) && e->m[k]->hst->t < t_stop && max_steps > 0) solo.push_back(k);
+        std::sort(solo.begin(), solo.end(), [&](int a, int b) {
+            return (int64_t)e->m[a]->nx * e->m[a]->ny < (int64_t)e->m[b]->nx * e->m[b]->ny;
+        });
+        for (int k : solo) {
+            rift_handle* h = e->m[k];
+            double tk = 0.0, dtk = 0.0;
+            int32_t dk = 0;
+            ENS_TRY(e, cudaEventRecord(ev0, h->stream));
+            int r = rift_run(h, max_steps, t_stop, &tk, &dtk, &dk);
+            if (r) {
+                cudaEventDestroy(ev0);
+                cudaEventDestroy(ev1);
+                return efail(e, r, "member " + std::to_string(k) + ": " + h->err);
+            }
+            ENS_TRY(e, cudaEventRecord(ev1, h->stream));
+            ENS_TRY(e, cudaEventSynchronize(ev1));
+            float ms = 0.f;
+            ENS_TRY(e, cudaEventElapsedTime(&ms, ev0, ev1));
+            offset += 1e-3 * ms;
+            e->memberSec[k] = dk > 0 ? offset : 0.0;
+        }
+    }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
     int rc = RIFT_OK;
     for (int k = 0; k < n; k++) {
         rift_handle* h = e->m[k];
@@ -1844,6 +1890,12 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
         e->steps += h->hst->steps_done;
     }
     return rc;
+}
+
+int rift_ensemble_set_solo_cells(rift_ensemble* e, int64_t min_cells) {
+    if (!e || min_cells < 0) return RIFT_ERR_ARG;
+    e->soloCells = min_cells;
+    return RIFT_OK;
 }
 
 int rift_ensemble_member_times(rift_ensemble* e, double* seconds) {

@@ -136,3 +136,28 @@ def test_ensemble_member_times_follow_completion(engine_api):
     assert k[order[0]] < k[order[-1]], k  # the wet cases take smaller steps than the dry front
     assert sec[order[0]] <= sec[order[-1]]
     ens.close()
+
+
+def test_ensemble_with_solo_members_matches_members_alone(engine_api):
+    """Members above the solo threshold run on their own per-step graphs after
+    the ensemble kernel; every member still ends where it ends alone, and the
+    completion times are measured for all of them."""
+    names = list(FX.CASES)
+    steps = 25
+    solo = _members(engine_api, names)
+    for s in solo:
+        s.run(steps)
+    members = _members(engine_api, names)
+    cells = np.array([(m.nx - 4) * (m.ny - 4) for m in members])
+    thr = int(np.median(cells))
+    ens = capi.Ensemble(members).set_solo_cells(thr)
+    t, k = ens.run(max_steps=steps)
+    assert (k == steps).all()
+    sec = ens.member_times()
+    assert (sec > 0).all()
+    big = cells >= thr
+    assert big.any() and (~big).any()
+    assert sec[big].min() >= sec[~big].max()  # the solo members run after the kernel
+    for name, a, b in zip(names, members, solo):
+        _same(_state(a), _state(b), name)
+    ens.close()
