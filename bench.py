@@ -648,10 +648,14 @@ def run_closure(args):
             sim = capi.Sim(cc).setup()
             bc_of[id(sim)] = sim.field("BC")
             if mode == "closure":
-                cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain)
+                cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain,
+                                        fine=fc if args.fine_fallback else None)
                 w, arr = _timed_chunks(cr.run, args.tf, 120.0, lambda: interior_depth(sim))
                 res["closure_blocks"], res["closure_fallback_blocks"] = cr.block_counts()
                 res["closure_applies"] = cr.applies
+                if cr.fallback is not None:
+                    res["fine_resolved_blocks"] = cr.fallback.refined
+                    cr.fallback.close()
             else:
                 w, arr = _timed_chunks(lambda t: sim.run(2 ** 31 - 1, t)[0], args.tf, 120.0,
                                        lambda: interior_depth(sim))
@@ -680,6 +684,8 @@ def run_closure(args):
                        "train_grid": f"{args.closure_train_N}^2 at 2 m", "train_patches": n_patches,
                        "train_steps": args.train_steps, "batch": 256, "closure_every_steps": args.closure_every,
                        "closure_gain": args.closure_gain,
+                       "fallback": "fine-grid re-solve of the block" if args.fine_fallback
+                       else "plain coarse solve of the block",
                        "eval_scenarios": args.eval_seeds},
             "peak_depth_rmse_m": {"closure": float(np.mean([r["closure"]["peak_depth_rmse_m"] for r in evals])),
                                   "plain_coarse": float(np.mean([r["plain"]["peak_depth_rmse_m"] for r in evals]))},
@@ -708,6 +714,9 @@ def main():
                     help="config 5: members coarsened 2x with the learned closure")
     ap.add_argument("--closure-profile", action="store_true",
                     help="config 4: time only the closure step on a wet coarse state")
+    ap.add_argument("--no-fine-fallback", dest="fine_fallback", action="store_false",
+                    help="config 4: blocks that fall back keep the plain coarse solve instead of "
+                         "a fine-grid re-solve")
     ap.add_argument("--closure-gain", type=float, default=0.25,
                     help="config 4: strength of the applied corrections (chosen on scenario 100000)")
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")

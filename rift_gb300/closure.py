@@ -453,14 +453,172 @@ def train(ds: Dataset, steps=1500, batch=256, lr=2e-3, seed=0, log=None, log_eve
 
 
 # -------------------------------------------------------- coarse closure run
+BLOCK = 16  # coarse cells per side of a closure block (k_closure's output block)
+
+
+def patch_range(j0, j1, halo, n):
+    """The coarse interior rows (or columns) [a, b) of a fine re-solve patch:
+    the block's [j0, j1) widened by `halo` cells, clipped to the interior
+    [2, n - 2) of an h-grid of n cells."""
+    return max(2, j0 - halo), min(n - 2, j1 + halo)
+
+
+def fine_patch_case(fine: synth.Case, Ja, Jb, Ia, Ib) -> synth.Case:
+    """The fine case under coarse interior cells [Ja, Jb) x [Ia, Ib) of its 2x
+    coarsening: the fine corner DEM of those cells, their n (and K), the same
+    uniform series, and the point sources that fall inside."""
+    fa, fb = 2 * (Ja - 2), 2 * (Jb - 2)  # fine interior rows (0-based) of the patch
+    ga, gb = 2 * (Ia - 2), 2 * (Ib - 2)
+    B = fine.B[fa:fb + 1, ga:gb + 1].copy()
+
+    def cells(a):
+        if a is None:
+            return None
+        out = np.zeros((fb - fa + 4, gb - ga + 4))
+        out[2:-2, 2:-2] = a[2 + fa:2 + fb, 2 + ga:2 + gb]
+        return out
+
+    src = None
+    flags = fine.flags & ~(synth.SAVE_MAX | synth.SAVE_ARRIVAL | synth.CHECK_VOLUME)
+    if fine.src_idx is not None:
+        j, i = np.divmod(np.asarray(fine.src_idx, dtype=np.int64), fine.h_nx)
+        inside = (j >= 2 + fa) & (j < 2 + fb) & (i >= 2 + ga) & (i < 2 + gb)
+        if inside.any():
+            nx_p = gb - ga + 4
+            src = ((j[inside] - fa) * nx_p + (i[inside] - ga)).astype(np.int32)
+        else:
+            flags &= ~synth.POINT_SOURCE
+    return dataclasses.replace(fine, name=fine.name + f"_patch{Ja}_{Ia}", B=B, n=cells(fine.n),
+                               K=cells(fine.K), h0=None, src_idx=src, rain_maps=None,
+                               flags=flags & ~synth.H_INIT)
+
+
+class FineFallback:
+    """The plain fine-grid solve as the per-block fallback of the closure.
+
+    A block whose residual indicator exceeds tau (k_closure's fallback test)
+    is re-solved on the fine grid over the closure interval [t0, t1]: a patch
+    of the fine case -- the block and `halo` coarse cells around it, at the
+    fine resolution -- starts from the coarse state at t0 (each coarse cell's
+    depth and momenta on its four fine cells; the bed is the fine bed), runs
+    the plain solver to t1, and its 2x2 means replace the block's coarse
+    cells at t1.  The block keeps the volume the coarse solve gave it (the
+    fine depths are scaled to it over the wet cells), so the run stays
+    conservative, and wet and dry cells keep their status, which the engine's
+    tile activity requires; cells next to the domain edge keep the coarse
+    values.  The halo absorbs the patch's own open edges over the interval."""
+
+    def __init__(self, coarse_sim: capi.Sim, fine: synth.Case, halo=4, max_blocks=256, cache=64):
+        self.sim, self.fine, self.halo = coarse_sim, fine, halo
+        self.max_blocks, self.cache = max_blocks, cache
+        self.patches = {}   # block -> (Sim, BC of the patch)
+        self.refined = 0    # blocks re-solved so far
+        self.skipped = 0    # fallen-back blocks beyond max_blocks in one interval
+
+    def _patch(self, key, Ja, Jb, Ia, Ib):
+        if key in self.patches:
+            self.patches[key] = self.patches.pop(key)  # most recent last
+            return self.patches[key]
+        if len(self.patches) >= self.cache:
+            old = next(iter(self.patches))
+            self.patches.pop(old)[0].close()
+        case = fine_patch_case(self.fine, Ja, Jb, Ia, Ib)
+        sim = capi.Sim(case).setup()
+        entry = (sim, sim.field("BC"))
+        self.patches[key] = entry
+        return entry
+
+    def refine(self, fell, u0, t0, t1, dt0):
+        """Re-solve the fallen-back blocks (fell: per-block flags, row-major
+        over ceil((nx-4)/16) blocks) from the coarse state u0 = (h, hu, hv)
+        at t0 (host arrays of the h-grid) to t1, writing the coarse state at t1
+        through the handle's device view."""
+        torch = _torch()
+        v = self.sim.device_view()
+        ny, nx = v.h_ny, v.h_nx
+        tx = -(-(nx - 4) // BLOCK)
+        blocks = np.nonzero(fell)[0]
+        if len(blocks) > self.max_blocks:
+            self.skipped += len(blocks) - self.max_blocks
+            blocks = blocks[:self.max_blocks]
+        if len(blocks) == 0:
+            return 0
+        planes = [_device_plane(ptr, v) for ptr in (v.h, v.hu, v.hv)]
+        torch.cuda.synchronize()
+        cur = [p[:ny, :nx].cpu().numpy() for p in planes]
+        eps = 1.19209e-07
+        for b in blocks:
+            by, bx = divmod(int(b), tx)
+            j0, i0 = 2 + BLOCK * by, 2 + BLOCK * bx
+            j1, i1 = min(j0 + BLOCK, ny - 2), min(i0 + BLOCK, nx - 2)
+            Ja, Jb = patch_range(j0, j1, self.halo, ny)
+            Ia, Ib = patch_range(i0, i1, self.halo, nx)
+            psim, pbc = self._patch((j0, i0), Ja, Jb, Ia, Ib)
+            # the coarse state at t0 on the fine cells of the patch
+            hf = np.zeros(pbc.shape)
+            huf, hvf = np.zeros(pbc.shape), np.zeros(pbc.shape)
+            for a, src in ((hf, u0[0]), (huf, u0[1]), (hvf, u0[2])):
+                blk = src[Ja:Jb, Ia:Ib].astype(np.float64)
+                a[2:-2, 2:-2] = np.repeat(np.repeat(blk, 2, axis=0), 2, axis=1)
+            hf = np.maximum(hf, 0.0)
+            n_bx, n_by = psim.nBX, psim.nBY
+            psim.set_state(t0, dt0, pbc + hf, huf, hvf, wet=np.ones(n_bx * n_by, np.uint8),
+                           active=np.arange(n_bx * n_by, dtype=np.int32))
+            psim.run(2 ** 31 - 1, t1)
+            hp = (psim.field("W") - pbc)[2:-2, 2:-2]
+            up, vp = psim.field("HU")[2:-2, 2:-2], psim.field("HV")[2:-2, 2:-2]
+            # the block's cells in the patch, 2x2 means; the edge cells of the
+            # domain keep the coarse values
+            r0, c0 = 2 * (j0 - Ja), 2 * (i0 - Ia)
+            sl = (slice(r0, r0 + 2 * (j1 - j0)), slice(c0, c0 + 2 * (i1 - i0)))
+            Hf, Uf, Vf = restrict(hp[sl]), restrict(up[sl]), restrict(vp[sl])
+            jj, ii = np.mgrid[j0:j1, i0:i1]
+            keep = (jj >= 3) & (jj <= ny - 4) & (ii >= 3) & (ii <= nx - 4)
+            Hc = cur[0][j0:j1, i0:i1].astype(np.float64)
+            wet = (Hc > eps) & keep
+            Hn = np.where(wet, np.maximum(Hf, 2 * eps), Hc)
+            vol_c, vol_f = Hc[wet].sum(), Hn[wet].sum()
+            if vol_f > 0:
+                Hn[wet] *= vol_c / vol_f
+                Hn[wet] = np.maximum(Hn[wet], 2 * eps)
+            cur[0][j0:j1, i0:i1] = np.where(wet, Hn, Hc).astype(np.float32)
+            cur[1][j0:j1, i0:i1] = np.where(wet, Uf, cur[1][j0:j1, i0:i1]).astype(np.float32)
+            cur[2][j0:j1, i0:i1] = np.where(wet, Vf, cur[2][j0:j1, i0:i1]).astype(np.float32)
+            self.refined += 1
+        for p, c in zip(planes, cur):
+            p[:ny, :nx].copy_(torch.as_tensor(c, device="cuda"))
+        torch.cuda.synchronize()
+        return len(blocks)
+
+    def close(self):
+        for sim, _ in self.patches.values():
+            sim.close()
+        self.patches.clear()
+
+
+def _device_plane(ptr, v):
+    """A (rows, pitch) FP32 CUDA tensor over a device-view plane (no copy)."""
+    torch = _torch()
+
+    class _Arr:
+        __cuda_array_interface__ = {"shape": (v.rows, v.pitch), "typestr": "<f4",
+                                    "data": (int(ptr), False), "version": 3, "strides": None}
+    return torch.as_tensor(_Arr(), device="cuda")
+
+
 class ClosureRun:
     """A coarse handle stepped by the engine, with the closure applied every
-    `every` steps over the time those steps covered."""
+    `every` steps over the time those steps covered.  With `fine` (the fine
+    case the coarse one was coarsened from), blocks that fall back are
+    re-solved on the fine grid (FineFallback) instead of keeping the plain
+    coarse solve."""
 
-    def __init__(self, sim: capi.Sim, model: Model, every=4, hmin=0.01, lim=0.2, tau=0.5, gain=1.0):
+    def __init__(self, sim: capi.Sim, model: Model, every=4, hmin=0.01, lim=0.2, tau=0.5, gain=1.0,
+                 fine: synth.Case | None = None, halo=4):
         torch = _torch()
         self.sim, self.model = sim, model
         self.every, self.hmin, self.lim, self.tau = every, hmin, lim, tau
+        self.fallback = FineFallback(sim, fine, halo=halo) if fine is not None else None
         v = sim.device_view()
         self.view = v
         rows, pitch = v.rows, v.pitch
@@ -508,14 +666,28 @@ class ClosureRun:
         self.applies += 1
 
     def run(self, tf):
-        t, _ = self.sim.time()
+        t, dt = self.sim.time()
         while t < tf:
-            t_new, _, k = self.sim.run(self.every, tf)
+            u0 = self._state_copy() if self.fallback is not None else None
+            t_new, dt_new, k = self.sim.run(self.every, tf)
             if k == 0:
                 break
             self.apply(t_new - t, t_new)
-            t = t_new
+            if self.fallback is not None:
+                _torch().cuda.synchronize()  # the closure kernels ran on the handle's stream
+                fell = self.fell.cpu().numpy()
+                if fell.any():
+                    v = self.view
+                    u = [p[:v.h_ny, :v.h_nx].cpu().numpy() for p in u0]
+                    self.fallback.refine(fell, u, t, t_new, 0.5 * dt)
+            t, dt = t_new, dt_new
         return t
+
+    def _state_copy(self):
+        """Device copy of the handle's h, hu, hv (the state at an interval's start)."""
+        v = self.view
+        _torch().cuda.synchronize()  # the handle's stream wrote the state
+        return [_device_plane(p, v).clone() for p in (v.h, v.hu, v.hv)]
 
     def block_counts(self):
         """(blocks evaluated, blocks that fell back) over every apply."""

@@ -1,6 +1,8 @@
 """Host-side logic of the learned flux closure (no GPU): the parameter
 layout against PyTorch's convolution weights, the coarse-grid geometry, the
 face masks and the patch cutter."""
+import dataclasses
+
 import numpy as np
 
 from rift_gb300 import closure, synth
@@ -106,3 +108,28 @@ def test_even_side_and_coarse_point_sources():
     J, I = divmod(int(k.src_idx[0]), k.h_nx)
     assert (J, I) == (2 + (je - 2) // 2, 2 + (ie - 2) // 2)
     assert 2 <= J <= k.h_ny - 3 and 2 <= I <= k.h_nx - 3
+
+
+def test_fine_patch_geometry():
+    """A fine re-solve patch covers the block and its halo of coarse cells at
+    the fine resolution: its corner DEM is the fine DEM under those cells,
+    its n the fine cells' n, and point sources inside it keep their cells."""
+    from rift_gb300 import closure, synth
+    fine = closure.scenario(0, N=128, cell=2.0)
+    fine = dataclasses.replace(fine, src_idx=np.array([(40 + 2) * fine.h_nx + (50 + 2)], np.int32),
+                               flags=fine.flags | synth.POINT_SOURCE)
+    cc = closure.coarse_case(fine)
+    ny = cc.h_ny
+    j0, i0 = 2 + 16, 2 + 16  # block (1, 1)
+    Ja, Jb = closure.patch_range(j0, j0 + 16, 4, ny)
+    Ia, Ib = closure.patch_range(i0, i0 + 16, 4, ny)
+    assert (Ja, Jb, Ia, Ib) == (14, 38, 14, 38)
+    p = closure.fine_patch_case(fine, Ja, Jb, Ia, Ib)
+    assert p.B.shape == (49, 49) and p.cell == fine.cell
+    np.testing.assert_array_equal(p.B, fine.B[24:73, 24:73])
+    np.testing.assert_array_equal(p.n[2:-2, 2:-2], fine.n[2 + 24:2 + 72, 2 + 24:2 + 72])
+    # fine cell (40, 50) is patch cell (16, 26), plus the ghost ring
+    assert list(p.src_idx) == [(16 + 2) * p.h_nx + (26 + 2)]
+    # the edge of the domain clips the halo
+    assert closure.patch_range(2, 18, 4, ny) == (2, 22)
+    assert closure.patch_range(ny - 18, ny - 2, 4, ny) == (ny - 22, ny - 2)

@@ -434,3 +434,48 @@ def test_ensemble_with_closure_matches_members_alone(torch):
         d = np.abs(s.field("W") - wa)[2:-2, 2:-2].max()
         assert d < 1e-3, (m, d)
     ens.close()
+
+
+def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
+    """The plain fine-grid solve as the per-block fallback: every block falls
+    back (tau = 0) and is re-solved from the coarse state at the interval's
+    start on a fine patch (block + 4 coarse cells of halo, 2 m cells under 4 m
+    ones).  The re-solve keeps each block's volume, keeps wet and dry cells as
+    they were, changes the wet cells of the blocks, and leaves the edge cells
+    of the domain alone; a run with the fallback on stays finite and its mass
+    ledger closes."""
+    fine = closure.scenario(6, N=256, cell=2.0, tf=900.0)  # rimmed plane with bumps
+    cc = closure.coarse_case(fine)
+    sim = capi.Sim(cc).setup()
+    sim.run(2 ** 31 - 1, 300.0)
+    rng = np.random.default_rng(9)
+    model = closure.Model(_params(rng), SCALE, np.full(4, 2e-3, np.float32))
+    run = closure.ClosureRun(sim, model, every=4, tau=0.0, fine=fine)
+    bc = sim.field("BC")
+    t0, dt0 = sim.time()
+    u0 = [p[:run.view.h_ny, :run.view.h_nx].cpu().numpy() for p in run._state_copy()]
+    t1, _, k = sim.run(4)
+    run.apply(t1 - t0, t1)
+    torch.cuda.synchronize()
+    fell = run.fell.cpu().numpy()
+    assert fell.all()
+    h1 = sim.field("W") - bc
+    v1 = sim.volume()
+    n = run.fallback.refine(fell, u0, t0, t1, 0.5 * dt0)
+    assert n == len(fell) and run.fallback.refined == n
+    h2 = sim.field("W") - bc
+    v2 = sim.volume()
+    assert abs(v2 - v1) <= 1e-6 * v1, (v1, v2)
+    eps = 1.19209e-07
+    inner = (slice(2, -2), slice(2, -2))
+    assert np.array_equal(h1[inner] > eps, h2[inner] > eps)
+    d = np.abs(h2 - h1)
+    assert d[3:-3, 3:-3].max() > 0
+    assert d[2, :].max() == 0 and d[-3, :].max() == 0 and d[:, 2].max() == 0 and d[:, -3].max() == 0
+    assert (h2[inner] >= 0).all() and d.max() < 1.0
+    # a run with the fallback on
+    t = run.run(400.0)
+    assert t >= 400.0 and np.isfinite(sim.field("W")).all()
+    vol, added = sim.mass_ledger()
+    assert abs(vol - added) <= 1e-4 * added
+    run.fallback.close()
