@@ -12,9 +12,12 @@
  *   layer 3 32 -> 4 channels, 1x1;
  *   outputs (east-face mass flux, east-face x-momentum flux, north-face mass
  *           flux, north-face y-momentum flux), per unit face width.
- * The contractions run on BF16 tensor cores with FP32 accumulation; the
- * parameters are one FP32 vector (RIFT_CLOSURE_NPARAM floats) laid out as
- * below, rounded to BF16 when a kernel stages them.
+ * Layers 1 and 2 run on the BF16 tensor cores with FP32 accumulation
+ * (tcgen05.mma with tensor-memory accumulators in the forward and apply
+ * kernels; the training kernel's forward and backward passes on mma.sync);
+ * layer 3 of the forward and apply kernels runs in FP32.  The parameters are
+ * one FP32 vector (RIFT_CLOSURE_NPARAM floats) laid out as below, rounded to
+ * BF16 when a kernel stages them for a tensor-core layer.
  *
  * Every pointer argument is a device pointer unless it says host; `stream`
  * is a cudaStream_t (NULL: the legacy default stream).  Calls are
@@ -118,6 +121,17 @@ int rift_closure_face_flux(const rift_device_view* view, int32_t ratio, float we
 int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src,
                        const float* params, const float* oscale_host, float dtw, float hmin,
                        float lim, float tau, float* corr, uint8_t* block_fell, int32_t* counters);
+
+/* Waits for `stream`, then reports (and clears) the device status of the
+ * tensor-core kernels: RIFT_ERR_CUDA when a completion wait of one of them
+ * gave up (its tile's outputs are then missing), else RIFT_OK. */
+int rift_closure_check(void* stream);
+
+/* One tensor-core MMA (128 x 32 x 16, BF16 in, FP32 out) on fixed values in
+ * the forward pass's operand layout; out (device, 128 x 32 FP32, row-major)
+ * receives the product A B^T with A[r][k] = (r % 7) - 3 + (k % 5) / 4 and
+ * B[n][k] = (n % 5) - 2 + (k % 3) / 2, exact in FP32.  For start-up checks. */
+int rift_closure_selftest(float* out, void* stream);
 
 const char* rift_closure_last_error(void);
 

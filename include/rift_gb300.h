@@ -290,11 +290,19 @@ int rift_ensemble_set_solo_cells(rift_ensemble* e, int64_t min_cells);
  * members run on their own, CUDA events, counted after the kernel and the
  * members run before them); 0 for a member that ran no step. */
 int rift_ensemble_member_times(rift_ensemble* e, double* seconds);
+/* Kernels launched so far by rift_ensemble_run: its ensemble kernels plus
+ * the launches of the members run on their own (rift_get_launch_count). */
+int rift_ensemble_launch_count(rift_ensemble* e, int64_t* kernels);
 const char* rift_ensemble_last_error(rift_ensemble* e);
 void rift_ensemble_destroy(rift_ensemble* e);
 
 /* Steps run so far by the persistent launch and by the per-step graph. */
 int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_steps);
+
+/* Kernels launched so far by rift_run / rift_step on this handle: each
+ * persistent launch counts one, each replay of the per-step graph the
+ * kernels in it. */
+int rift_get_launch_count(rift_handle* h, int64_t* kernels);
 
 /* Of the persistent steps, those run from the loop's tile table: one
    scheduled tile per CTA kept from step to step, no grow phase (no gridded

@@ -106,6 +106,9 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
         if hasattr(lib, p + "ensemble_set_solo_cells"):
             ns["ensemble_set_solo_cells"] = _sig(lib, p + "ensemble_set_solo_cells", C.c_int,
                                                  [_P, C.c_int64])
+        if hasattr(lib, p + "ensemble_launch_count"):
+            ns["ensemble_launch_count"] = _sig(lib, p + "ensemble_launch_count", C.c_int,
+                                               [_P, C.POINTER(C.c_int64)])
     if hasattr(lib, p + "autotune"):
         ns["autotune"] = _sig(lib, p + "autotune", C.c_int, [_P, C.c_int32, _I, _D])
     if hasattr(lib, p + "set_persistent"):
@@ -114,6 +117,8 @@ def bind(lib, prefix: str, create_has_mode: bool = False):
                                     [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)])
         ns["get_table_steps"] = _sig(lib, p + "get_table_steps", C.c_int,
                                      [_P, C.POINTER(C.c_int64)])
+    if hasattr(lib, p + "get_launch_count"):
+        ns["get_launch_count"] = _sig(lib, p + "get_launch_count", C.c_int, [_P, C.POINTER(C.c_int64)])
     if hasattr(lib, p + "set_host_access"):
         ns["set_host_access"] = _sig(lib, p + "set_host_access", C.c_int, [_P, C.c_int32])
         ns["get_host_access"] = _sig(lib, p + "get_host_access", C.c_int, [_P, C.POINTER(C.c_int32)])
@@ -296,6 +301,12 @@ class Sim:
         self._check(self.f["autotune"](self.h, probe_steps, C.byref(choice), _dp(ms)), "autotune")
         return choice.value, ms
 
+    def launch_count(self):
+        """Kernels launched by rift_run / rift_step so far (rift_get_launch_count)."""
+        n = C.c_int64()
+        self._check(self.f["get_launch_count"](self.h, C.byref(n)), "get_launch_count")
+        return int(n.value)
+
     def path_stats(self):
         """(steps run by the persistent launch, steps run by the per-step graph)."""
         a, b = C.c_int64(), C.c_int64()
@@ -444,6 +455,14 @@ class Ensemble:
         if rc != RIFT_OK:
             raise RiftError(f"ensemble_set_solo_cells failed: {ERRORS.get(rc, rc)}")
         return self
+
+    def launch_count(self):
+        """Kernels launched by rift_ensemble_run so far (rift_ensemble_launch_count)."""
+        n = C.c_int64()
+        rc = self.f["ensemble_launch_count"](self.h, C.byref(n))
+        if rc != RIFT_OK:
+            raise RiftError(f"ensemble_launch_count failed: {ERRORS.get(rc, rc)}")
+        return int(n.value)
 
     def member_times(self):
         """Device seconds from the last run's start to each member's end."""

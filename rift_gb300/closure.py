@@ -66,6 +66,8 @@ def load():
             "rift_closure_face_flux": [C.POINTER(capi.DeviceView), I, F, P, I, I, I, I],
             "rift_closure_apply": [C.POINTER(capi.DeviceView), C.POINTER(Src), P,
                                    C.POINTER(C.c_float), F, F, F, F, P, P, P],
+            "rift_closure_selftest": [P, P],
+            "rift_closure_check": [P],
         }
         for name, args in sig.items():
             fn = getattr(lib, name)
@@ -163,7 +165,14 @@ def forward(feats, params, scale):
     out = torch.empty((src.samples, 4, src.OH, src.OW), device=feats.device, dtype=torch.float32)
     _check(load().rift_closure_forward(C.byref(src), params.data_ptr(), out.data_ptr(), _stream()),
            "rift_closure_forward")
+    check(_stream())
     return out
+
+
+def check(stream=None):
+    """Wait for `stream` and raise if a tensor-core completion wait of the
+    closure kernels gave up (rift_closure_check)."""
+    _check(load().rift_closure_check(stream), "rift_closure_check")
 
 
 def train_pass(feats, params, scale, target, weight, loss_scale, grad, loss):
@@ -681,6 +690,7 @@ class ClosureRun:
                     u = [p[:v.h_ny, :v.h_nx].cpu().numpy() for p in u0]
                     self.fallback.refine(fell, u, t, t_new, 0.5 * dt)
             t, dt = t_new, dt_new
+        check(self.view.stream)
         return t
 
     def _state_copy(self):
@@ -734,6 +744,7 @@ class EnsembleClosure:
             t_prev = t
             if (t >= t_stop).all():
                 break
+        check(None)
         return t_prev, steps
 
     def launches(self):

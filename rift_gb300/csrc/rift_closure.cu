@@ -350,39 +350,387 @@ __host__ __device__ __forceinline__ int tileCount(const rift_closure_src& src) {
     return src.samples * ((src.OW + OT - 1) / OT) * ((src.OH + OT - 1) / OT);
 }
 
+// ------------------------------------------------- tcgen05 forward (inference)
+// The forward pass of k_forward and k_closure on the 5th-generation tensor
+// cores: layers 1 and 2 are tcgen05.mma (kind::f16, BF16 operands from
+// shared memory, FP32 accumulators in tensor memory), issued by one thread;
+// layer 3 (32 -> 4) runs in FP32 on the CUDA cores in the layer-2 epilogue.
+//
+// Implicit GEMM without an im2col copy.  The input block and the layer-1
+// activations are stored as cells of 8 BF16 channels (16 bytes, one row of
+// an 8 x 16-byte core matrix), cell (y, x) of the 22-wide block at linear
+// index y*22 + x.  An MMA row is a linear cell index m, so the eight rows of
+// a core matrix are eight consecutive cells (16-byte stride) and the row
+// groups are 128 bytes apart; the operand of tap (dy, dx) is the same
+// layout started dy*22 + dx cells later.  Rows whose column m % 22 is past
+// the valid width compute values that no valid output reads.
+//  layer 1: M = 512 rows (4 tiles of 128; the 18 x 18 region is rows
+//           m < 396 with m % 22 < 18), N = 32, K = 15 steps of 16: taps
+//           (dy, dx) and (dy+1, dx) for dy = 0, 2, 4 (dy = 5 carries zero
+//           weights), the two 8-channel K chunks 22 cells apart;
+//  layer 2: M = 384 rows (3 tiles; the 16 x 16 outputs are rows m < 352
+//           with m % 22 < 16), N = 32, K = 9 taps x 2 steps of 16 over the
+//           four 8-channel planes of the layer-1 activations.
+// Tensor memory: 128 columns, one 32-column accumulator per M tile (layer 2
+// reuses the columns of layer 1 once its epilogue has read them).
+constexpr int XBC = 640;             // BF16 input cells staged (reads reach m + 5*22 + 4 < 640)
+constexpr int A1C = 432;             // layer-1 cells kept per plane (layer 2 reads < 384 + 46)
+constexpr int M1TC = 4, M2TC = 3;    // M tiles of 128 rows
+constexpr int KS1 = 15, KS2 = 18;    // K steps of 16
+constexpr int NTAPT = 30;            // layer-1 taps incl. the zero row dy = 5
+constexpr uint32_t TMEM_COLS = 128;
+constexpr uint32_t A1PLANE = A1C * 16;  // bytes per 8-channel plane
+// instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B
+// BF16 (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+struct __align__(128) TcSmem {
+    uint16_t xb[XBC * 8];        // input cells (BF16 x 8), zero past the 22 x 22 block
+    uint16_t a1[4][A1C * 8];     // layer-1 activations, channels 8p..8p+7 in plane p
+    uint16_t w1t[NTAPT * 32 * 8];  // [tap][o][c8], tap 2s + h = (2(s/5) + h, s%5)
+    uint16_t w2t[36 * 32 * 8];   // [tap*4 + c/8][o][c%8]
+    float xs[NRI * CIN];         // scaled FP32 inputs, channels last
+    float w3[COUT][C1];
+    float b1[C1], b2[C1], b3[COUT], sbed[C1];
+    float bref;
+    int red[2];
+    uint64_t bar;
+    uint32_t tmem;
+};
+static_assert(offsetof(TcSmem, a1) % 16 == 0 && offsetof(TcSmem, w1t) % 16 == 0 &&
+                  offsetof(TcSmem, w2t) % 16 == 0 && offsetof(TcSmem, bar) % 8 == 0,
+              "operand alignment");
+
+__device__ int g_tc_error;  // 1: a tensor-core completion wait gave up
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading (K)
+// and stride (M/N) byte offsets, each >> 4; version 1 at bit 46; no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
+           ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, bool acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(IDESC), "r"((uint32_t)acc)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Bounded wait on an mbarrier phase: false after the spin limit.
+__device__ __forceinline__ bool bar_wait(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(saddr(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+// 32 consecutive FP32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float v[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+        "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+          "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+          "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+          "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
+}
+
+// Weights in the operand layouts, biases, the bed-weight sums; the zero pad
+// of the input cells.  Tensor memory (warp 0) and the completion barrier.
+__device__ void tcSetup(TcSmem& S, const float* __restrict__ P) {
+    const int tid = threadIdx.x;
+    constexpr int MAP[CB] = {0, 1, 2, 3, 3, 4, 5, -1};
+    for (int i = tid; i < NTAPT * 32 * 8; i += NT) {
+        const int T = i / 256, o = (i / 8) % 32, c8 = i % 8;
+        const int s = T >> 1, dy = 2 * (s / 5) + (T & 1), dx = s % 5, c = MAP[c8];
+        S.w1t[i] = bf(dy < 5 && c >= 0 ? P[OFF_W1 + o * K1P + (dy * 5 + dx) * CIN + c] : 0.f);
+    }
+    for (int i = tid; i < 36 * 32 * 8; i += NT) {
+        const int blk = i / 256, o = (i / 8) % 32, c8 = i % 8;
+        S.w2t[i] = bf(P[OFF_W2 + o * K2 + (blk >> 2) * 32 + (blk & 3) * 8 + c8]);
+    }
+    for (int i = tid; i < COUT * C1; i += NT) S.w3[i / C1][i % C1] = P[OFF_W3 + i];
+    for (int i = tid; i < (XBC - NRI) * 8; i += NT) S.xb[NRI * 8 + i] = 0;
+    if (tid < C1) {
+        S.b1[tid] = P[OFF_B1 + tid];
+        S.b2[tid] = P[OFF_B2 + tid];
+        float sb = 0.f;
+        for (int tap = 0; tap < 25; tap++) sb += fb(bf(P[OFF_W1 + tid * K1P + tap * CIN + 3]));
+        S.sbed[tid] = sb;
+    }
+    if (tid < COUT) S.b3[tid] = P[OFF_B3 + tid];
+    if (tid == 0) bar_init(&S.bar);
+    if (tid < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         saddr(&S.tmem)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+}
+
+__device__ void tcTeardown(TcSmem& S) {
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (threadIdx.x < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(S.tmem),
+                     "r"(TMEM_COLS)
+                     : "memory");
+}
+
+// The block's input cells (stageInput's values), then the BF16 cells as the
+// layer-1 operand: each writer fences its shared stores for the async proxy.
+__device__ void tcStageInput(TcSmem& S, const rift_closure_src& src, int s, int Y0, int X0) {
+    const size_t sbase = (size_t)s * (size_t)src.sample_stride;
+    auto at = [&](int ry, int rx) {
+        int y = min(max(Y0 + ry, 0), src.H - 1), x = min(max(X0 + rx, 0), src.W - 1);
+        return sbase + (size_t)y * (size_t)src.pitch + (size_t)x;
+    };
+    const float bref = (src.plane[3] ? __ldg(src.plane[3] + at(RI / 2, RI / 2)) : src.value[3]) * src.scale[3];
+    if (threadIdx.x == 0) S.bref = bref;
+    for (int i = threadIdx.x; i < NRI; i += NT) {
+        const size_t off = at(i / RI, i % RI);
+        float v[CIN];
+#pragma unroll
+        for (int c = 0; c < CIN; c++) {
+            v[c] = (src.plane[c] ? __ldg(src.plane[c] + off) : src.value[c]) * src.scale[c];
+            S.xs[i * CIN + c] = v[c];
+        }
+        const float br = v[3] - bref;
+        const uint16_t bh = bf(br);
+        const uint16_t bl = bf(br - fb(bh));
+        uint4 w;
+        w.x = pack2(v[0], v[1]);
+        w.y = pack16(bf(v[2]), bh);
+        w.z = pack16(bl, bf(v[4]));
+        w.w = pack16(bf(v[5]), 0);
+        *reinterpret_cast<uint4*>(&S.xb[i * CB]) = w;
+    }
+    proxy_fence();
+}
+
+// Thread 0: the MMAs of one layer, then their completion on the barrier.
+__device__ void tcIssue1(const TcSmem& S, uint32_t tmem) {
+    tc_after_sync();
+    const uint32_t xb = saddr(S.xb), w1 = saddr(S.w1t);
+    for (int mt = 0; mt < M1TC; mt++)
+        for (int s = 0; s < KS1; s++) {
+            const uint32_t cell = mt * 128 + (s / 5) * 2 * RI + s % 5;
+            tc_mma(tmem + mt * 32, sdesc(xb + cell * 16, RI * 16, 128), sdesc(w1 + s * 1024, 512, 128),
+                   s > 0);
+        }
+    tc_commit(const_cast<uint64_t*>(&S.bar));
+}
+__device__ void tcIssue2(const TcSmem& S, uint32_t tmem) {
+    tc_after_sync();
+    const uint32_t a1 = saddr(S.a1), w2 = saddr(S.w2t);
+    for (int mt = 0; mt < M2TC; mt++)
+        for (int s = 0; s < KS2; s++) {
+            const int tap = s >> 1, kb = s & 1;
+            const uint32_t cell = mt * 128 + (tap / 3) * RI + tap % 3;
+            tc_mma(tmem + mt * 32, sdesc(a1 + kb * 2 * A1PLANE + cell * 16, A1PLANE, 128),
+                   sdesc(w2 + (tap * 4 + 2 * kb) * 512, 512, 128), s > 0);
+        }
+    tc_commit(const_cast<uint64_t*>(&S.bar));
+}
+
+// Wait for the layer's MMAs (every thread); false (and the device error
+// flag set) when the wait gave up, after a second bounded wait for them.
+__device__ bool tcWait(TcSmem& S, uint32_t& phase) {
+    const bool ok = __syncthreads_and(bar_wait(&S.bar, phase));
+    if (!ok) {
+        bar_wait(&S.bar, phase);
+        if (threadIdx.x == 0) atomicOr(&g_tc_error, 1);
+    }
+    phase ^= 1u;
+    tc_after_sync();
+    return ok;
+}
+
+// Layer-1 epilogue: rows of M tiles warp/4 and warp/4 + 2 at this warp's
+// tensor-memory lanes -> relu(acc + b1 - (centre bed - bref) sbed) as BF16
+// into the activation planes.
+__device__ void tcEpilogue1(TcSmem& S, uint32_t tmem) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, lg = warp & 3;
+    const float bref = S.bref;
+#pragma unroll 1
+    for (int mt = warp >> 2; mt < M1TC; mt += 2) {
+        float v[32];
+        tc_ld32(tmem + ((uint32_t)(32 * lg) << 16) + mt * 32, v);
+        const int m = mt * 128 + 32 * lg + lane;
+        if (m >= A1C) continue;
+        const float cb = S.xs[(m + 2 * RI + 2) * CIN + 3] - bref;
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            uint4 w;
+            uint32_t q[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int o = 8 * p + 2 * e;
+                q[e] = pack2(relu(v[o] + S.b1[o] - cb * S.sbed[o]),
+                             relu(v[o + 1] + S.b1[o + 1] - cb * S.sbed[o + 1]));
+            }
+            w.x = q[0];
+            w.y = q[1];
+            w.z = q[2];
+            w.w = q[3];
+            *reinterpret_cast<uint4*>(&S.a1[p][m * 8]) = w;
+        }
+    }
+    proxy_fence();
+    tc_before_sync();
+}
+
+// Layer-2 epilogue and layer 3 for the row of M tile mt at this thread's
+// lane: out = W3 relu(acc + b2) + b3.  Returns the output cell's index in
+// the 16 x 16 tile (oy*16 + ox), or -1 for a row that is not an output.
+__device__ int tcOutputs(const TcSmem& S, uint32_t tmem, int mt, float out[COUT]) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, lg = warp & 3;
+    float v[32];
+    tc_ld32(tmem + ((uint32_t)(32 * lg) << 16) + mt * 32, v);
+    const int m = mt * 128 + 32 * lg + lane, oy = m / RI, ox = m % RI;
+    if (oy >= OT || ox >= OT) return -1;
+#pragma unroll
+    for (int c = 0; c < COUT; c++) out[c] = S.b3[c];
+#pragma unroll
+    for (int k = 0; k < C1; k++) {
+        const float a = relu(v[k] + S.b2[k]);
+#pragma unroll
+        for (int c = 0; c < COUT; c++) out[c] = fmaf(S.w3[c][k], a, out[c]);
+    }
+    return oy * OT + ox;
+}
+
+// One tcgen05.mma (M 128, N 32, K 16) on fixed BF16 values, with the
+// operand layout of the forward pass (K-major, no swizzle, 8-row groups
+// 128 bytes apart, the two K chunks LBO bytes apart: 2048 for A, 512 for B),
+// and the accumulator read back through tcgen05.ld: out[row * 32 + col] = D.
+// A[r][k] = (r % 7) - 3 + (k % 5) / 4, B[n][k] = (n % 5) - 2 + (k % 3) / 2,
+// so every product and sum is exact in FP32.  The buffers are larger than
+// the operands so that any reading of the two offsets stays inside them.
+__global__ void __launch_bounds__(128) k_tc_selftest(float* __restrict__ out) {
+    __shared__ __align__(128) uint16_t a[16384];
+    __shared__ __align__(128) uint16_t b[1024];
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tm;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < 16384; i += 128) a[i] = 0;
+    for (int i = tid; i < 1024; i += 128) b[i] = 0;
+    __syncthreads();
+    for (int i = tid; i < 128 * 16; i += 128) {
+        const int r = i / 16, k = i % 16;
+        a[((r / 8) * 128 + (k / 8) * 2048 + (r % 8) * 16) / 2 + k % 8] = bf((r % 7) - 3 + 0.25f * (k % 5));
+    }
+    for (int i = tid; i < 32 * 16; i += 128) {
+        const int n = i / 16, k = i % 16;
+        b[((n / 8) * 128 + (k / 8) * 512 + (n % 8) * 16) / 2 + k % 8] = bf((n % 5) - 2 + 0.5f * (k % 3));
+    }
+    proxy_fence();
+    if (tid == 0) bar_init(&bar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&tm)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = tm;
+    if (tid == 0) {
+        tc_mma(tmem, sdesc(saddr(a), 2048, 128), sdesc(saddr(b), 512, 128), false);
+        tc_commit(&bar);
+    }
+    const bool ok = __syncthreads_and(bar_wait(&bar, 0));
+    if (!ok) {
+        bar_wait(&bar, 0);
+        if (tid == 0) atomicOr(&g_tc_error, 1);
+    }
+    tc_after_sync();
+    if (ok) {
+        float v[32];
+        tc_ld32(tmem + ((uint32_t)(32 * warp) << 16), v);
+#pragma unroll
+        for (int c = 0; c < 32; c++) out[(32 * warp + lane) * 32 + c] = v[c];
+    }
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS)
+                     : "memory");
+}
+
 // ------------------------------------------------------------------ forward
 // Raw net outputs of every output cell of src.
 __global__ void __launch_bounds__(NT, 2) k_forward(rift_closure_src src, const float* __restrict__ P,
                                                    float* __restrict__ out) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    NetSmem& S = *reinterpret_cast<NetSmem*>(smem_raw);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    stageNet(S, P);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
+    const int warp = threadIdx.x >> 5;
+    tcSetup(S, P);
+    const uint32_t tmem = S.tmem;
+    uint32_t phase = 0;
     const int ntile = tileCount(src);
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const TileGeom G = tileGeom(src, tile);
         __syncthreads();
-        stageInput(S, src, G.s, G.Y - 3, G.X - 3);
+        tcStageInput(S, src, G.s, G.Y - 3, G.X - 3);
         __syncthreads();
-        conv1(S, warp, lane);
+        if (threadIdx.x == 0) tcIssue1(S, tmem);
+        if (!tcWait(S, phase)) break;
+        tcEpilogue1(S, tmem);
         __syncthreads();
-        float z2[2][4][4], o[2][4];
-        conv23(S, warp, lane, z2, o);
-        if (t < 2) {
+        if (threadIdx.x == 0) tcIssue2(S, tmem);
+        if (!tcWait(S, phase)) break;
 #pragma unroll
-            for (int m = 0; m < 2; m++)
+        for (int k = 0; k < 2; k++) {
+            const int mt = (warp >> 2) + 2 * k;
+            if (mt >= M2TC) break;
+            float o[COUT];
+            const int q = tcOutputs(S, tmem, mt, o);
+            if (q < 0) continue;
+            const int y = G.Y + q / OT - src.oy0, x = G.X + q % OT - src.ox0;
+            if (y >= src.OH || x >= src.OW) continue;
 #pragma unroll
-                for (int r = 0; r < 2; r++) {
-                    const int y = G.Y + warp + 8 * m - src.oy0, x = G.X + g + 8 * r - src.ox0;
-                    if (y >= src.OH || x >= src.OW) continue;
-#pragma unroll
-                    for (int e = 0; e < 2; e++) {
-                        const int ch = 2 * t + e;
-                        out[(((size_t)G.s * COUT + ch) * src.OH + y) * src.OW + x] = o[m][2 * r + e];
-                    }
-                }
+            for (int c = 0; c < COUT; c++)
+                out[(((size_t)G.s * COUT + c) * src.OH + y) * src.OW + x] = o[c];
         }
+        tc_before_sync();
     }
+    tcTeardown(S);
 }
 
 // ----------------------------------------------------------------- training
@@ -397,7 +745,7 @@ struct TrainArgs {
 };
 
 __global__ void __launch_bounds__(NT, 1) k_train(TrainArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     TrainSmem& T = *reinterpret_cast<TrainSmem*>(smem_raw);
     NetSmem& S = T.n;
     const rift_closure_src& src = A.src;
@@ -734,18 +1082,20 @@ struct ApplyArgs {
 // Net outputs -> gated, limited face corrections of every 16 x 16 block of
 // interior cells (zeros for dry blocks and blocks that fall back).
 __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    NetSmem& S = *reinterpret_cast<NetSmem*>(smem_raw);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
     const rift_closure_src& src = A.src;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
-    stageNet(S, A.P);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    tcSetup(S, A.P);
+    const uint32_t tmem = S.tmem;
+    uint32_t phase = 0;
     const float hminS = A.hmin * src.scale[0], invS0 = 1.f / src.scale[0];
     const int ntile = tileCount(src);
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const TileGeom G = tileGeom(src, tile);
         __syncthreads();
         if (tid == 0) S.red[0] = 0;
-        stageInput(S, src, 0, G.Y - 3, G.X - 3);
+        tcStageInput(S, src, 0, G.Y - 3, G.X - 3);
         __syncthreads();
         int wet = 0;
         for (int i = tid; i < (OT + 1) * (OT + 1); i += NT) {
@@ -763,52 +1113,59 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
             }
             continue;
         }
-        conv1(S, warp, lane);
+        if (tid == 0) tcIssue1(S, tmem);
+        if (!tcWait(S, phase)) break;
+        tcEpilogue1(S, tmem);
         __syncthreads();
-        float z2[2][4][4], o[2][4];
-        conv23(S, warp, lane, z2, o);
-        float cm[2][2] = {}, cq[2][2] = {}, ind = 0.f;
-        if (t < 2) {
-            const bool east = t == 0;
-            const float inv = east ? A.inv_dx : A.inv_dy;
+        if (tid == 0) tcIssue2(S, tmem);
+        if (!tcWait(S, phase)) break;
+        // this thread's output cells (up to two) and their four corrections:
+        // east-face mass and momentum, north-face mass and momentum
+        int cell[2] = {-1, -1};
+        float cv[2][4] = {};
+        float ind = 0.f;
 #pragma unroll
-            for (int m = 0; m < 2; m++)
+        for (int k = 0; k < 2; k++) {
+            const int mt = (warp >> 2) + 2 * k;
+            if (mt >= M2TC) break;
+            float o[COUT];
+            const int q = tcOutputs(S, tmem, mt, o);
+            if (q < 0) continue;
+            const int oy = q / OT, ox = q % OT, y = G.Y + oy, x = G.X + ox;
+            if (y - src.oy0 >= src.OH || x - src.ox0 >= src.OW) continue;
+            cell[k] = q;
+            const float hc = S.xs[((oy + 3) * RI + ox + 3) * CIN] * invS0;
 #pragma unroll
-                for (int r = 0; r < 2; r++) {
-                    const int oy = warp + 8 * m, ox = g + 8 * r;
-                    const int y = G.Y + oy, x = G.X + ox;
-                    const int yn = east ? y : y + 1, xn = east ? x + 1 : x;
-                    bool ok = x >= 3 && y >= 3 && xn <= A.nx - 4 && yn <= A.ny - 4;
-                    const float hc = S.xs[((oy + 3) * RI + ox + 3) * CIN] * invS0;
-                    const float hn = S.xs[((oy + 3 + (east ? 0 : 1)) * RI + ox + 3 + (east ? 1 : 0)) * CIN] * invS0;
-                    ok = ok && hc > A.hmin && hn > A.hmin;
-                    float vm = ok ? o[m][2 * r] * A.osc[2 * t] : 0.f;
-                    float vq = ok ? o[m][2 * r + 1] * A.osc[2 * t + 1] : 0.f;
-                    const float hd = vm > 0.f ? hc : hn;
-                    if (ok) {
-                        ind = fmaxf(ind, fabsf(vm) * A.dtw * inv / hd);
-                        const float cap = A.lim * hd / (A.dtw * inv);
-                        vm = fminf(fmaxf(vm, -cap), cap);
-                    }
-                    cm[m][r] = vm;
-                    cq[m][r] = vq;
+            for (int f = 0; f < 2; f++) {
+                const bool east = f == 0;
+                const float inv = east ? A.inv_dx : A.inv_dy;
+                const int yn = east ? y : y + 1, xn = east ? x + 1 : x;
+                const float hn = S.xs[((oy + 3 + (east ? 0 : 1)) * RI + ox + 3 + (east ? 1 : 0)) * CIN] * invS0;
+                const bool ok = x >= 3 && y >= 3 && xn <= A.nx - 4 && yn <= A.ny - 4 && hc > A.hmin &&
+                                hn > A.hmin;
+                float vm = ok ? o[2 * f] * A.osc[2 * f] : 0.f;
+                const float vq = ok ? o[2 * f + 1] * A.osc[2 * f + 1] : 0.f;
+                const float hd = vm > 0.f ? hc : hn;
+                if (ok) {
+                    ind = fmaxf(ind, fabsf(vm) * A.dtw * inv / hd);
+                    const float cap = A.lim * hd / (A.dtw * inv);
+                    vm = fminf(fmaxf(vm, -cap), cap);
                 }
+                cv[k][2 * f] = vm;
+                cv[k][2 * f + 1] = vq;
+            }
         }
+        tc_before_sync();
         for (int s = 16; s > 0; s >>= 1) ind = fmaxf(ind, __shfl_xor_sync(0xffffffffu, ind, s));
         if (lane == 0) atomicMax(&S.red[0], __float_as_int(ind));
         __syncthreads();
         const bool fallback = __int_as_float(S.red[0]) > A.tau;
-        if (t < 2) {
 #pragma unroll
-            for (int m = 0; m < 2; m++)
+        for (int k = 0; k < 2; k++) {
+            if (cell[k] < 0) continue;
+            const size_t c = (size_t)(G.Y + cell[k] / OT) * A.pitch + G.X + cell[k] % OT;
 #pragma unroll
-                for (int r = 0; r < 2; r++) {
-                    const int y = G.Y + warp + 8 * m, x = G.X + g + 8 * r;
-                    if (y - src.oy0 >= src.OH || x - src.ox0 >= src.OW) continue;
-                    size_t c = (size_t)y * A.pitch + x;
-                    A.corr[(2 * t) * A.plane + c] = fallback ? 0.f : cm[m][r];
-                    A.corr[(2 * t + 1) * A.plane + c] = fallback ? 0.f : cq[m][r];
-                }
+            for (int ch = 0; ch < 4; ch++) A.corr[ch * A.plane + c] = fallback ? 0.f : cv[k][ch];
         }
         if (tid == 0) {
             A.fell[tile] = fallback ? 1 : 0;
@@ -816,6 +1173,7 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
             if (fallback) atomicAdd(&A.counters[1], 1);
         }
     }
+    tcTeardown(S);
 }
 
 // U^n -= dtw x divergence of the face corrections (cells one inside the
@@ -892,7 +1250,7 @@ extern "C" {
 
 int rift_closure_forward(const rift_closure_src* src, const float* params, float* out, void* stream) {
     if (!srcOk(src) || !params || !out) return fail(RIFT_ERR_ARG, "rift_closure_forward: bad argument");
-    const size_t smem = sizeof(rc::NetSmem);
+    const size_t smem = sizeof(rc::TcSmem);
     const int tiles = rc::tileCount(*src);
     int grid = 0, rc_;
     if ((rc_ = residentGrid((const void*)rc::k_forward, smem, tiles, &grid))) return rc_;
@@ -969,7 +1327,7 @@ int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src
     A.tau = tau;
     A.fell = block_fell;
     A.counters = counters;
-    const size_t smem = sizeof(rc::NetSmem);
+    const size_t smem = sizeof(rc::TcSmem);
     const int tiles = rc::tileCount(*src);
     int grid = 0, rc_;
     if ((rc_ = residentGrid((const void*)rc::k_closure, smem, tiles, &grid))) return rc_;
@@ -979,6 +1337,24 @@ int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src
     rc::k_apply<<<grd, blk, 0, st>>>(view->h, view->hu, view->hv, corr, block_fell, A.plane, view->pitch,
                                      view->h_nx, view->h_ny, (float)(dtw / view->dx), (float)(dtw / view->dy));
     return launched("k_apply");
+}
+
+int rift_closure_selftest(float* out, void* stream) {
+    if (!out) return fail(RIFT_ERR_ARG, "rift_closure_selftest: bad argument");
+    rc::k_tc_selftest<<<1, 128, 0, (cudaStream_t)stream>>>(out);
+    return launched("k_tc_selftest");
+}
+
+int rift_closure_check(void* stream) {
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) return fail(RIFT_ERR_CUDA, std::string("rift_closure_check: ") + cudaGetErrorString(e));
+    int flag = 0;
+    const int zero = 0;
+    if (cudaMemcpyFromSymbol(&flag, rc::g_tc_error, sizeof(int)) != cudaSuccess ||
+        cudaMemcpyToSymbol(rc::g_tc_error, &zero, sizeof(int)) != cudaSuccess)
+        return fail(RIFT_ERR_CUDA, "rift_closure_check: status read failed");
+    if (flag) return fail(RIFT_ERR_CUDA, "rift_closure_check: a tensor-core completion wait gave up");
+    return RIFT_OK;
 }
 
 const char* rift_closure_last_error(void) { return g_err.c_str(); }

@@ -28,6 +28,9 @@
 #include "rift_grow.cuh"
 #include "rift_kernels.cuh"
 #include "rift_march.cuh"
+#ifdef RIFT_UPDATE1_TMA
+#include "rift_update1t.cuh"
+#endif
 #include "rift_persist.cuh"
 #include "rift_ensemble.cuh"
 
@@ -70,10 +73,16 @@ struct rift_handle {
     int* owner = nullptr;  // [gridSize] tile table of the persistent loop
     int* tileFlag = nullptr;  // [gridSize] stage-1 completion of the persistent loop
     long long persistSteps = 0, graphSteps = 0;  // steps run by each path (diagnostics)
+    long long launches = 0;  // kernels launched by the run paths (graph replays count their kernels)
+    int graphKernels = 0;    // kernel nodes of the per-step graph
     int* strips = nullptr;
     uint8_t* stripFlag = nullptr;
     int marchRows = STRIP_TY;  // tile rows per march work item (1, 2 or 4)
     CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
+#ifdef RIFT_UPDATE1_TMA
+    U1Maps tmU1{};                           // 116 x 7-row boxes of k_update1t
+    float* tmU1Rain[2] = {nullptr, nullptr};  // rain maps the boxes were encoded for
+#endif
     cudaStream_t stream = nullptr;
     float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
     float* D = nullptr;  // [3] planes: the march's stage-1 divergence
@@ -360,7 +369,27 @@ const void* persistKernel(const rift_handle* h) {
     }
 }
 
+#ifdef RIFT_UPDATE1_TMA
+template <uint32_t FIX>
+constexpr uint32_t u1Smem() {
+    return u1SmemBytes<(FIX & F_RAIN_G) != 0>();
+}
+template <uint32_t FIX>
+void launchUpdate1t(const rift_handle* h, const Params& P, cudaStream_t s) {
+    k_update1t<FIX><<<h->gridUpdate, MT, u1Smem<FIX>(), s>>>(h->tmU1, P);
+}
+#endif
+
 void launchUpdate1(const rift_handle* h, const Params& P, cudaStream_t s) {
+#ifdef RIFT_UPDATE1_TMA
+    switch (marchFix(h)) {
+        case FIX_RAIN: launchUpdate1t<FIX_RAIN>(h, P, s); break;
+        case FIX_INFIL_SRC: launchUpdate1t<FIX_INFIL_SRC>(h, P, s); break;
+        case FIX_RAINMAP_DRAIN: launchUpdate1t<FIX_RAINMAP_DRAIN>(h, P, s); break;
+        default: launchUpdate1t<0>(h, P, s);
+    }
+    return;
+#endif
     switch (marchFix(h)) {
         case FIX_RAIN: k_update1<FIX_RAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
         case FIX_INFIL_SRC: k_update1<FIX_INFIL_SRC><<<h->gridUpdate, MT, 0, s>>>(P); break;
@@ -369,7 +398,21 @@ void launchUpdate1(const rift_handle* h, const Params& P, cudaStream_t s) {
     }
 }
 
+// Boxes of the rain maps for k_update1t (the maps appear with rift_set_map).
+void refreshUpdateMaps(rift_handle* h) {
+#ifdef RIFT_UPDATE1_TMA
+    for (int k = 0; k < 2; k++)
+        if (h->maps[0][k] && h->maps[0][k] != h->tmU1Rain[k]) {
+            encodeMap(h, k ? &h->tmU1.r1 : &h->tmU1.r0, h->maps[0][k], 1, UBOXW, URC);
+            h->tmU1Rain[k] = h->maps[0][k];
+        }
+#else
+    (void)h;
+#endif
+}
+
 void enqueueStep(rift_handle* h) {
+    refreshUpdateMaps(h);
     Params P = makeParams(h);
     cudaStream_t s = h->stream;
     if (h->has(RIFT_F_RAIN_GRID) || h->has(RIFT_F_SURGE_GRID))
@@ -396,6 +439,9 @@ int buildGraph(rift_handle* h) {
     cudaError_t e = cudaStreamEndCapture(h->stream, &h->graph);
     if (e != cudaSuccess) return fail(h, RIFT_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
     CUDA_TRY(h, cudaGraphInstantiate(&h->graphExec, h->graph, 0));
+    size_t nodes = 0;  // every node of the step graph is a kernel launch
+    CUDA_TRY(h, cudaGraphGetNodes(h->graph, nullptr, &nodes));
+    h->graphKernels = (int)nodes;
     return RIFT_OK;
 }
 
@@ -681,6 +727,19 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
         (r = encodeMap(h, &h->tmBm, h->B, 3, MBOXW, MRC)) ||
         (r = encodeMap(h, &h->tmEm, h->E, 4, MBOXW, MRC)))
         return r;
+#ifdef RIFT_UPDATE1_TMA
+    if ((r = encodeMap(h, &h->tmU1.a, h->A, 3, UBOXW, URC)) ||
+        (r = encodeMap(h, &h->tmU1.d, h->D, 3, UBOXW, URC)) ||
+        (r = encodeMap(h, &h->tmU1.n, h->nman, 1, UBOXW, URC)))
+        return r;
+    cudaFuncSetAttribute(k_update1t<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, u1Smem<0>());
+    cudaFuncSetAttribute(k_update1t<FIX_RAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         u1Smem<FIX_RAIN>());
+    cudaFuncSetAttribute(k_update1t<FIX_INFIL_SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         u1Smem<FIX_INFIL_SRC>());
+    cudaFuncSetAttribute(k_update1t<FIX_RAINMAP_DRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         u1Smem<FIX_RAINMAP_DRAIN>());
+#endif
     h->nSX = (h->nBX + STRIP_TX - 1) / STRIP_TX;
     h->nSY = (h->nBY + STRIP_TY - 1) / STRIP_TY;
     const int NS = h->nSX * h->nSY;
@@ -698,7 +757,12 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_march<1>, MT, 0);
     h->gridMarch1 = std::max(1, std::min(NS, h->numSMs * std::max(occ1, 1)));
     int occU = 1;
+#ifdef RIFT_UPDATE1_TMA
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1t<FIX_RAINMAP_DRAIN>, MT,
+                                                  u1Smem<FIX_RAINMAP_DRAIN>());
+#else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1<>, MT, 0);
+#endif
     h->gridUpdate = std::max(1, std::min(2 * NS, h->numSMs * std::max(occU, 1)));
     // the march pays off once every resident march CTA has a strip of its own
     h->marchMin = h->numSMs * occ;
@@ -1024,6 +1088,7 @@ int launchPersist(rift_handle* h, int nsteps) {
     void* args[] = {(void*)&h->tmA, (void*)&h->tmB, (void*)&h->tmE, (void*)&P, (void*)&nsteps};
     CUDA_TRY(h, cudaLaunchCooperativeKernel(persistKernel(h), dim3(grid), dim3(NT), args, 0,
                                             h->stream));
+    h->launches += 1;
     return RIFT_OK;
 }
 
@@ -1055,6 +1120,7 @@ int runSteps(rift_handle* h, int nsteps, bool* mirrorCurrent) {
         if ((rc = buildGraph(h))) return rc;
         for (int k = 0; k < chunk; k++) CUDA_TRY(h, cudaGraphLaunch(h->graphExec, h->stream));
         h->graphSteps += chunk;
+        h->launches += (long long)chunk * h->graphKernels;
         left -= chunk;
         *mirrorCurrent = false;
         if (left > 0) {
@@ -1123,6 +1189,7 @@ bool stepGraph(rift_handle* h, int& rc) {
         return true;
     }
     h->persistSteps += h->hst->steps_done - before;
+    h->launches += 1;
     return true;
 }
 }  // namespace
@@ -1572,6 +1639,7 @@ int rift_bench_run(rift_handle* h, int32_t nsteps, double* ms_total, double* act
     const int M = std::min(nsteps, 20);
     h->hst->activeCells = 0;
     if ((rc = pushState(h))) return rc;
+    refreshUpdateMaps(h);
     Params P = makeParams(h);
     cudaStream_t s = h->stream;
     double stageSum = 0.0;
@@ -1625,6 +1693,12 @@ int rift_get_path_stats(rift_handle* h, int64_t* persist_steps, int64_t* graph_s
     if (!h) return RIFT_ERR_ARG;
     if (persist_steps) *persist_steps = h->persistSteps;
     if (graph_steps) *graph_steps = h->graphSteps;
+    return RIFT_OK;
+}
+
+int rift_get_launch_count(rift_handle* h, int64_t* kernels) {
+    if (!h || !kernels) return RIFT_ERR_ARG;
+    *kernels = h->launches;
     return RIFT_OK;
 }
 
@@ -1735,6 +1809,7 @@ struct rift_ensemble {
     std::vector<rift_handle*> m;
     std::vector<double> memberSec;  // last run: device time from its start to each member's end
     int64_t soloCells = 0;          // members with at least this many interior cells run on their own
+    long long launches = 0;         // ensemble kernels launched (members run on their own count theirs)
     cudaStream_t stream = nullptr;
     Params* dP = nullptr;
     CUtensorMap* dMaps = nullptr;
@@ -1828,9 +1903,11 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
     ENS_TRY(e, cudaEventCreate(&ev0));
     ENS_TRY(e, cudaEventCreate(&ev1));
     ENS_TRY(e, cudaEventRecord(ev0, e->stream));
-    if (nAlive > 0)
+    if (nAlive > 0) {
         ENS_TRY(e, cudaLaunchCooperativeKernel((const void*)k_ensemble, dim3(e->grid), dim3(NT), args, 0,
                                                e->stream));
+        e->launches += 1;
+    }
     ENS_TRY(e, cudaEventRecord(ev1, e->stream));
     ENS_TRY(e, cudaStreamSynchronize(e->stream));
     {  // each member's completion on the device clock
@@ -1890,6 +1967,14 @@ int rift_ensemble_run(rift_ensemble* e, double t_stop, int32_t max_steps, double
         e->steps += h->hst->steps_done;
     }
     return rc;
+}
+
+int rift_ensemble_launch_count(rift_ensemble* e, int64_t* kernels) {
+    if (!e || !kernels) return RIFT_ERR_ARG;
+    long long n = e->launches;
+    for (rift_handle* h : e->m) n += h->launches;
+    *kernels = n;
+    return RIFT_OK;
 }
 
 int rift_ensemble_set_solo_cells(rift_ensemble* e, int64_t min_cells) {

@@ -164,6 +164,12 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c, in
 #ifndef RIFT_MARCH2_MINB
 #define RIFT_MARCH2_MINB 6
 #endif
+// Rows ahead at which stage 2 loads a cell's U^n and rain-map entries.
+#ifndef RIFT_MARCH2_PD
+#define RIFT_MARCH2_PD 1
+#endif
+constexpr int MARCH2_PD = RIFT_MARCH2_PD;
+static_assert(MARCH2_PD == 1 || MARCH2_PD == 2, "prefetch distance");
 template <int STAGE, uint32_t FIX = 0, int STY = STRIP_TY>
 __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH2_MINB)
     k_march(const __grid_constant__ CUtensorMap tmIn,
@@ -251,15 +257,22 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
         // centre values of the first output row (stage 2: U^n, and the rain
         // maps when the instantiation reads them ahead), loaded ahead of use
         const bool colIn = owned && i <= P.nx - 3;
-        float pre[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nextPre[8];
+        // row jj's centre values into d (U^n; the rain maps, or an L1 hint)
+        auto loadCentre = [&](float (&d)[8], int jj) {
+            const size_t cn = cidx(P, 0, jj, i);
+            d[0] = P.A[cn];
+            d[1] = P.A[cn + P.planeSize];
+            d[2] = P.A[cn + 2 * (size_t)P.planeSize];
+            if (RAINPRE)
+                loadRainMaps(P, cn, d + 6);
+            else
+                prefetchMaps(P, cellFlags<FIX>(C.fl), cn);
+        };
+        float pre[8], nextPre[8], farPre[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) nextPre[q] = 0.f;
-        if (STAGE == 2 && colIn && Y0 <= P.ny - 3) {
-            pre[0] = P.A[cidx(P, 0, Y0, i)];
-            pre[1] = P.A[cidx(P, 1, Y0, i)];
-            pre[2] = P.A[cidx(P, 2, Y0, i)];
-            if (RAINPRE) loadRainMaps(P, cidx(P, 0, Y0, i), pre + 6);
-        }
+        for (int q = 0; q < 8; q++) pre[q] = nextPre[q] = farPre[q] = 0.f;
+        if (STAGE == 2 && colIn && Y0 <= P.ny - 3) loadCentre(pre, Y0);
+        if (STAGE == 2 && MARCH2_PD == 2 && colIn && Y0 + 1 <= P.ny - 3) loadCentre(nextPre, Y0 + 1);
         float accMx = 0.f, accMy = 0.f;
         bool accWet = false;
         // two rows per iteration: the compiler interleaves their independent
@@ -283,16 +296,12 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             }
             const Row ld = loadRow(S.slot[(lead / MRC) % MNSLOT], lead % MRC, col);
             const int j = Y0 + R - 2;
-            // centre values of the next output row, in flight during this one
-            if (STAGE == 2 && colIn && j + 1 <= P.ny - 3) {
-                const size_t cn = cidx(P, 0, j + 1, i);
-                nextPre[0] = P.A[cn];
-                nextPre[1] = P.A[cn + P.planeSize];
-                nextPre[2] = P.A[cn + 2 * (size_t)P.planeSize];
-                if (RAINPRE)
-                    loadRainMaps(P, cn, nextPre + 6);
+            // centre values of the row MARCH2_PD ahead, in flight meanwhile
+            if (STAGE == 2 && colIn && j + MARCH2_PD <= P.ny - 3) {
+                if (MARCH2_PD == 2)
+                    loadCentre(farPre, j + 2);
                 else
-                    prefetchMaps(P, cellFlags<FIX>(C.fl), cn);
+                    loadCentre(nextPre, j + 1);
             }
             const int tslot = ((R - 2) / TH) * STRIP_TX + tcol;
             const bool cellOn = colIn && S.tact[tslot] && j <= P.ny - 3;
@@ -365,6 +374,13 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             pre[2] = nextPre[2];
             pre[6] = nextPre[6];
             pre[7] = nextPre[7];
+            if (MARCH2_PD == 2) {
+                nextPre[0] = farPre[0];
+                nextPre[1] = farPre[1];
+                nextPre[2] = farPre[2];
+                nextPre[6] = farPre[6];
+                nextPre[7] = farPre[7];
+            }
             cur = nxt;
             nxt = ld;
         }

@@ -30,6 +30,24 @@ def torch():
     return torch
 
 
+def test_tcgen05_mma_layout_selftest(torch):
+    """One tcgen05.mma (128 x 32 x 16) through the forward pass's operand
+    descriptors and instruction descriptor, read back from tensor memory:
+    the product of small exactly representable values must be exact."""
+    out = torch.zeros(128 * 32, dtype=torch.float32, device="cuda")
+    closure._check(closure.load().rift_closure_selftest(ctypes.c_void_p(out.data_ptr()), None),
+                   "rift_closure_selftest")
+    closure._check(closure.load().rift_closure_check(None), "rift_closure_check")
+    r = np.arange(128)[:, None]
+    n = np.arange(32)[:, None]
+    k = np.arange(16)[None, :]
+    A = (r % 7) - 3 + 0.25 * (k % 5)
+    B = (n % 5) - 2 + 0.5 * (k % 3)
+    ref = (A @ B.T).astype(np.float32)
+    got = out.cpu().numpy().reshape(128, 32)
+    assert np.array_equal(got, ref), np.abs(got - ref).max()
+
+
 def _patches(rng, S=3, H=70):
     x = np.zeros((S, 6, H, H), np.float32)
     x[:, 0] = np.abs(rng.normal(0.3, 0.3, (S, H, H)))
