@@ -455,10 +455,11 @@ def test_ensemble_with_closure_matches_members_alone(torch):
 
 
 def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
-    """The plain fine-grid solve as the per-block fallback: every block falls
-    back (tau = 0) and is re-solved from the coarse state at the interval's
-    start on a fine patch (block + 4 coarse cells of halo, 2 m cells under 4 m
-    ones).  The re-solve keeps each block's volume, keeps wet and dry cells as
+    """The plain fine-grid solve as the per-block fallback: every block that
+    runs the net falls back (tau = 0; a block runs it when a cell of it is
+    deeper than hmin, here the wetter blocks along the rim after 300 s of
+    rain) and is re-solved from the coarse state at the interval's start on a
+    fine patch (block + 4 coarse cells of halo, 2 m cells under 4 m ones).  The re-solve keeps each block's volume, keeps wet and dry cells as
     they were, changes the wet cells of the blocks, and leaves the edge cells
     of the domain alone; a run with the fallback on stays finite and its mass
     ledger closes."""
@@ -476,11 +477,12 @@ def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
     run.apply(t1 - t0, t1)
     torch.cuda.synchronize()
     fell = run.fell.cpu().numpy()
-    assert fell.all()
+    evaluated, fallen = run.block_counts()
+    assert fallen == evaluated and int(fell.sum()) == fallen and fallen >= 8, (evaluated, fallen)
     h1 = sim.field("W") - bc
     v1 = sim.volume()
     n = run.fallback.refine(fell, u0, t0, t1, 0.5 * dt0)
-    assert n == len(fell) and run.fallback.refined == n
+    assert n == fallen and run.fallback.refined == n
     h2 = sim.field("W") - bc
     v2 = sim.volume()
     assert abs(v2 - v1) <= 1e-6 * v1, (v1, v2)
