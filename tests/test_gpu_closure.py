@@ -14,9 +14,12 @@ from rift_gb300 import capi, closure, synth
 
 pytestmark = pytest.mark.gpu
 
-# BF16 operands (8-bit mantissa) in every contraction, FP32 accumulation,
-# against true FP32 PyTorch (TF32 off).  Measured on GB300: forward 5.1e-3,
-# loss 2.5e-4, gradient blocks 1.6e-3 .. 2.5e-3; the bars keep 3-4x margin.
+# BF16 operands (8-bit mantissa) in the tensor-core layers (1 and 2 in the
+# forward and apply kernels on tcgen05, layer 3 there in FP32; all three in
+# the training kernel on mma.sync), FP32 accumulation, against true FP32
+# PyTorch (TF32 off).  Measured on GB300 with mma.sync everywhere: forward
+# 5.1e-3, loss 2.5e-4, gradient blocks 1.6e-3 .. 2.5e-3; the bars keep 3-4x
+# margin.
 FWD_TOL = 1.5e-2    # max |out - ref| / max |ref|
 LOSS_TOL = 2e-3     # relative loss difference
 GRAD_TOL = 1e-2     # |g - g_ref| / |g_ref| per parameter block
@@ -455,11 +458,13 @@ def test_ensemble_with_closure_matches_members_alone(torch):
 
 
 def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
-    """The plain fine-grid solve as the per-block fallback: every block that
-    runs the net falls back (tau = 0; a block runs it when a cell of it is
-    deeper than hmin, here the wetter blocks along the rim after 300 s of
-    rain) and is re-solved from the coarse state at the interval's start on a
-    fine patch (block + 4 coarse cells of halo, 2 m cells under 4 m ones).  The re-solve keeps each block's volume, keeps wet and dry cells as
+    """The plain fine-grid solve as the per-block fallback: every block whose
+    net output corrects a face falls back (tau = 0; a block runs the net when
+    a cell of it is deeper than hmin, here the wetter blocks along the rim
+    after 300 s of rain, and a block whose only deep cells sit on the domain
+    edge corrects no face) and is re-solved from the coarse state at the
+    interval's start on a fine patch (block + 4 coarse cells of halo, 2 m
+    cells under 4 m ones).  The re-solve keeps each block's volume, keeps wet and dry cells as
     they were, changes the wet cells of the blocks, and leaves the edge cells
     of the domain alone; a run with the fallback on stays finite and its mass
     ledger closes."""
@@ -478,7 +483,7 @@ def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
     torch.cuda.synchronize()
     fell = run.fell.cpu().numpy()
     evaluated, fallen = run.block_counts()
-    assert fallen == evaluated and int(fell.sum()) == fallen and fallen >= 8, (evaluated, fallen)
+    assert int(fell.sum()) == fallen and 8 <= fallen <= evaluated, (evaluated, fallen)
     h1 = sim.field("W") - bc
     v1 = sim.volume()
     n = run.fallback.refine(fell, u0, t0, t1, 0.5 * dt0)
