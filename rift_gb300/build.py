@@ -14,7 +14,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-use_fast_math", "-lineinfo", "-Xcompiler", "-fPIC", "-shared"]
 SOURCES = ["rift_engine.cu"]
 DEPS = ["rift_engine.cu", "rift_kernels.cuh", "rift_march.cuh", "rift_persist.cuh", "rift_grow.cuh",
-        "rift_device.cuh", "rift_ensemble.cuh", "rift_update1t.cuh"]
+        "rift_device.cuh", "rift_ensemble.cuh", "rift_update1.cuh"]
 
 
 def _stale(out, deps):

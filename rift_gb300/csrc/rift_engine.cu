@@ -28,9 +28,7 @@
 #include "rift_grow.cuh"
 #include "rift_kernels.cuh"
 #include "rift_march.cuh"
-#ifdef RIFT_UPDATE1_TMA
-#include "rift_update1t.cuh"
-#endif
+#include "rift_update1.cuh"
 #include "rift_persist.cuh"
 #include "rift_ensemble.cuh"
 
@@ -79,10 +77,8 @@ struct rift_handle {
     uint8_t* stripFlag = nullptr;
     int marchRows = STRIP_TY;  // tile rows per march work item (1, 2 or 4)
     CUtensorMap tmAm{}, tmBm{}, tmEm{};  // 120 x 4-row boxes of the march kernels
-#ifdef RIFT_UPDATE1_TMA
-    U1Maps tmU1{};                           // 116 x 7-row boxes of k_update1t
+    U1Maps tmU1{};                           // 116 x 7-row boxes of k_update1
     float* tmU1Rain[2] = {nullptr, nullptr};  // rain maps the boxes were encoded for
-#endif
     cudaStream_t stream = nullptr;
     float *A = nullptr, *B = nullptr, *E = nullptr, *nman = nullptr, *K = nullptr;
     float* D = nullptr;  // [3] planes: the march's stage-1 divergence
@@ -369,46 +365,31 @@ const void* persistKernel(const rift_handle* h) {
     }
 }
 
-#ifdef RIFT_UPDATE1_TMA
 template <uint32_t FIX>
 constexpr uint32_t u1Smem() {
     return u1SmemBytes<(FIX & F_RAIN_G) != 0>();
 }
 template <uint32_t FIX>
-void launchUpdate1t(const rift_handle* h, const Params& P, cudaStream_t s) {
-    k_update1t<FIX><<<h->gridUpdate, MT, u1Smem<FIX>(), s>>>(h->tmU1, P);
+void launchUpdate1Fix(const rift_handle* h, const Params& P, cudaStream_t s) {
+    k_update1<FIX><<<h->gridUpdate, MT, u1Smem<FIX>(), s>>>(h->tmU1, P);
 }
-#endif
 
 void launchUpdate1(const rift_handle* h, const Params& P, cudaStream_t s) {
-#ifdef RIFT_UPDATE1_TMA
     switch (marchFix(h)) {
-        case FIX_RAIN: launchUpdate1t<FIX_RAIN>(h, P, s); break;
-        case FIX_INFIL_SRC: launchUpdate1t<FIX_INFIL_SRC>(h, P, s); break;
-        case FIX_RAINMAP_DRAIN: launchUpdate1t<FIX_RAINMAP_DRAIN>(h, P, s); break;
-        default: launchUpdate1t<0>(h, P, s);
-    }
-    return;
-#endif
-    switch (marchFix(h)) {
-        case FIX_RAIN: k_update1<FIX_RAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
-        case FIX_INFIL_SRC: k_update1<FIX_INFIL_SRC><<<h->gridUpdate, MT, 0, s>>>(P); break;
-        case FIX_RAINMAP_DRAIN: k_update1<FIX_RAINMAP_DRAIN><<<h->gridUpdate, MT, 0, s>>>(P); break;
-        default: k_update1<><<<h->gridUpdate, MT, 0, s>>>(P);
+        case FIX_RAIN: launchUpdate1Fix<FIX_RAIN>(h, P, s); break;
+        case FIX_INFIL_SRC: launchUpdate1Fix<FIX_INFIL_SRC>(h, P, s); break;
+        case FIX_RAINMAP_DRAIN: launchUpdate1Fix<FIX_RAINMAP_DRAIN>(h, P, s); break;
+        default: launchUpdate1Fix<0>(h, P, s);
     }
 }
 
-// Boxes of the rain maps for k_update1t (the maps appear with rift_set_map).
+// Boxes of the rain maps for k_update1 (the maps appear with rift_set_map).
 void refreshUpdateMaps(rift_handle* h) {
-#ifdef RIFT_UPDATE1_TMA
     for (int k = 0; k < 2; k++)
         if (h->maps[0][k] && h->maps[0][k] != h->tmU1Rain[k]) {
             encodeMap(h, k ? &h->tmU1.r1 : &h->tmU1.r0, h->maps[0][k], 1, UBOXW, URC);
             h->tmU1Rain[k] = h->maps[0][k];
         }
-#else
-    (void)h;
-#endif
 }
 
 void enqueueStep(rift_handle* h) {
@@ -727,19 +708,19 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
         (r = encodeMap(h, &h->tmBm, h->B, 3, MBOXW, MRC)) ||
         (r = encodeMap(h, &h->tmEm, h->E, 4, MBOXW, MRC)))
         return r;
-#ifdef RIFT_UPDATE1_TMA
     if ((r = encodeMap(h, &h->tmU1.a, h->A, 3, UBOXW, URC)) ||
         (r = encodeMap(h, &h->tmU1.d, h->D, 3, UBOXW, URC)) ||
         (r = encodeMap(h, &h->tmU1.n, h->nman, 1, UBOXW, URC)))
         return r;
-    cudaFuncSetAttribute(k_update1t<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, u1Smem<0>());
-    cudaFuncSetAttribute(k_update1t<FIX_RAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         u1Smem<FIX_RAIN>());
-    cudaFuncSetAttribute(k_update1t<FIX_INFIL_SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         u1Smem<FIX_INFIL_SRC>());
-    cudaFuncSetAttribute(k_update1t<FIX_RAINMAP_DRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         u1Smem<FIX_RAINMAP_DRAIN>());
-#endif
+    CUDA_TRY(h, cudaFuncSetAttribute(k_update1<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     u1Smem<0>()));
+    CUDA_TRY(h, cudaFuncSetAttribute(k_update1<FIX_RAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     u1Smem<FIX_RAIN>()));
+    CUDA_TRY(h, cudaFuncSetAttribute(k_update1<FIX_INFIL_SRC>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, u1Smem<FIX_INFIL_SRC>()));
+    CUDA_TRY(h, cudaFuncSetAttribute(k_update1<FIX_RAINMAP_DRAIN>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     u1Smem<FIX_RAINMAP_DRAIN>()));
     h->nSX = (h->nBX + STRIP_TX - 1) / STRIP_TX;
     h->nSY = (h->nBY + STRIP_TY - 1) / STRIP_TY;
     const int NS = h->nSX * h->nSY;
@@ -757,12 +738,9 @@ int rift_create(const rift_grid_desc* g, rift_handle** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, k_march<1>, MT, 0);
     h->gridMarch1 = std::max(1, std::min(NS, h->numSMs * std::max(occ1, 1)));
     int occU = 1;
-#ifdef RIFT_UPDATE1_TMA
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1t<FIX_RAINMAP_DRAIN>, MT,
+    // the gridded-rain instantiation stages two more planes (3 CTAs per SM, 4 without)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1<FIX_RAINMAP_DRAIN>, MT,
                                                   u1Smem<FIX_RAINMAP_DRAIN>());
-#else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occU, k_update1<>, MT, 0);
-#endif
     h->gridUpdate = std::max(1, std::min(2 * NS, h->numSMs * std::max(occU, 1)));
     // the march pays off once every resident march CTA has a strip of its own
     h->marchMin = h->numSMs * occ;

@@ -21,7 +21,8 @@
 // Stage 1 needs dt, and dt needs the speeds of stage 1's own fluxes (the
 // first ComputeFluxes of the step).  So the stage-1 march computes the
 // fluxes, the tile speeds and dt (last CTA), and stores each cell's flux
-// divergence with the bed-slope source folded in (3 words); k_update1 then
+// divergence with the bed-slope source folded in (3 words); k_update1
+// (rift_update1.cuh) then
 // applies the rest of Integrate_1_k.  The step does one flux pass per stage
 // and no separate speed pass.
 #pragma once
@@ -164,12 +165,7 @@ __device__ __forceinline__ void marchDrain(MarchSmem& S, uint32_t par, int c, in
 #ifndef RIFT_MARCH2_MINB
 #define RIFT_MARCH2_MINB 6
 #endif
-// Rows ahead at which stage 2 loads a cell's U^n and rain-map entries.
-#ifndef RIFT_MARCH2_PD
-#define RIFT_MARCH2_PD 1
-#endif
-constexpr int MARCH2_PD = RIFT_MARCH2_PD;
-static_assert(MARCH2_PD == 1 || MARCH2_PD == 2, "prefetch distance");
+
 template <int STAGE, uint32_t FIX = 0, int STY = STRIP_TY>
 __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH2_MINB)
     k_march(const __grid_constant__ CUtensorMap tmIn,
@@ -268,11 +264,10 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             else
                 prefetchMaps(P, cellFlags<FIX>(C.fl), cn);
         };
-        float pre[8], nextPre[8], farPre[8];
+        float pre[8], nextPre[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) pre[q] = nextPre[q] = farPre[q] = 0.f;
+        for (int q = 0; q < 8; q++) pre[q] = nextPre[q] = 0.f;
         if (STAGE == 2 && colIn && Y0 <= P.ny - 3) loadCentre(pre, Y0);
-        if (STAGE == 2 && MARCH2_PD == 2 && colIn && Y0 + 1 <= P.ny - 3) loadCentre(nextPre, Y0 + 1);
         float accMx = 0.f, accMy = 0.f;
         bool accWet = false;
         // two rows per iteration: the compiler interleaves their independent
@@ -296,13 +291,8 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             }
             const Row ld = loadRow(S.slot[(lead / MRC) % MNSLOT], lead % MRC, col);
             const int j = Y0 + R - 2;
-            // centre values of the row MARCH2_PD ahead, in flight meanwhile
-            if (STAGE == 2 && colIn && j + MARCH2_PD <= P.ny - 3) {
-                if (MARCH2_PD == 2)
-                    loadCentre(farPre, j + 2);
-                else
-                    loadCentre(nextPre, j + 1);
-            }
+            // centre values of the next output row, in flight during this one
+            if (STAGE == 2 && colIn && j + 1 <= P.ny - 3) loadCentre(nextPre, j + 1);
             const int tslot = ((R - 2) / TH) * STRIP_TX + tcol;
             const bool cellOn = colIn && S.tact[tslot] && j <= P.ny - 3;
             float spx, spy;
@@ -374,13 +364,7 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
             pre[2] = nextPre[2];
             pre[6] = nextPre[6];
             pre[7] = nextPre[7];
-            if (MARCH2_PD == 2) {
-                nextPre[0] = farPre[0];
-                nextPre[1] = farPre[1];
-                nextPre[2] = farPre[2];
-                nextPre[6] = farPre[6];
-                nextPre[7] = farPre[7];
-            }
+
             cur = nxt;
             nxt = ld;
         }
@@ -417,91 +401,6 @@ __global__ void __launch_bounds__(MT, STAGE == 1 ? RIFT_MARCH1_MINB : RIFT_MARCH
         finishDt(P, tmxAll, tmyAll, &last);
         resyncDeactivated(P);
     }
-}
-
-// The rest of Integrate_1_k (grid.cu:856-1023) on the march's strips, once
-// dt is known: sources, friction, the RK stage, outputs and ghost cells, from
-// U^n and the stored divergence; in Euler mode also the tile wet flags.  No
-// halo, so the work item is half a strip (one tile row of 7 tiles): finer
-// items balance the grid.  One thread per column, rows in pairs whose loads
-// are in flight together (64 registers: 8 CTAs per SM).
-template <uint32_t FIX = 0>
-__global__ void __launch_bounds__(MT, 8) k_update1(Params P) {
-    __shared__ int tact[STRIP_TX];
-    __shared__ int twet[STRIP_TX];
-    if (P.st->stop || !useMarch(P)) return;
-    const int tid = threadIdx.x;
-    const int nItems = 2 * P.st->nStrips;
-    const StageConsts C = blockConsts<1>(P);
-    const size_t pl = (size_t)P.planeSize;
-    const bool led = (cellFlags<FIX>(C.fl) & F_CHECKVOL) != 0;
-    Led L;
-    ledZero(L);
-    for (int item = blockIdx.x; item < nItems; item += gridDim.x) {
-        const int strip = P.strips[item >> 1];
-        const int half = item & 1;
-        const int sx = strip % P.nSX, sy = strip / P.nSX;
-        const int by = STRIP_TY * sy + half;  // the tile row of this item
-        const int X0 = MCOLS * sx + 2, Y0 = by * TH + 2;
-        const bool edgeStrip =
-            X0 == 2 || Y0 == 2 || X0 + MCOLS - 1 >= P.nx - 3 || Y0 + TH - 1 >= P.ny - 3;
-        __syncthreads();  // the previous item no longer reads the tile tables
-        if (tid < STRIP_TX) {
-            const int bx = STRIP_TX * sx + tid;
-            int a = 0;
-            if (bx < P.nBX && by < P.nBY)
-                a = P.prevAct[by * P.nBX + bx] && (bx * TW + 2 <= P.nx - 3) && (Y0 <= P.ny - 3);
-            tact[tid] = a;
-            twet[tid] = 0;
-        }
-        __syncthreads();
-        const int i = X0 + tid, slot = tid / TW;
-        if (tid < MCOLS && i <= P.nx - 3 && tact[slot]) {
-            const int tile = by * P.nBX + STRIP_TX * sx + slot;
-            constexpr int G = 2;
-            bool wetAny = false;
-            constexpr bool RAINPRE = (FIX & F_RAIN_G) != 0;
-            for (int r0 = 0; r0 < TH; r0 += G) {
-                float v[G][9];
-                bool on[G];
-#pragma unroll
-                for (int q = 0; q < G; q++) {
-                    const int j = Y0 + r0 + q;
-                    on[q] = r0 + q < TH && j <= P.ny - 3;
-                    if (on[q]) {
-                        const size_t c = cidx(P, 0, j, i);
-                        v[q][0] = P.D[c];
-                        v[q][1] = P.D[c + pl];
-                        v[q][2] = P.D[c + 2 * pl];
-                        v[q][3] = P.A[c];
-                        v[q][4] = P.A[c + pl];
-                        v[q][5] = P.A[c + 2 * pl];
-                        v[q][6] = P.nman[c];
-                        if (RAINPRE)
-                            loadRainMaps(P, c, &v[q][7]);
-                        else
-                            prefetchMaps(P, cellFlags<FIX>(C.fl), c);
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < G; q++) {
-                    if (!on[q]) continue;
-                    const float pre[8] = {v[q][6], 0.f, 0.f, 0.f, 0.f, 0.f, v[q][7], v[q][8]};
-                    wetAny |= cellUpdate<1, false, false, FIX, RAINPRE>(P, C, tile, Y0 + r0 + q, i, v[q][0],
-                                                          v[q][1], v[q][2], v[q][3], v[q][4],
-                                                          v[q][5], 0.f, 0.f, 0.f, 0.f, pre,
-                                                          edgeStrip, led ? &L : nullptr);
-                }
-            }
-            if (C.euler && wetAny) atomicOr(&twet[slot], 1);
-        }
-        if (C.euler) {
-            __syncthreads();
-            if (tid < STRIP_TX && tact[tid])
-                P.wet[by * P.nBX + STRIP_TX * sx + tid] = (uint8_t)((!(C.fl & F_TILE_ACC)) || twet[tid]);
-        }
-    }
-    if (led) flushLed(L, P.st->led);
 }
 
 }  // namespace rift

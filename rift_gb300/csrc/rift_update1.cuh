@@ -1,14 +1,17 @@
-// rift_update1t.cuh -- the rest of RK stage 1 on the march's items, with the
-// inputs streamed through shared memory by TMA.
+// rift_update1.cuh -- the rest of Integrate_1_k (grid.cu:856-1023) on the
+// march's items once dt is known: sources, friction, the RK stage, outputs
+// and ghost cells, from U^n and the divergence k_march<1> stored; in Euler
+// mode also the tile wet flags.
 //
-// Same work and arithmetic as k_update1 (rift_march.cuh): for every cell of
-// an active tile of a half strip (one tile row of 7 tiles, 112 x 14 cells),
-// the stage-1 sources, friction and RK combination from U^n and the stored
-// divergence.  k_update1 keeps its loads in registers two rows at a time and
-// waits on them; here an item's rows arrive in two 7-row chunks -- U^n (3
-// planes), the divergence (3), n, and with gridded rain the rain maps --
-// through a 2-slot ring of TMA copies that runs one chunk ahead, across
-// items, so the copies of the next chunk overlap the update of this one.
+// No halo, so the work item is half a strip (one tile row of 7 tiles,
+// 112 x 14 cells): finer items balance the grid.  One thread per column.
+// An item's rows arrive in two 7-row chunks -- U^n (3 planes), the
+// divergence (3), n, and with gridded rain the rain maps -- through a
+// 2-slot ring of TMA copies that runs one chunk ahead, across items, so the
+// copies of the next chunk overlap the update of this one.  (Loading the
+// same values into registers two rows at a time, the copies' latency was
+// exposed: 71% of the copy bandwidth; measured 1.9% slower per config-3
+// step than this kernel.)
 #pragma once
 #include "rift_march.cuh"
 
@@ -50,7 +53,7 @@ __device__ __forceinline__ void u1Item(const Params& P, int item, int& sx, int& 
 }
 
 template <uint32_t FIX = 0>
-__global__ void __launch_bounds__(MT, 3) k_update1t(const __grid_constant__ U1Maps M, Params P) {
+__global__ void __launch_bounds__(MT, 3) k_update1(const __grid_constant__ U1Maps M, Params P) {
     constexpr bool RAIN = (FIX & F_RAIN_G) != 0;
     constexpr uint32_t SLOT = u1SlotBytes<RAIN>();
     extern __shared__ __align__(128) unsigned char u1raw[];

@@ -160,4 +160,8 @@ def test_ensemble_with_solo_members_matches_members_alone(engine_api):
     assert sec[big].min() >= sec[~big].max()  # the solo members run after the kernel
     for name, a, b in zip(names, members, solo):
         _same(_state(a), _state(b), name)
+    # launches: the one ensemble kernel plus every kernel the solo members ran
+    solo_launches = sum(m.launch_count() for m, b_ in zip(members, big) if b_)
+    assert solo_launches > 0
+    assert ens.launch_count() == 1 + solo_launches
     ens.close()

@@ -236,3 +236,17 @@ def test_march_item_heights_match_on_a_dense_grid(engine_api, rows):
     assert abs(t0[0] - t1[0]) <= 1e-6 * t0[0]
     _close(W1, W0, f"{rows}-row items vs 2-row items")
     assert np.abs(U1 - U0)[2:-2, 2:-2].max() <= 1e-4
+
+
+def test_launch_count_counts_the_step_graph_kernels(engine_api):
+    """rift_get_launch_count: on the per-step graph (persistent loop off) each
+    step replays grow, speed, march and per-tile stage-1 kernels, the update,
+    and the two stage-2 kernels; gridded rain adds the map tracker."""
+    from rift_gb300 import synth
+    for case, per_step in ((synth.config1(N=256), 7),
+                           (synth.config3(N=512, nblocks=20), 8)):
+        sim = capi.Sim(case, api=engine_api).set_persistent(0).setup()
+        n0 = sim.launch_count()
+        sim.run(70)
+        assert sim.launch_count() - n0 == 70 * per_step, case.name
+        sim.close()
