@@ -510,22 +510,44 @@ __device__ void tcTeardown(TcSmem& S) {
                      : "memory");
 }
 
-// The block's input cells (stageInput's values), then the BF16 cells as the
-// layer-1 operand: each writer fences its shared stores for the async proxy.
-__device__ void tcStageInput(TcSmem& S, const rift_closure_src& src, int s, int Y0, int X0) {
+// A block's raw inputs in registers: this thread's cells i = tid and
+// tid + NT of the 22 x 22 block (484 < 2 NT), and the block's reference bed.
+// Loaded one block ahead, while the tensor cores work on the current one.
+struct TcInput {
+    float v[2][CIN];
+    float bref;
+};
+__device__ void tcLoadInput(TcInput& R, const rift_closure_src& src, int s, int Y0, int X0) {
     const size_t sbase = (size_t)s * (size_t)src.sample_stride;
     auto at = [&](int ry, int rx) {
         int y = min(max(Y0 + ry, 0), src.H - 1), x = min(max(X0 + rx, 0), src.W - 1);
         return sbase + (size_t)y * (size_t)src.pitch + (size_t)x;
     };
-    const float bref = (src.plane[3] ? __ldg(src.plane[3] + at(RI / 2, RI / 2)) : src.value[3]) * src.scale[3];
-    if (threadIdx.x == 0) S.bref = bref;
-    for (int i = threadIdx.x; i < NRI; i += NT) {
+    R.bref = src.plane[3] ? __ldg(src.plane[3] + at(RI / 2, RI / 2)) : src.value[3];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const int i = threadIdx.x + k * NT;
+        if (i >= NRI) break;
         const size_t off = at(i / RI, i % RI);
+#pragma unroll
+        for (int c = 0; c < CIN; c++) R.v[k][c] = src.plane[c] ? __ldg(src.plane[c] + off) : src.value[c];
+    }
+}
+
+// The loaded block into shared memory: scaled FP32 values (xs) and the
+// BF16 cells of the layer-1 operand (the bed relative to bref in two
+// halves); each writer fences its shared stores for the async proxy.
+__device__ void tcStoreInput(TcSmem& S, const TcInput& R, const rift_closure_src& src) {
+    const float bref = R.bref * src.scale[3];
+    if (threadIdx.x == 0) S.bref = bref;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const int i = threadIdx.x + k * NT;
+        if (i >= NRI) break;
         float v[CIN];
 #pragma unroll
         for (int c = 0; c < CIN; c++) {
-            v[c] = (src.plane[c] ? __ldg(src.plane[c] + off) : src.value[c]) * src.scale[c];
+            v[c] = R.v[k][c] * src.scale[c];
             S.xs[i * CIN + c] = v[c];
         }
         const float br = v[3] - bref;
@@ -704,12 +726,21 @@ __global__ void __launch_bounds__(NT, 2) k_forward(rift_closure_src src, const f
     const uint32_t tmem = S.tmem;
     uint32_t phase = 0;
     const int ntile = tileCount(src);
+    TcInput R;
+    if ((int)blockIdx.x < ntile) {
+        const TileGeom G0 = tileGeom(src, blockIdx.x);
+        tcLoadInput(R, src, G0.s, G0.Y - 3, G0.X - 3);
+    }
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const TileGeom G = tileGeom(src, tile);
         __syncthreads();
-        tcStageInput(S, src, G.s, G.Y - 3, G.X - 3);
+        tcStoreInput(S, R, src);
         __syncthreads();
         if (threadIdx.x == 0) tcIssue1(S, tmem);
+        if (tile + (int)gridDim.x < ntile) {  // the next block's inputs, during the MMAs
+            const TileGeom Gn = tileGeom(src, tile + gridDim.x);
+            tcLoadInput(R, src, Gn.s, Gn.Y - 3, Gn.X - 3);
+        }
         if (!tcWait(S, phase)) break;
         tcEpilogue1(S, tmem);
         __syncthreads();
@@ -1091,11 +1122,20 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
     uint32_t phase = 0;
     const float hminS = A.hmin * src.scale[0], invS0 = 1.f / src.scale[0];
     const int ntile = tileCount(src);
+    TcInput R;
+    if ((int)blockIdx.x < ntile) {
+        const TileGeom G0 = tileGeom(src, blockIdx.x);
+        tcLoadInput(R, src, 0, G0.Y - 3, G0.X - 3);
+    }
     for (int tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
         const TileGeom G = tileGeom(src, tile);
         __syncthreads();
         if (tid == 0) S.red[0] = 0;
-        tcStageInput(S, src, 0, G.Y - 3, G.X - 3);
+        tcStoreInput(S, R, src);
+        if (tile + (int)gridDim.x < ntile) {  // the next block's inputs, in flight meanwhile
+            const TileGeom Gn = tileGeom(src, tile + gridDim.x);
+            tcLoadInput(R, src, 0, Gn.Y - 3, Gn.X - 3);
+        }
         __syncthreads();
         int wet = 0;
         for (int i = tid; i < (OT + 1) * (OT + 1); i += NT) {
@@ -1238,6 +1278,11 @@ int residentGrid(const void* k, size_t smem, int tiles, int* out) {
     if (cudaGetDevice(&dev) != cudaSuccess) return fail(RIFT_ERR_CUDA, "no device");
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the whole shared-memory carveout, so that the occupancy below (and the
+    // launch) can place two 85 KB CTAs on an SM
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
     if (e != cudaSuccess) return fail(RIFT_ERR_CUDA, cudaGetErrorString(e));
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, rc::NT, smem);
     if (e != cudaSuccess || occ < 1) return fail(RIFT_ERR_CUDA, "closure kernel does not fit an SM");
