@@ -564,26 +564,32 @@ __device__ void tcStoreInput(TcSmem& S, const TcInput& R, const rift_closure_src
 }
 
 // Thread 0: the MMAs of one layer, then their completion on the barrier.
+// The loops unroll completely: every operand offset is a compile-time
+// constant added to a base descriptor (its address field counts 16-byte
+// units, and no shared address reaches 256 KB, so the sum never carries out
+// of the field), so the issuing thread spends a few instructions per MMA.
 __device__ void tcIssue1(const TcSmem& S, uint32_t tmem) {
     tc_after_sync();
-    const uint32_t xb = saddr(S.xb), w1 = saddr(S.w1t);
+    const uint64_t a0 = sdesc(saddr(S.xb), RI * 16, 128), b0 = sdesc(saddr(S.w1t), 512, 128);
+#pragma unroll
     for (int mt = 0; mt < M1TC; mt++)
+#pragma unroll
         for (int s = 0; s < KS1; s++) {
-            const uint32_t cell = mt * 128 + (s / 5) * 2 * RI + s % 5;
-            tc_mma(tmem + mt * 32, sdesc(xb + cell * 16, RI * 16, 128), sdesc(w1 + s * 1024, 512, 128),
-                   s > 0);
+            const uint32_t cell = mt * 128 + (s / 5) * 2 * RI + s % 5;  // 16-byte cells
+            tc_mma(tmem + mt * 32, a0 + cell, b0 + s * (1024 / 16), s > 0);
         }
     tc_commit(const_cast<uint64_t*>(&S.bar));
 }
 __device__ void tcIssue2(const TcSmem& S, uint32_t tmem) {
     tc_after_sync();
-    const uint32_t a1 = saddr(S.a1), w2 = saddr(S.w2t);
+    const uint64_t a0 = sdesc(saddr(S.a1), A1PLANE, 128), b0 = sdesc(saddr(S.w2t), 512, 128);
+#pragma unroll
     for (int mt = 0; mt < M2TC; mt++)
+#pragma unroll
         for (int s = 0; s < KS2; s++) {
             const int tap = s >> 1, kb = s & 1;
-            const uint32_t cell = mt * 128 + (tap / 3) * RI + tap % 3;
-            tc_mma(tmem + mt * 32, sdesc(a1 + kb * 2 * A1PLANE + cell * 16, A1PLANE, 128),
-                   sdesc(w2 + (tap * 4 + 2 * kb) * 512, 512, 128), s > 0);
+            const uint32_t cell = kb * 2 * A1C + mt * 128 + (tap / 3) * RI + tap % 3;
+            tc_mma(tmem + mt * 32, a0 + cell, b0 + (tap * 4 + 2 * kb) * (512 / 16), s > 0);
         }
     tc_commit(const_cast<uint64_t*>(&S.bar));
 }
