@@ -1292,6 +1292,26 @@ int residentGrid(const void* k, size_t smem, int tiles, int* out) {
     if (e != cudaSuccess) return fail(RIFT_ERR_CUDA, cudaGetErrorString(e));
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, rc::NT, smem);
     if (e != cudaSuccess || occ < 1) return fail(RIFT_ERR_CUDA, "closure kernel does not fit an SM");
+    // The same count from the SM's own limits (the occupancy call above gave
+    // one CTA per SM for the 85 KB tensor-core kernels on GB300, where two
+    // fit in shared memory and registers): CTAs per SM by shared memory (with
+    // the per-block reservation) and by registers (allocated per warp in
+    // units of 256), at most 4 (4 x 128 tensor-memory columns).  The kernels
+    // loop over tiles with no CTA waiting on another, so a CTA that does not
+    // fit simply starts when one ends.
+    cudaFuncAttributes fa{};
+    int smemSM = 0, resv = 0;
+    if (cudaFuncGetAttributes(&fa, k) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess) {
+        const size_t perBlock = smem + fa.sharedSizeBytes + (size_t)resv;
+        const int bySmem = (int)((size_t)smemSM / perBlock);
+        const int regsWarp = ((fa.numRegs * 32 + 255) / 256) * 256;
+        const int byRegs = regsWarp > 0 ? 65536 / (regsWarp * (rc::NT / 32)) : 1;
+        int mine = bySmem < byRegs ? bySmem : byRegs;
+        mine = mine < 4 ? mine : 4;
+        occ = occ > mine ? occ : mine;
+    }
     *out = tiles < sms * occ ? tiles : sms * occ;
     return RIFT_OK;
 }
