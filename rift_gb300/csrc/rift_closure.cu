@@ -372,12 +372,15 @@ __host__ __device__ __forceinline__ int tileCount(const rift_closure_src& src) {
 //           with m % 22 < 16), N = 32, K = 9 taps x 2 steps of 16 over the
 //           four 8-channel planes of the layer-1 activations.
 // Tensor memory: 128 columns, one 32-column accumulator per M tile (layer 2
-// reuses the columns of layer 1 once its epilogue has read them).
+// reuses the columns of layer 1 once its epilogue has read them).  A CTA
+// holds 74 KB of shared memory and 80 registers per thread, so three run on
+// an SM (384 of the 512 tensor-memory columns); the epilogues read the
+// accumulators 8 columns at a time to stay within the registers.
 constexpr int XBC = 640;             // BF16 input cells staged (reads reach m + 5*22 + 4 < 640)
 constexpr int A1C = 432;             // layer-1 cells kept per plane (layer 2 reads < 384 + 46)
 constexpr int M1TC = 4, M2TC = 3;    // M tiles of 128 rows
 constexpr int KS1 = 15, KS2 = 18;    // K steps of 16
-constexpr int NTAPT = 30;            // layer-1 taps incl. the zero row dy = 5
+constexpr int NTAPT = 26;            // layer-1 weight blocks: the 25 taps, then one of zeros
 constexpr uint32_t TMEM_COLS = 128;
 constexpr uint32_t A1PLANE = A1C * 16;  // bytes per 8-channel plane
 // instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B
@@ -388,9 +391,10 @@ constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 1
 struct __align__(128) TcSmem {
     uint16_t xb[XBC * 8];        // input cells (BF16 x 8), zero past the 22 x 22 block
     uint16_t a1[4][A1C * 8];     // layer-1 activations, channels 8p..8p+7 in plane p
-    uint16_t w1t[NTAPT * 32 * 8];  // [tap][o][c8], tap 2s + h = (2(s/5) + h, s%5)
+    uint16_t w1t[NTAPT * 32 * 8];  // [dy*5 + dx][o][c8]; block 25 all zero
     uint16_t w2t[36 * 32 * 8];   // [tap*4 + c/8][o][c%8]
-    float xs[NRI * CIN];         // scaled FP32 inputs, channels last
+    float xh[NRI];               // scaled FP32 depth of the input cells
+    float xbed[NRI];             // scaled FP32 bed of the input cells
     float w3[COUT][C1];
     float b1[C1], b2[C1], b3[COUT], sbed[C1];
     float bref;
@@ -463,15 +467,27 @@ __device__ __forceinline__ void tc_ld32(uint32_t taddr, float v[32]) {
     for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
 }
 
+// 8 consecutive FP32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tc_ld8(uint32_t taddr, float v[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = __uint_as_float(r[k]);
+}
+
 // Weights in the operand layouts, biases, the bed-weight sums; the zero pad
 // of the input cells.  Tensor memory (warp 0) and the completion barrier.
 __device__ void tcSetup(TcSmem& S, const float* __restrict__ P) {
     const int tid = threadIdx.x;
     constexpr int MAP[CB] = {0, 1, 2, 3, 3, 4, 5, -1};
     for (int i = tid; i < NTAPT * 32 * 8; i += NT) {
-        const int T = i / 256, o = (i / 8) % 32, c8 = i % 8;
-        const int s = T >> 1, dy = 2 * (s / 5) + (T & 1), dx = s % 5, c = MAP[c8];
-        S.w1t[i] = bf(dy < 5 && c >= 0 ? P[OFF_W1 + o * K1P + (dy * 5 + dx) * CIN + c] : 0.f);
+        const int T = i / 256, o = (i / 8) % 32, c8 = i % 8, c = MAP[c8];
+        S.w1t[i] = bf(T < 25 && c >= 0 ? P[OFF_W1 + o * K1P + T * CIN + c] : 0.f);
     }
     for (int i = tid; i < 36 * 32 * 8; i += NT) {
         const int blk = i / 256, o = (i / 8) % 32, c8 = i % 8;
@@ -546,10 +562,9 @@ __device__ void tcStoreInput(TcSmem& S, const TcInput& R, const rift_closure_src
         if (i >= NRI) break;
         float v[CIN];
 #pragma unroll
-        for (int c = 0; c < CIN; c++) {
-            v[c] = R.v[k][c] * src.scale[c];
-            S.xs[i * CIN + c] = v[c];
-        }
+        for (int c = 0; c < CIN; c++) v[c] = R.v[k][c] * src.scale[c];
+        S.xh[i] = v[0];
+        S.xbed[i] = v[3];
         const float br = v[3] - bref;
         const uint16_t bh = bf(br);
         const uint16_t bl = bf(br - fb(bh));
@@ -570,13 +585,17 @@ __device__ void tcStoreInput(TcSmem& S, const TcInput& R, const rift_closure_src
 // of the field), so the issuing thread spends a few instructions per MMA.
 __device__ void tcIssue1(const TcSmem& S, uint32_t tmem) {
     tc_after_sync();
-    const uint64_t a0 = sdesc(saddr(S.xb), RI * 16, 128), b0 = sdesc(saddr(S.w1t), 512, 128);
+    // B: the K chunks of step s are taps (dy, dx) and (dy + 1, dx), dy = 2(s/5), five weight
+    // blocks apart; for dy = 4 the second chunk is the zero block
+    const uint64_t a0 = sdesc(saddr(S.xb), RI * 16, 128), b0 = sdesc(saddr(S.w1t), 0, 128);
 #pragma unroll
     for (int mt = 0; mt < M1TC; mt++)
 #pragma unroll
         for (int s = 0; s < KS1; s++) {
             const uint32_t cell = mt * 128 + (s / 5) * 2 * RI + s % 5;  // 16-byte cells
-            tc_mma(tmem + mt * 32, a0 + cell, b0 + s * (1024 / 16), s > 0);
+            const uint32_t T0 = (s / 5) * 10 + s % 5, T1 = s < 10 ? T0 + 5 : 25;
+            const uint64_t lbo = (uint64_t)((T1 - T0) * 512 / 16) << 16;
+            tc_mma(tmem + mt * 32, a0 + cell, b0 + T0 * (512 / 16) + lbo, s > 0);
         }
     tc_commit(const_cast<uint64_t*>(&S.bar));
 }
@@ -615,20 +634,20 @@ __device__ void tcEpilogue1(TcSmem& S, uint32_t tmem) {
     const float bref = S.bref;
 #pragma unroll 1
     for (int mt = warp >> 2; mt < M1TC; mt += 2) {
-        float v[32];
-        tc_ld32(tmem + ((uint32_t)(32 * lg) << 16) + mt * 32, v);
         const int m = mt * 128 + 32 * lg + lane;
-        if (m >= A1C) continue;
-        const float cb = S.xs[(m + 2 * RI + 2) * CIN + 3] - bref;
+        const float cb = S.xbed[min(m, A1C - 1) + 2 * RI + 2] - bref;
 #pragma unroll
-        for (int p = 0; p < 4; p++) {
+        for (int p = 0; p < 4; p++) {  // 8 channels (one plane) at a time
+            float v[8];
+            tc_ld8(tmem + ((uint32_t)(32 * lg) << 16) + mt * 32 + 8 * p, v);
+            if (m >= A1C) continue;
             uint4 w;
             uint32_t q[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 const int o = 8 * p + 2 * e;
-                q[e] = pack2(relu(v[o] + S.b1[o] - cb * S.sbed[o]),
-                             relu(v[o + 1] + S.b1[o + 1] - cb * S.sbed[o + 1]));
+                q[e] = pack2(relu(v[2 * e] + S.b1[o] - cb * S.sbed[o]),
+                             relu(v[2 * e + 1] + S.b1[o + 1] - cb * S.sbed[o + 1]));
             }
             w.x = q[0];
             w.y = q[1];
@@ -646,19 +665,21 @@ __device__ void tcEpilogue1(TcSmem& S, uint32_t tmem) {
 // the 16 x 16 tile (oy*16 + ox), or -1 for a row that is not an output.
 __device__ int tcOutputs(const TcSmem& S, uint32_t tmem, int mt, float out[COUT]) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, lg = warp & 3;
-    float v[32];
-    tc_ld32(tmem + ((uint32_t)(32 * lg) << 16) + mt * 32, v);
     const int m = mt * 128 + 32 * lg + lane, oy = m / RI, ox = m % RI;
-    if (oy >= OT || ox >= OT) return -1;
 #pragma unroll
     for (int c = 0; c < COUT; c++) out[c] = S.b3[c];
 #pragma unroll
-    for (int k = 0; k < C1; k++) {
-        const float a = relu(v[k] + S.b2[k]);
+    for (int q = 0; q < 4; q++) {  // 8 channels at a time
+        float v[8];
+        tc_ld8(tmem + ((uint32_t)(32 * lg) << 16) + mt * 32 + 8 * q, v);
 #pragma unroll
-        for (int c = 0; c < COUT; c++) out[c] = fmaf(S.w3[c][k], a, out[c]);
+        for (int k = 0; k < 8; k++) {
+            const float a = relu(v[k] + S.b2[8 * q + k]);
+#pragma unroll
+            for (int c = 0; c < COUT; c++) out[c] = fmaf(S.w3[c][8 * q + k], a, out[c]);
+        }
     }
-    return oy * OT + ox;
+    return (oy >= OT || ox >= OT) ? -1 : oy * OT + ox;
 }
 
 // One tcgen05.mma (M 128, N 32, K 16) on fixed BF16 values, with the
@@ -723,7 +744,7 @@ __global__ void __launch_bounds__(128) k_tc_selftest(float* __restrict__ out) {
 
 // ------------------------------------------------------------------ forward
 // Raw net outputs of every output cell of src.
-__global__ void __launch_bounds__(NT, 2) k_forward(rift_closure_src src, const float* __restrict__ P,
+__global__ void __launch_bounds__(NT, 3) k_forward(rift_closure_src src, const float* __restrict__ P,
                                                    float* __restrict__ out) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
@@ -1118,7 +1139,7 @@ struct ApplyArgs {
 
 // Net outputs -> gated, limited face corrections of every 16 x 16 block of
 // interior cells (zeros for dry blocks and blocks that fall back).
-__global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
+__global__ void __launch_bounds__(NT, 3) k_closure(ApplyArgs A) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
     const rift_closure_src& src = A.src;
@@ -1146,7 +1167,7 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
         int wet = 0;
         for (int i = tid; i < (OT + 1) * (OT + 1); i += NT) {
             int ry = 3 + i / (OT + 1), rx = 3 + i % (OT + 1);
-            wet |= S.xs[(ry * RI + rx) * CIN] > hminS;
+            wet |= S.xh[ry * RI + rx] > hminS;
         }
         if (!__syncthreads_or(wet)) {
             if (tid == 0) A.fell[tile] = 0;
@@ -1180,13 +1201,13 @@ __global__ void __launch_bounds__(NT, 2) k_closure(ApplyArgs A) {
             const int oy = q / OT, ox = q % OT, y = G.Y + oy, x = G.X + ox;
             if (y - src.oy0 >= src.OH || x - src.ox0 >= src.OW) continue;
             cell[k] = q;
-            const float hc = S.xs[((oy + 3) * RI + ox + 3) * CIN] * invS0;
+            const float hc = S.xh[(oy + 3) * RI + ox + 3] * invS0;
 #pragma unroll
             for (int f = 0; f < 2; f++) {
                 const bool east = f == 0;
                 const float inv = east ? A.inv_dx : A.inv_dy;
                 const int yn = east ? y : y + 1, xn = east ? x + 1 : x;
-                const float hn = S.xs[((oy + 3 + (east ? 0 : 1)) * RI + ox + 3 + (east ? 1 : 0)) * CIN] * invS0;
+                const float hn = S.xh[(oy + 3 + (east ? 0 : 1)) * RI + ox + 3 + (east ? 1 : 0)] * invS0;
                 const bool ok = x >= 3 && y >= 3 && xn <= A.nx - 4 && yn <= A.ny - 4 && hc > A.hmin &&
                                 hn > A.hmin;
                 float vm = ok ? o[2 * f] * A.osc[2 * f] : 0.f;
@@ -1285,7 +1306,7 @@ int residentGrid(const void* k, size_t smem, int tiles, int* out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // the whole shared-memory carveout, so that the occupancy below (and the
-    // launch) can place two 85 KB CTAs on an SM
+    // launch) can place three 74 KB tensor-core CTAs on an SM
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
@@ -1293,8 +1314,8 @@ int residentGrid(const void* k, size_t smem, int tiles, int* out) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, rc::NT, smem);
     if (e != cudaSuccess || occ < 1) return fail(RIFT_ERR_CUDA, "closure kernel does not fit an SM");
     // The same count from the SM's own limits (the occupancy call above gave
-    // one CTA per SM for the 85 KB tensor-core kernels on GB300, where two
-    // fit in shared memory and registers): CTAs per SM by shared memory (with
+    // one CTA per SM for an 85 KB tensor-core kernel on GB300, where two fit
+    // in shared memory and registers): CTAs per SM by shared memory (with
     // the per-block reservation) and by registers (allocated per warp in
     // units of 256), at most 4 (4 x 128 tensor-memory columns).  The kernels
     // loop over tiles with no CTA waiting on another, so a CTA that does not
