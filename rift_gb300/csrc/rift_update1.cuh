@@ -39,6 +39,10 @@ template <bool RAIN>
 __host__ __device__ constexpr uint32_t u1SmemBytes() {
     return UNSLOT * u1SlotBytes<RAIN>() + 128;  // + barriers and tile tables
 }
+static_assert(u1SlotBytes<true>() >= U1_OFF_R1 + U1PLANE && u1SlotBytes<false>() >= U1_OFF_N + U1PLANE &&
+                  u1SlotBytes<true>() % 128 == 0 && u1SlotBytes<false>() % 128 == 0,
+              "slot sizes");
+static_assert(UNSLOT * 8 + 2 * STRIP_TX * 4 + 16 <= 128, "barriers and tile tables after the ring");
 
 // Tensor maps of the staged planes (116 x 7-row boxes).
 struct U1Maps {
