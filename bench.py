@@ -654,7 +654,8 @@ def run_closure(args):
             bc_of[id(sim)] = sim.field("BC")
             if mode == "closure":
                 cr = closure.ClosureRun(sim, model, every=args.closure_every, gain=args.closure_gain,
-                                        fine=fc if args.fine_fallback else None)
+                                        fine=fc if args.fine_fallback else None,
+                                        fine_batch=args.fine_batch)
                 w, arr = _timed_chunks(cr.run, args.tf, 120.0, lambda: interior_depth(sim))
                 res["closure_blocks"], res["closure_fallback_blocks"] = cr.block_counts()
                 res["closure_applies"] = cr.applies
@@ -689,6 +690,7 @@ def run_closure(args):
                        "train_grid": f"{args.closure_train_N}^2 at 2 m", "train_patches": n_patches,
                        "train_steps": args.train_steps, "batch": 256, "closure_every_steps": args.closure_every,
                        "closure_gain": args.closure_gain,
+                       "fallback_batched": args.fine_fallback and args.fine_batch,
                        "fallback": "fine-grid re-solve of the block" if args.fine_fallback
                        else "plain coarse solve of the block",
                        "eval_scenarios": args.eval_seeds},
@@ -722,6 +724,9 @@ def main():
     ap.add_argument("--no-fine-fallback", dest="fine_fallback", action="store_false",
                     help="config 4: blocks that fall back keep the plain coarse solve instead of "
                          "a fine-grid re-solve")
+    ap.add_argument("--no-fine-batch", dest="fine_batch", action="store_false",
+                    help="config 4: re-solve fallen-back blocks one patch run after another "
+                         "instead of one ensemble launch per interval")
     ap.add_argument("--closure-gain", type=float, default=0.25,
                     help="config 4: strength of the applied corrections (chosen on scenario 100000)")
     ap.add_argument("--members", type=int, default=32, help="config 5: ensemble members")

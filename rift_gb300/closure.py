@@ -515,11 +515,15 @@ class FineFallback:
     fine depths are scaled to it over the wet cells), so the run stays
     conservative, and wet and dry cells keep their status, which the engine's
     tile activity requires; cells next to the domain edge keep the coarse
-    values.  The halo absorbs the patch's own open edges over the interval."""
+    values.  The halo absorbs the patch's own open edges over the interval.
+    With `batch`, the patches of an interval run to t1 together as members of
+    one ensemble launch (up to `cache` of them per launch)."""
 
-    def __init__(self, coarse_sim: capi.Sim, fine: synth.Case, halo=4, max_blocks=256, cache=64):
+    def __init__(self, coarse_sim: capi.Sim, fine: synth.Case, halo=4, max_blocks=256, cache=64,
+                 batch=True):
         self.sim, self.fine, self.halo = coarse_sim, fine, halo
-        self.max_blocks, self.cache = max_blocks, cache
+        self.max_blocks, self.cache, self.batch = max_blocks, cache, batch
+        self.ensembles = 0  # ensemble launches that re-solved a group of patches
         self.patches = {}   # block -> (Sim, BC of the patch)
         self.refined = 0    # blocks re-solved so far
         self.skipped = 0    # fallen-back blocks beyond max_blocks in one interval
@@ -556,44 +560,63 @@ class FineFallback:
         torch.cuda.synchronize()
         cur = [p[:ny, :nx].cpu().numpy() for p in planes]
         eps = 1.19209e-07
-        for b in blocks:
-            by, bx = divmod(int(b), tx)
-            j0, i0 = 2 + BLOCK * by, 2 + BLOCK * bx
-            j1, i1 = min(j0 + BLOCK, ny - 2), min(i0 + BLOCK, nx - 2)
-            Ja, Jb = patch_range(j0, j1, self.halo, ny)
-            Ia, Ib = patch_range(i0, i1, self.halo, nx)
-            psim, pbc = self._patch((j0, i0), Ja, Jb, Ia, Ib)
-            # the coarse state at t0 on the fine cells of the patch
-            hf = np.zeros(pbc.shape)
-            huf, hvf = np.zeros(pbc.shape), np.zeros(pbc.shape)
-            for a, src in ((hf, u0[0]), (huf, u0[1]), (hvf, u0[2])):
-                blk = src[Ja:Jb, Ia:Ib].astype(np.float64)
-                a[2:-2, 2:-2] = np.repeat(np.repeat(blk, 2, axis=0), 2, axis=1)
-            hf = np.maximum(hf, 0.0)
-            n_bx, n_by = psim.nBX, psim.nBY
-            psim.set_state(t0, dt0, pbc + hf, huf, hvf, wet=np.ones(n_bx * n_by, np.uint8),
-                           active=np.arange(n_bx * n_by, dtype=np.int32))
-            psim.run(2 ** 31 - 1, t1)
-            hp = (psim.field("W") - pbc)[2:-2, 2:-2]
-            up, vp = psim.field("HU")[2:-2, 2:-2], psim.field("HV")[2:-2, 2:-2]
-            # the block's cells in the patch, 2x2 means; the edge cells of the
-            # domain keep the coarse values
-            r0, c0 = 2 * (j0 - Ja), 2 * (i0 - Ia)
-            sl = (slice(r0, r0 + 2 * (j1 - j0)), slice(c0, c0 + 2 * (i1 - i0)))
-            Hf, Uf, Vf = restrict(hp[sl]), restrict(up[sl]), restrict(vp[sl])
-            jj, ii = np.mgrid[j0:j1, i0:i1]
-            keep = (jj >= 3) & (jj <= ny - 4) & (ii >= 3) & (ii <= nx - 4)
-            Hc = cur[0][j0:j1, i0:i1].astype(np.float64)
-            wet = (Hc > eps) & keep
-            Hn = np.where(wet, np.maximum(Hf, 2 * eps), Hc)
-            vol_c, vol_f = Hc[wet].sum(), Hn[wet].sum()
-            if vol_f > 0:
-                Hn[wet] *= vol_c / vol_f
-                Hn[wet] = np.maximum(Hn[wet], 2 * eps)
-            cur[0][j0:j1, i0:i1] = np.where(wet, Hn, Hc).astype(np.float32)
-            cur[1][j0:j1, i0:i1] = np.where(wet, Uf, cur[1][j0:j1, i0:i1]).astype(np.float32)
-            cur[2][j0:j1, i0:i1] = np.where(wet, Vf, cur[2][j0:j1, i0:i1]).astype(np.float32)
-            self.refined += 1
+        # groups of at most `cache` blocks, so that no patch of a group is
+        # evicted while the group runs
+        group = max(1, self.cache)
+        for g0 in range(0, len(blocks), group):
+            work = []
+            for b in blocks[g0:g0 + group]:
+                by, bx = divmod(int(b), tx)
+                j0, i0 = 2 + BLOCK * by, 2 + BLOCK * bx
+                j1, i1 = min(j0 + BLOCK, ny - 2), min(i0 + BLOCK, nx - 2)
+                Ja, Jb = patch_range(j0, j1, self.halo, ny)
+                Ia, Ib = patch_range(i0, i1, self.halo, nx)
+                psim, pbc = self._patch((j0, i0), Ja, Jb, Ia, Ib)
+                # the coarse state at t0 on the fine cells of the patch
+                hf = np.zeros(pbc.shape)
+                huf, hvf = np.zeros(pbc.shape), np.zeros(pbc.shape)
+                for a, src in ((hf, u0[0]), (huf, u0[1]), (hvf, u0[2])):
+                    blk = src[Ja:Jb, Ia:Ib].astype(np.float64)
+                    a[2:-2, 2:-2] = np.repeat(np.repeat(blk, 2, axis=0), 2, axis=1)
+                hf = np.maximum(hf, 0.0)
+                n_bx, n_by = psim.nBX, psim.nBY
+                psim.set_state(t0, dt0, pbc + hf, huf, hvf, wet=np.ones(n_bx * n_by, np.uint8),
+                               active=np.arange(n_bx * n_by, dtype=np.int32))
+                work.append((psim, pbc, j0, i0, j1, i1, Ja, Ia))
+            if self.batch and len(work) > 1:
+                # every patch of the group to t1 in one ensemble launch, each
+                # with its own dt (the ensemble kernel), instead of one patch
+                # run after another
+                ens = capi.Ensemble([w[0] for w in work])
+                try:
+                    ens.run(t_stop=t1)
+                finally:
+                    ens.close()
+                self.ensembles += 1
+            else:
+                for w in work:
+                    w[0].run(2 ** 31 - 1, t1)
+            for psim, pbc, j0, i0, j1, i1, Ja, Ia in work:
+                hp = (psim.field("W") - pbc)[2:-2, 2:-2]
+                up, vp = psim.field("HU")[2:-2, 2:-2], psim.field("HV")[2:-2, 2:-2]
+                # the block's cells in the patch, 2x2 means; the edge cells of
+                # the domain keep the coarse values
+                r0, c0 = 2 * (j0 - Ja), 2 * (i0 - Ia)
+                sl = (slice(r0, r0 + 2 * (j1 - j0)), slice(c0, c0 + 2 * (i1 - i0)))
+                Hf, Uf, Vf = restrict(hp[sl]), restrict(up[sl]), restrict(vp[sl])
+                jj, ii = np.mgrid[j0:j1, i0:i1]
+                keep = (jj >= 3) & (jj <= ny - 4) & (ii >= 3) & (ii <= nx - 4)
+                Hc = cur[0][j0:j1, i0:i1].astype(np.float64)
+                wet = (Hc > eps) & keep
+                Hn = np.where(wet, np.maximum(Hf, 2 * eps), Hc)
+                vol_c, vol_f = Hc[wet].sum(), Hn[wet].sum()
+                if vol_f > 0:
+                    Hn[wet] *= vol_c / vol_f
+                    Hn[wet] = np.maximum(Hn[wet], 2 * eps)
+                cur[0][j0:j1, i0:i1] = np.where(wet, Hn, Hc).astype(np.float32)
+                cur[1][j0:j1, i0:i1] = np.where(wet, Uf, cur[1][j0:j1, i0:i1]).astype(np.float32)
+                cur[2][j0:j1, i0:i1] = np.where(wet, Vf, cur[2][j0:j1, i0:i1]).astype(np.float32)
+                self.refined += 1
         for p, c in zip(planes, cur):
             p[:ny, :nx].copy_(torch.as_tensor(c, device="cuda"))
         torch.cuda.synchronize()
@@ -623,11 +646,12 @@ class ClosureRun:
     coarse solve."""
 
     def __init__(self, sim: capi.Sim, model: Model, every=4, hmin=0.01, lim=0.2, tau=0.5, gain=1.0,
-                 fine: synth.Case | None = None, halo=4):
+                 fine: synth.Case | None = None, halo=4, fine_batch=True):
         torch = _torch()
         self.sim, self.model = sim, model
         self.every, self.hmin, self.lim, self.tau = every, hmin, lim, tau
-        self.fallback = FineFallback(sim, fine, halo=halo) if fine is not None else None
+        self.fallback = (FineFallback(sim, fine, halo=halo, batch=fine_batch)
+                         if fine is not None else None)
         v = sim.device_view()
         self.view = v
         rows, pitch = v.rows, v.pitch

@@ -464,10 +464,12 @@ def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
     after 300 s of rain, and a block whose only deep cells sit on the domain
     edge corrects no face) and is re-solved from the coarse state at the
     interval's start on a fine patch (block + 4 coarse cells of halo, 2 m
-    cells under 4 m ones).  The re-solve keeps each block's volume, keeps wet and dry cells as
-    they were, changes the wet cells of the blocks, and leaves the edge cells
-    of the domain alone; a run with the fallback on stays finite and its mass
-    ledger closes."""
+    cells under 4 m ones).  The patches run together in ensemble launches and
+    end where they end run one after another (within 1e-4).  The re-solve
+    keeps each block's volume, keeps wet and dry cells as they were, changes
+    the wet cells of the blocks, and leaves the edge cells of the domain
+    alone; a run with the fallback on stays finite and its mass ledger
+    closes."""
     fine = closure.scenario(6, N=256, cell=2.0, tf=900.0)  # rimmed plane with bumps
     cc = closure.coarse_case(fine)
     sim = capi.Sim(cc).setup()
@@ -486,9 +488,24 @@ def test_fine_fallback_resolves_blocks_on_the_fine_grid(torch):
     assert int(fell.sum()) == fallen and 8 <= fallen <= evaluated, (evaluated, fallen)
     h1 = sim.field("W") - bc
     v1 = sim.volume()
+    v = run.view
+    planes = [closure._device_plane(p, v) for p in (v.h, v.hu, v.hv)]
+    before = [p[:v.h_ny, :v.h_nx].clone() for p in planes]
     n = run.fallback.refine(fell, u0, t0, t1, 0.5 * dt0)
     assert n == fallen and run.fallback.refined == n
+    assert run.fallback.ensembles >= 1  # the patches ran together in ensemble launches
     h2 = sim.field("W") - bc
+    # the same re-solve with one patch run after another ends in the same state
+    after = [p[:v.h_ny, :v.h_nx].clone() for p in planes]
+    for p, b in zip(planes, before):
+        p[:v.h_ny, :v.h_nx].copy_(b)
+    one_by_one = closure.FineFallback(sim, fine, batch=False)
+    assert one_by_one.refine(fell, u0, t0, t1, 0.5 * dt0) == n and one_by_one.ensembles == 0
+    for p, a in zip(planes, after):
+        assert (p[:v.h_ny, :v.h_nx] - a).abs().max().item() <= 1e-4
+        p[:v.h_ny, :v.h_nx].copy_(a)
+    torch.cuda.synchronize()
+    one_by_one.close()
     v2 = sim.volume()
     assert abs(v2 - v1) <= 1e-6 * v1, (v1, v2)
     eps = 1.19209e-07
