@@ -126,7 +126,9 @@ int rift_closure_apply(const rift_device_view* view, const rift_closure_src* src
  * tensor-core kernels: RIFT_ERR_CUDA when a completion wait of one of them
  * gave up (its tile's outputs are then missing), else RIFT_OK.  The status
  * is one flag per device for the whole process, so a check after one
- * stream's launches also reports a give-up in kernels of another stream. */
+ * stream's launches also reports a give-up in kernels of another stream.
+ * While the flag is set, rift_closure_apply changes no state (the step keeps
+ * the plain solve). */
 int rift_closure_check(void* stream);
 
 /* One tensor-core MMA (128 x 32 x 16, BF16 in, FP32 out) on fixed values in
